@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark of the GFAz transform hot path on GB300.
+
+A step is one pass of the path over the chromosome-scale workload: seeded
+synthetic graph of the cfg2 shape (90 haplotype P-lines of ~5.7M steps,
+~513M int32 steps, ~4.5 GB of P-line text), compressed on the GPU (delta
+coding + 8 grammar rounds) and decompressed again (expansion + inverse
+delta + P-line text emission).
+
+  value  GB/s of GFA P-line text per (compress + decompress) step, inputs
+         resident in HBM, text left in HBM, CUDA events on the library's
+         stream; total over all ranks.
+  e2e    the same through the C ABI with host buffers: pinned host steps in,
+         encoded stream + rulebook out to the host (what the entropy stage
+         consumes), loaded back from the host and decoded to pinned host
+         text; every copy inside the timed region.
+
+`--impl reference` times the reference algorithm's CPU implementation on
+the host cores (the oracle port: the reference is not built on the GPU
+host), on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): independent replicas, one per rank (the transform has
+no cross-rank exchange); a barrier and the max over ranks bracket the timed
+region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GFA GB/s compress+decompress, batched vs plain GPU vs CPU; extract p50/p99 ms"
+UNIT = "GB/s"
+HBM_FALLBACK = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the cfg2 workload (testing)")
+    ap.add_argument("--cpu-sample-paths", type=int, default=12)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(scale: float):
+    from gfaz_gb300 import synthetic
+    n_paths = max(2, int(round(90 * min(1.0, scale * 4)))) if scale < 1 else 90
+    nseg = int(8_000_000 * scale) if scale < 1 else 8_000_000
+    steps, off, nseg = synthetic.cfg2_stream(seed=2, n_segments=max(nseg, 10_000), n_paths=n_paths)
+    return steps, off, nseg
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", HBM_FALLBACK)), "measured"
+    return HBM_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_cpu_port(steps, off, sample_paths, threads):
+    """Times the oracle port (reference algorithm on the CPU) on the first
+    `sample_paths` traversals; returns (GB/s, seconds, text bytes, sample)."""
+    from oracle import oracle
+    k = min(sample_paths, len(off) - 1)
+    s = steps[:int(off[k])]
+    o = off[:k + 1].copy()
+    oracle.lib()
+    t0 = time.perf_counter()
+    nbytes, _, _ = oracle.roundtrip_p(s, o, 8, 1, threads)
+    dt = time.perf_counter() - t0
+    return nbytes / dt / 1e9, dt, nbytes, f"{k} of {len(off) - 1} P-lines ({int(o[-1])} steps)"
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return 0
+    steps, off, _ = workload(args.scale)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        run_cpu_port(steps, off, args.cpu_sample_paths, threads)
+    vals, secs = [], []
+    nbytes, sample = 0, ""
+    for _ in range(args.steps):
+        v, dt, nbytes, sample = run_cpu_port(steps, off, args.cpu_sample_paths, threads)
+        vals.append(v)
+        secs.append(dt)
+    value = nbytes * len(secs) / sum(secs) / 1e9
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic (seeded cfg2-shape generator)",
+           "config": {"workload": "chromosome-scale cfg2: 90 P-lines x ~5.7M steps; CPU sample per step",
+                      "rounds": 8, "delta_round": 1, "threshold": 2},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": sample + " per step; oracle/gfaz_oracle.c (OpenMP), reference CLI "
+                                               "not buildable on the GPU host"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import gfaz_gb300 as gz
+
+    ws, rank, local = dist_init()
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    steps, off, nseg = workload(args.scale)
+    ntrav = len(off) - 1
+    names = [f"hap{i}" for i in range(ntrav)]
+    overlaps = ["*"] * ntrav
+
+    stream = torch.cuda.Stream(device=dev)
+    ctx = gz.Context(local, stream.cuda_stream)
+    d_steps = torch.from_numpy(steps).to(dev)
+    torch.cuda.synchronize()
+
+    def step():
+        g = gz.encode(None, off, rounds=8, delta_round=1, ctx=ctx, device_ptr=d_steps.data_ptr())
+        n = g.decode_text(0, ntrav, names=names, overlaps=overlaps)
+        return g, n
+
+    for _ in range(args.warmup):
+        g, text_bytes = step()
+        del g
+    # parity: decode(encode(x)) == x on the device-resident input
+    g, text_bytes = step()
+    x, xoff = g.decode()
+    parity_ok = bool(np.array_equal(xoff, off) and np.array_equal(x, steps))
+    ginfo = g.info()
+    del g, x
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    ctx.set_timing(True)
+    ctx.kernel_stats(reset=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    with torch.cuda.stream(stream):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            ev[3 * i].record(stream)
+            g = gz.encode(None, off, rounds=8, delta_round=1, ctx=ctx, device_ptr=d_steps.data_ptr())
+            ev[3 * i + 1].record(stream)
+            g.decode_text(0, ntrav, names=names, overlaps=overlaps)
+            ev[3 * i + 2].record(stream)
+            del g
+        t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    comp_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
+    dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
+    kstats = ctx.kernel_stats(reset=True)
+    ctx.set_timing(False)
+    launches = int(kstats.pop("_launches", 0)) // max(1, args.steps)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * text_bytes / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (algorithmic bytes / measured time)
+    peak, peak_kind = peaks()
+    top = max(kstats.items(), key=lambda kv: kv[1]["ms"])
+    kname, kst = top
+    achieved = kst["bytes"] / (kst["ms"] / 1e3) / 1e9 if kst["ms"] > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            tj = json.load(fh)
+        if kname in tj and tj[kname].get("bytes_per_algorithmic_byte"):
+            traffic = tj[kname]["bytes_per_algorithmic_byte"] * kst["bytes"] / max(1, kst["launches"])
+    kernels = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                   "gbps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None}
+               for k, v in sorted(kstats.items(), key=lambda kv: -kv[1]["ms"])}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_steps = torch.from_numpy(steps).pin_memory()
+        rules_cap = max(1, ginfo["num_rules"] * 2 + 1024)
+        h_enc = torch.empty(max(1, int(ginfo["encoded_len"] * 1.5) + 1024), dtype=torch.int32).pin_memory()
+        h_f = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
+        h_s = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
+        h_text = torch.empty(int(text_bytes * 1.1) + 4096, dtype=torch.uint8).pin_memory()
+
+        import ctypes
+        from gfaz_gb300._ffi import lib as L, check
+
+        def e2e_step():
+            h = ctypes.c_void_p()
+            offa = np.ascontiguousarray(off, np.uint64)
+            check(L().gfz_encode(ctx.handle, ctypes.c_void_p(h_steps.data_ptr()), offa.ctypes.data, ntrav, 8, 2, 1,
+                                 gz.WHERE_HOST, ctypes.byref(h)))
+            g = gz.Grammar(h, ctx)
+            info = g.info()
+            eoff = np.zeros(ntrav + 1, np.uint64)
+            check(L().gfz_grammar_copy(ctx.handle, g.handle, ctypes.c_void_p(h_enc.data_ptr()), eoff.ctypes.data,
+                                       None, gz.WHERE_HOST))
+            check(L().gfz_grammar_rule_columns(ctx.handle, g.handle, ctypes.c_void_p(h_f.data_ptr()),
+                                               ctypes.c_void_p(h_s.data_ptr()), gz.WHERE_HOST))
+            del g
+            h2 = ctypes.c_void_p()
+            check(L().gfz_grammar_load(ctx.handle, ctypes.c_void_p(h_enc.data_ptr()), eoff.ctypes.data, ntrav,
+                                       ctypes.c_void_p(h_f.data_ptr()), ctypes.c_void_p(h_s.data_ptr()),
+                                       info["num_rules"], info["layer_start"], 1, gz.WHERE_HOST, ctypes.byref(h2)))
+            g2 = gz.Grammar(h2, ctx)
+            n = g2.decode_text(0, ntrav, names=names, overlaps=overlaps, out_ptr=h_text.data_ptr(),
+                               cap=h_text.numel(), where=gz.WHERE_HOST)
+            del g2
+            return info, n
+
+        for _ in range(max(1, args.warmup // 2)):
+            info, n = e2e_step()
+        k2 = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        w0 = time.perf_counter()
+        for _ in range(k2):
+            info, n = e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - w0) / k2
+        ev_ms = a.elapsed_time(b) / k2
+        e2e_ms = max(ev_ms, wall * 1e3)
+        e2e_text = bytes(h_text[:min(n, 64)].numpy().tobytes())
+        h2d = 4 * len(steps) + 4 * info["encoded_len"] + 8 * info["num_rules"] + 8 * (ntrav + 1) * 2
+        d2h = 4 * info["encoded_len"] + 8 * info["num_rules"] + n
+        e2e = {"value": ws * n / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+               "text_head_ok": e2e_text.startswith(b"P\thap0\t")}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        v, dt, nb, sample = run_cpu_port(steps, off, args.cpu_sample_paths, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s "
+                         "(oracle/gfaz_oracle.c, OpenMP)"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded cfg2-shape generator; published datasets unavailable)",
+        "config": {"workload": "chromosome-scale cfg2: 90 P-lines, %d steps, %d segments" % (len(steps), nseg),
+                   "rounds": 8, "delta_round": 1, "threshold": 2, "text_bytes_per_replica": int(text_bytes),
+                   "encoded_len": int(ginfo["encoded_len"]), "rules": int(ginfo["num_rules"]),
+                   "rounds_done": int(ginfo["rounds_done"]),
+                   "l2": "inputs larger than L2 (%.2f GB stream per step)" % (4 * len(steps) / 1e9),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "compress_gbps": ws * text_bytes / (comp_ms / 1e3) / 1e9,
+        "decompress_gbps": ws * text_bytes / (dec_ms / 1e3) / 1e9,
+        "compress_ms": comp_ms, "decompress_ms": dec_ms,
+        "parity": "decode(encode(x)) == x: %s" % ("exact" if parity_ok else "MISMATCH"),
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic},
+        "kernels": kernels,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0 if parity_ok else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())

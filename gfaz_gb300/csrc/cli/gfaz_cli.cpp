@@ -1,0 +1,244 @@
+// gfaz - command-line front end of the GB300 GFAz build, written purely
+// against the C ABI (include/gfaz_gb300.h).
+//
+// Commands, options, default output names and error behaviour follow the
+// reference CLI (src/cli/gfaz_cli.cpp, compress_command.cpp,
+// decompress_command.cpp, extract_path_command.cpp, extract_walk_command.cpp,
+// add_haplotypes_command.cpp): "Error: <message>" on stderr and exit code 1
+// on failure, extracted lines on stdout.  The transform always runs on the
+// GPU; --gpu is accepted for compatibility.
+#include <getopt.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "../../../include/gfaz_gb300.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+int fail(const char *what = nullptr) {
+  std::cerr << "Error: " << (what ? what : gfz_last_error()) << std::endl;
+  return 1;
+}
+
+void usage() {
+  std::cout << "gfaz - GFA Compression Tool (GB300 transform)\n\nUSAGE:\n"
+               "    gfaz compress [OPTIONS] <input.gfa> [output.gfaz]\n"
+               "    gfaz decompress [OPTIONS] <input.gfaz> [output.gfa]\n"
+               "    gfaz extract-path [OPTIONS] <input.gfaz> <path_name> [path_name ...]\n"
+               "    gfaz extract-walk [OPTIONS] <input.gfaz>\n"
+               "                      <sample_id> <hap_index> <seq_id> <seq_start> <seq_end> [...]\n"
+               "    gfaz add-haplotypes [OPTIONS] <input.gfaz> <paths_or_walks.gfa> [output.gfaz]\n\n"
+               "compress options: -r/--rounds N (8)  -d/--delta N (1)  -t/--threshold N (2)\n"
+               "                  -j/--threads N (0 = auto)  -g/--gpu  -s/--stats\n"
+               "other commands:   -j/--threads N\n";
+}
+
+long file_size(const std::string &p) {
+  FILE *f = std::fopen(p.c_str(), "rb");
+  if (!f) return 0;
+  std::fseek(f, 0, SEEK_END);
+  long n = std::ftell(f);
+  std::fclose(f);
+  return n;
+}
+
+int do_compress(int argc, char **argv) {
+  int rounds = 8, delta = 1, threshold = 2, threads = 0;
+  bool stats = false;
+  static struct option lo[] = {{"rounds", required_argument, 0, 'r'},    {"delta", required_argument, 0, 'd'},
+                               {"threshold", required_argument, 0, 't'}, {"threads", required_argument, 0, 'j'},
+                               {"gpu", no_argument, 0, 'g'},             {"stats", no_argument, 0, 's'},
+                               {"help", no_argument, 0, 'h'},            {0, 0, 0, 0}};
+  int opt;
+  optind = 1;
+  while ((opt = getopt_long(argc, argv, "r:d:t:j:gsh", lo, nullptr)) != -1) {
+    switch (opt) {
+      case 'r': rounds = std::atoi(optarg); break;
+      case 'd':
+        delta = std::atoi(optarg);
+        if (delta < 0) {
+          std::cerr << "Warning: --delta must be >= 0, clamping to 0" << std::endl;
+          delta = 0;
+        }
+        break;
+      case 't': threshold = std::atoi(optarg); break;
+      case 'j': threads = std::atoi(optarg); break;
+      case 'g': break;
+      case 's': stats = true; break;
+      case 'h': usage(); return 0;
+      default: usage(); return 1;
+    }
+  }
+  if (optind >= argc) {
+    std::cerr << "Error: No input file specified\n";
+    return 1;
+  }
+  const std::string in = argv[optind];
+  const std::string out = optind + 1 < argc ? argv[optind + 1] : in + ".gfaz";
+  std::cout << "=== GFAZ Compress ===\nInput:  " << in << "\nOutput: " << out << "\nBackend: GPU\nRounds: " << rounds
+            << "\nDelta:  " << delta << "\nThreshold: " << threshold << "\n\n";
+  const auto t0 = Clock::now();
+  gfz_compressed *c = nullptr;
+  if (gfz_compress_file(nullptr, in.c_str(), rounds, (uint64_t)threshold, delta, threads, stats ? 1 : 0, &c) != GFZ_OK)
+    return fail();
+  const gfz_status st = gfz_serialize(c, out.c_str());
+  gfz_compressed_free(c);
+  if (st != GFZ_OK) return fail();
+  const double s = std::chrono::duration<double>(Clock::now() - t0).count();
+  std::cout << "Compression complete!" << std::endl;
+  if (stats) {
+    const long a = file_size(in), b = file_size(out);
+    std::printf("Stats:\n  Time: %.3f s\n  Input: %ld B\n  Output: %ld B\n  Ratio: %.2fx\n  Throughput: %.2f MB/s\n", s,
+                a, b, b ? (double)a / b : 0.0, a / 1048576.0 / (s > 0 ? s : 1));
+  }
+  return 0;
+}
+
+int simple_opts(int argc, char **argv, int &threads, const char *shortopts) {
+  static struct option lo[] = {{"threads", required_argument, 0, 'j'}, {"gpu", no_argument, 0, 'g'},
+                               {"stats", no_argument, 0, 's'},         {"legacy", no_argument, 0, 'l'},
+                               {"help", no_argument, 0, 'h'},          {0, 0, 0, 0}};
+  int opt;
+  optind = 1;
+  while ((opt = getopt_long(argc, argv, shortopts, lo, nullptr)) != -1) {
+    switch (opt) {
+      case 'j': threads = std::atoi(optarg); break;
+      case 'g': case 's': case 'l': break;
+      case 'h': usage(); return 0;
+      default: usage(); return 1;
+    }
+  }
+  return -1;
+}
+
+int do_decompress(int argc, char **argv) {
+  int threads = 0;
+  if (int r = simple_opts(argc, argv, threads, "j:glsh"); r >= 0) return r;
+  if (optind >= argc) {
+    std::cerr << "Error: No input file specified\n";
+    return 1;
+  }
+  const std::string in = argv[optind];
+  std::string out;
+  if (optind + 1 < argc) out = argv[optind + 1];
+  else if (in.size() > 5 && in.substr(in.size() - 5) == ".gfaz") out = in.substr(0, in.size() - 5);
+  else out = in + ".decompressed";
+  std::cout << "=== GFAZ Decompress ===\nInput:  " << in << "\nOutput: " << out << "\n\n";
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(in.c_str(), &c) != GFZ_OK) return fail();
+  const gfz_status st = gfz_write_gfa(nullptr, c, out.c_str(), threads);
+  gfz_compressed_free(c);
+  if (st != GFZ_OK) return fail();
+  std::cout << "\nDecompression complete!" << std::endl;
+  return 0;
+}
+
+int print_and_free(gfz_status st, char *text, size_t len) {
+  if (st != GFZ_OK) return fail();
+  std::fwrite(text, 1, len, stdout);
+  gfz_free(text);
+  return 0;
+}
+
+int do_extract_path(int argc, char **argv) {
+  int threads = 0;
+  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (optind + 1 >= argc) {
+    std::cerr << "Error: Expected <input.gfaz> and at least one <path_name>\n";
+    return 1;
+  }
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(argv[optind], &c) != GFZ_OK) return fail();
+  std::vector<const char *> names(argv + optind + 1, argv + argc);
+  char *text = nullptr;
+  size_t len = 0;
+  const gfz_status st = gfz_extract_path_lines(nullptr, c, names.data(), names.size(), threads, &text, &len);
+  gfz_compressed_free(c);
+  return print_and_free(st, text, len);
+}
+
+int do_extract_walk(int argc, char **argv) {
+  int threads = 0;
+  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (optind + 5 >= argc) {
+    std::cerr << "Error: Expected <input.gfaz> and at least one walk identifier tuple\n";
+    return 1;
+  }
+  if ((argc - (optind + 1)) % 5 != 0) {
+    std::cerr << "Error: Walk identifiers must be provided in groups of 5: "
+                 "<sample_id> <hap_index> <seq_id> <seq_start> <seq_end>\n";
+    return 1;
+  }
+  std::vector<gfz_walk_key> keys;
+  try {
+    for (int i = optind + 1; i < argc; i += 5) {
+      gfz_walk_key k;
+      k.sample_id = argv[i];
+      k.hap_index = (uint32_t)std::stoul(argv[i + 1]);
+      k.seq_id = argv[i + 2];
+      k.seq_start = std::string(argv[i + 3]) == "*" ? -1 : std::stoll(argv[i + 3]);
+      k.seq_end = std::string(argv[i + 4]) == "*" ? -1 : std::stoll(argv[i + 4]);
+      keys.push_back(k);
+    }
+  } catch (const std::exception &e) {
+    return fail(e.what());
+  }
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(argv[optind], &c) != GFZ_OK) return fail();
+  char *text = nullptr;
+  size_t len = 0;
+  const gfz_status st = gfz_extract_walk_lines(nullptr, c, keys.data(), keys.size(), threads, &text, &len);
+  gfz_compressed_free(c);
+  return print_and_free(st, text, len);
+}
+
+int do_add_haplotypes(int argc, char **argv) {
+  int threads = 0;
+  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (optind + 1 >= argc) {
+    std::cerr << "Error: Expected <input.gfaz> and <paths_or_walks.gfa>\n";
+    return 1;
+  }
+  const std::string in = argv[optind], haps = argv[optind + 1];
+  std::string out;
+  if (optind + 2 < argc) out = argv[optind + 2];
+  else if (in.size() > 5 && in.substr(in.size() - 5) == ".gfaz") out = in.substr(0, in.size() - 5) + ".updated.gfaz";
+  else out = in + ".updated.gfaz";
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(in.c_str(), &c) != GFZ_OK) return fail();
+  gfz_status st = gfz_add_haplotypes(nullptr, c, haps.c_str(), threads);
+  if (st == GFZ_OK) st = gfz_serialize(c, out.c_str());
+  gfz_compressed_free(c);
+  if (st != GFZ_OK) return fail();
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc < 2) {
+    usage();
+    return 1;
+  }
+  const std::string cmd = argv[1];
+  if (cmd == "compress") return do_compress(argc - 1, argv + 1);
+  if (cmd == "decompress") return do_decompress(argc - 1, argv + 1);
+  if (cmd == "extract-path") return do_extract_path(argc - 1, argv + 1);
+  if (cmd == "extract-walk") return do_extract_walk(argc - 1, argv + 1);
+  if (cmd == "add-haplotypes") return do_add_haplotypes(argc - 1, argv + 1);
+  if (cmd == "-h" || cmd == "--help" || cmd == "help") {
+    usage();
+    return 0;
+  }
+  std::cerr << "Unknown command: " << cmd << std::endl;
+  usage();
+  return 1;
+}

@@ -1,0 +1,461 @@
+// Decompression-side kernels: rule-length table, expansion offsets,
+// expansion, segmented inverse delta and P/W-line text emission.
+//
+// Semantics follow the reference CPU path:
+//   expansion      src/workflows/decompression_workflow.cpp:70-106 (a symbol
+//                  v with |v| in [min_id, min_id + R) is a rule; +R expands
+//                  first then second, -R expands -second then -first)
+//   inverse delta  src/codec/codec.cpp:29-41, applied delta_round times
+//   text           src/io/gfa_write_utils.cpp:238-290 (P: "<id><+|->" joined
+//                  by ',', W: "<>|<><id>" concatenated; decimal digits)
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gfz {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
+  uint64_t g = (n + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g == 0) g = 1;
+  return (unsigned)g;
+}
+
+__device__ __forceinline__ bool is_rule(uint32_t a, uint32_t min_id, uint64_t nrules) {
+  return a >= min_id && (uint64_t)(a - min_id) < nrules;
+}
+
+// Block-wide exclusive sum of a u64 per thread; also returns the total.
+template <int BLOCK>
+__device__ __forceinline__ unsigned long long block_excl_sum(unsigned long long v, unsigned long long &total) {
+  __shared__ unsigned long long s_w[BLOCK / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long inc = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long o = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += o;
+  }
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  unsigned long long pre = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < BLOCK / 32; ++w) {
+    if (w == warp) pre = tot;
+    tot += s_w[w];
+  }
+  total = tot;
+  __syncthreads();
+  return pre + inc - v;
+}
+
+// ---------------------------------------------------------------------------
+// Rule lengths
+// ---------------------------------------------------------------------------
+__global__ void k_rule_len_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
+                                uint64_t nrules, uint32_t min_id, uint32_t *rlen, DevStatus *status) {
+  uint32_t open = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nrules;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    if (rlen[i]) continue;
+    const uint32_t a = abs32(first[i]), b = abs32(second[i]);
+    const uint32_t la = is_rule(a, min_id, nrules) ? ((volatile uint32_t *)rlen)[a - min_id] : 1u;
+    const uint32_t lb = is_rule(b, min_id, nrules) ? ((volatile uint32_t *)rlen)[b - min_id] : 1u;
+    if (la && lb) {
+      const unsigned long long s = (unsigned long long)la + lb;
+      if (s > 0xFFFFFFFFull) {
+        atomicOr(&status->err, kErrLength);
+        rlen[i] = 0xFFFFFFFFu;
+      } else {
+        rlen[i] = (uint32_t)s;
+      }
+    } else {
+      open++;
+    }
+  }
+  open = __reduce_add_sync(0xffffffffu, open);
+  if ((threadIdx.x & 31) == 0 && open) atomicAdd(&status->u64[6], (unsigned long long)open);
+}
+
+// ---------------------------------------------------------------------------
+// Expansion offsets (exclusive scan of symbol expansion lengths)
+// ---------------------------------------------------------------------------
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_symbol_positions(const int32_t *__restrict__ enc, uint64_t m,
+                                                            uint32_t min_id, uint64_t nrules,
+                                                            const uint32_t *__restrict__ rlen, uint64_t *pos,
+                                                            unsigned long long *desc, uint32_t *tile_counter,
+                                                            DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  __shared__ uint32_t sl[TILE];
+  __shared__ unsigned long long s_excl;
+  const uint32_t tile = claim_tile(tile_counter);
+  const uint64_t base = (uint64_t)tile * TILE;
+  const uint32_t len = (uint32_t)min((uint64_t)TILE, m - base);
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) {
+    const uint32_t a = abs32(enc[base + j]);
+    sl[j] = is_rule(a, min_id, nrules) ? rlen[a - min_id] : 1u;
+  }
+  __syncthreads();
+  unsigned long long mine = 0;
+  const uint32_t j0 = threadIdx.x * ITEMS;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k)
+    if (j0 + k < len) mine += sl[j0 + k];
+  unsigned long long total;
+  unsigned long long ex = block_excl_sum<BLOCK>(mine, total);
+  if (threadIdx.x == 0) s_excl = lookback_sum(desc, tile, total, &status->err);
+  __syncthreads();
+  unsigned long long p = s_excl + ex;
+  // write through shared memory for coalesced stores
+  __syncthreads();
+  unsigned long long vals[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    vals[k] = p;
+    if (j0 + k < len) p += sl[j0 + k];
+  }
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k)
+    if (j0 + k < len) pos[base + j0 + k] = vals[k];
+  if (base + len == m && threadIdx.x == 0) pos[m] = s_excl + total;
+}
+
+// ---------------------------------------------------------------------------
+// Expansion: one thread per encoded symbol, explicit stack
+// ---------------------------------------------------------------------------
+constexpr int kStackDepth = 64;
+
+__global__ void k_expand(const int32_t *__restrict__ enc, uint64_t m, const uint64_t *__restrict__ pos,
+                         const int32_t *__restrict__ first, const int32_t *__restrict__ second, uint64_t nrules,
+                         uint32_t min_id, int32_t *__restrict__ out, DevStatus *status) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int32_t v = enc[i];
+    uint64_t p = pos[i];
+    if (!is_rule(abs32(v), min_id, nrules)) {
+      out[p] = v;
+      continue;
+    }
+    int32_t stack[kStackDepth];
+    int sp = 0;
+    stack[sp++] = v;
+    while (sp > 0) {
+      const int32_t x = stack[--sp];
+      const uint32_t a = abs32(x);
+      if (!is_rule(a, min_id, nrules)) {
+        out[p++] = x;
+        continue;
+      }
+      if (sp + 2 > kStackDepth) {
+        atomicOr(&status->err, kErrDepth);
+        break;
+      }
+      const int32_t f = first[a - min_id], g = second[a - min_id];
+      if (x > 0) {
+        stack[sp++] = g;
+        stack[sp++] = f;
+      } else {
+        stack[sp++] = neg32(f);
+        stack[sp++] = neg32(g);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Segmented inverse delta (in-place inclusive prefix sum per traversal)
+// ---------------------------------------------------------------------------
+struct SegAgg {
+  uint32_t f;    // a traversal starts inside
+  uint32_t sum;  // sum since the last start (or of everything)
+};
+__device__ __forceinline__ SegAgg seg_compose(const SegAgg &a, const SegAgg &b) {
+  return b.f ? b : SegAgg{a.f, a.sum + b.sum};
+}
+
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n, const uint64_t *__restrict__ off,
+                                                         uint64_t ntrav, unsigned long long *desc,
+                                                         uint32_t *tile_counter, DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  constexpr int NW = BLOCK / 32;
+  __shared__ uint32_t sv[TILE];
+  __shared__ uint32_t hb[TILE / 32 + 2];
+  __shared__ uint64_t s_tlo;
+  __shared__ SegAgg s_w[NW];
+  __shared__ uint32_t s_carry;
+  const uint32_t tile = claim_tile(tile_counter);
+  const uint64_t base = (uint64_t)tile * TILE;
+  const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
+  for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[j] = (uint32_t)x[base + j];
+  mark_heads(off, ntrav, base, len, hb, &s_tlo);
+  __syncthreads();
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  SegAgg a{0u, 0u};
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const uint32_t j = j0 + k;
+    if (j < len) {
+      if (bit_at(hb, j)) a = SegAgg{1u, sv[j]};
+      else a.sum += sv[j];
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  SegAgg inc = a;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    SegAgg o{__shfl_up_sync(0xffffffffu, inc.f, d), __shfl_up_sync(0xffffffffu, inc.sum, d)};
+    if (lane >= d) inc = seg_compose(o, inc);
+  }
+  SegAgg ex{__shfl_up_sync(0xffffffffu, inc.f, 1), __shfl_up_sync(0xffffffffu, inc.sum, 1)};
+  if (lane == 0) ex = SegAgg{0u, 0u};
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  SegAgg wpre{0u, 0u}, total{0u, 0u};
+  for (int w = 0; w < NW; ++w) {
+    if (w == warp) wpre = total;
+    total = seg_compose(total, s_w[w]);
+  }
+  ex = seg_compose(wpre, ex);
+  if (threadIdx.x == 0) {
+    uint32_t carry = 0;
+    if (tile == 0) {
+      st_release(desc, kDescIncl | total.sum);
+    } else {
+      st_release(desc + tile, kDescAgg | ((unsigned long long)total.f << 32) | total.sum);
+      uint64_t j = tile;
+      while (j > 0) {
+        --j;
+        const unsigned long long d = wait_desc(desc, j, &status->err);
+        carry += (uint32_t)d;
+        if ((d & kDescMask) == kDescIncl || ((d >> 32) & 1u)) break;
+      }
+      st_release(desc + tile, kDescIncl | (uint32_t)(total.f ? total.sum : carry + total.sum));
+    }
+    s_carry = carry;
+  }
+  __syncthreads();
+  uint32_t run = ex.f ? ex.sum : s_carry + ex.sum;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const uint32_t j = j0 + k;
+    if (j < len) {
+      run = bit_at(hb, j) ? sv[j] : run + sv[j];
+      sv[j] = run;
+    }
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) x[base + j] = (int32_t)sv[j];
+}
+
+// ---------------------------------------------------------------------------
+// Text emission
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t dec_digits(uint32_t v) {
+  uint32_t d = 1;
+  d += v >= 10u;
+  d += v >= 100u;
+  d += v >= 1000u;
+  d += v >= 10000u;
+  d += v >= 100000u;
+  d += v >= 1000000u;
+  d += v >= 10000000u;
+  d += v >= 100000000u;
+  d += v >= 1000000000u;
+  return d;
+}
+
+__device__ __forceinline__ void put_dec(char *dst, uint32_t v, uint32_t nd) {
+  for (uint32_t i = nd; i-- > 0;) {
+    dst[i] = (char)('0' + v % 10u);
+    v /= 10u;
+  }
+}
+
+// Largest t with off[t] <= p (p < off[ntrav]).
+__device__ __forceinline__ uint64_t trav_of(const uint64_t *off, uint64_t ntrav, uint64_t p) {
+  uint64_t lo = 0, hi = ntrav;  // answer in [0, ntrav)
+  while (hi - lo > 1) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= p) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Copies len bytes from a 16-byte aligned shared buffer (with >= 16 bytes of
+// slack after len) to global memory using 16-byte stores where aligned.
+template <int BLOCK>
+__device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, char *dst) {
+  const uint32_t mis = (uint32_t)((uintptr_t)dst & 15u);
+  uint32_t head = (16u - mis) & 15u;
+  if (head > len) head = len;
+  for (uint32_t i = threadIdx.x; i < head; i += BLOCK) dst[i] = sbuf[i];
+  const uint32_t body = (len - head) >> 4;
+  const uint32_t *sw = reinterpret_cast<const uint32_t *>(sbuf);
+  const uint32_t r = head & 3u, sh = 8u * r;
+  for (uint32_t v = threadIdx.x; v < body; v += BLOCK) {
+    const uint32_t o = head + 16u * v;
+    const uint32_t w = o >> 2;
+    uint4 val;
+    if (r == 0) {
+      val = make_uint4(sw[w], sw[w + 1], sw[w + 2], sw[w + 3]);
+    } else {
+      const uint32_t a0 = sw[w], a1 = sw[w + 1], a2 = sw[w + 2], a3 = sw[w + 3], a4 = sw[w + 4];
+      val = make_uint4(__funnelshift_r(a0, a1, sh), __funnelshift_r(a1, a2, sh), __funnelshift_r(a2, a3, sh),
+                       __funnelshift_r(a3, a4, sh));
+    }
+    *reinterpret_cast<uint4 *>(dst + o) = val;
+  }
+  for (uint32_t i = head + 16u * body + threadIdx.x; i < len; i += BLOCK) dst[i] = sbuf[i];
+}
+
+constexpr uint32_t kTextBuf = 28 * 1024;
+
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_emit_text(const int32_t *__restrict__ x, uint64_t n,
+                                                     const uint64_t *__restrict__ off, uint64_t ntrav, TextMeta meta,
+                                                     char *__restrict__ text, unsigned long long *desc,
+                                                     uint32_t *tile_counter, DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  __shared__ int32_t sv[TILE];
+  __shared__ __align__(16) char sbuf[kTextBuf + 32];
+  __shared__ unsigned long long s_off;
+  const uint32_t tile = claim_tile(tile_counter);
+  const uint64_t base = (uint64_t)tile * TILE;
+  const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[j] = x[base + j];
+  __syncthreads();
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  const bool pmode = meta.mode == 0;
+  // per element: traversal boundaries and text length
+  uint64_t t = 0;
+  unsigned long long mine = 0;
+  uint32_t flags = 0;  // bit 2k: first step, bit 2k+1: last step
+  if (j0 < len) {
+    t = trav_of(off, ntrav, base + j0);
+    uint64_t tt = t;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const uint32_t j = j0 + k;
+      if (j >= len) break;
+      const uint64_t p = base + j;
+      while (__ldg(off + tt + 1) <= p) ++tt;
+      const bool fst = p == __ldg(off + tt);
+      const bool lst = p + 1 == __ldg(off + tt + 1);
+      flags |= ((uint32_t)fst << (2 * k)) | ((uint32_t)lst << (2 * k + 1));
+      mine += dec_digits(abs32(sv[j])) + 1u + ((pmode && !lst) ? 1u : 0u);
+      if (fst) mine += meta.pre_off[tt + 1] - meta.pre_off[tt];
+      if (lst) mine += meta.suf_off[tt + 1] - meta.suf_off[tt];
+    }
+  }
+  unsigned long long total;
+  const unsigned long long ex = block_excl_sum<BLOCK>(mine, total);
+  if (threadIdx.x == 0) s_off = lookback_sum(desc, tile, total, &status->err);
+  __syncthreads();
+  const unsigned long long toff = s_off;
+  const bool last_tile = base + len == n;
+  if (last_tile && threadIdx.x == 0) status->u64[7] = toff + total + meta.tail_len;
+  if (text == nullptr) return;
+  const bool staged = total <= kTextBuf;
+  char *dst = staged ? sbuf + ex : text + toff + ex;
+  if (j0 < len) {
+    uint64_t tt = t;
+    uint32_t o = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const uint32_t j = j0 + k;
+      if (j >= len) break;
+      const uint64_t p = base + j;
+      while (__ldg(off + tt + 1) <= p) ++tt;
+      const bool fst = (flags >> (2 * k)) & 1u, lst = (flags >> (2 * k + 1)) & 1u;
+      if (fst) {
+        const uint64_t a = meta.pre_off[tt], b = meta.pre_off[tt + 1];
+        for (uint64_t q = a; q < b; ++q) dst[o++] = meta.blob[q];
+      }
+      const int32_t v = sv[j];
+      const uint32_t av = abs32(v), nd = dec_digits(av);
+      if (pmode) {
+        put_dec(dst + o, av, nd);
+        o += nd;
+        dst[o++] = v < 0 ? '-' : '+';
+        if (!lst) dst[o++] = ',';
+      } else {
+        dst[o++] = v < 0 ? '<' : '>';
+        put_dec(dst + o, av, nd);
+        o += nd;
+      }
+      if (lst) {
+        const uint64_t a = meta.suf_off[tt], b = meta.suf_off[tt + 1];
+        for (uint64_t q = a; q < b; ++q) dst[o++] = meta.blob[q];
+      }
+    }
+  }
+  if (staged) {
+    __syncthreads();
+    block_copy_out<BLOCK>(sbuf, (uint32_t)total, text + toff);
+  }
+  if (last_tile && meta.tail_len) {
+    for (uint64_t q = threadIdx.x; q < meta.tail_len; q += BLOCK) text[toff + total + q] = meta.tail[q];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+constexpr int kScanItems = 16;
+constexpr int kDeltaItems = 16;
+constexpr int kTextItems = 8;
+
+void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
+                          uint32_t *rlen, DevStatus *status, cudaStream_t st) {
+  if (!nrules) return;
+  k_rule_len_pass<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(first, second, nrules, min_id, rlen, status);
+}
+
+uint64_t scan_num_tiles(uint64_t n) {
+  constexpr uint64_t TILE = kBlock * kScanItems;
+  return (n + TILE - 1) / TILE;
+}
+
+void launch_symbol_positions(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules, const uint32_t *rlen,
+                             uint64_t *pos, unsigned long long *desc, uint32_t *tile_counter, DevStatus *status,
+                             cudaStream_t st) {
+  if (!m) return;
+  k_symbol_positions<kBlock, kScanItems><<<(unsigned)scan_num_tiles(m), kBlock, 0, st>>>(
+      enc, m, min_id, nrules, rlen, pos, desc, tile_counter, status);
+}
+
+void launch_expand(const int32_t *enc, uint64_t m, const uint64_t *pos, const int32_t *first, const int32_t *second,
+                   uint64_t nrules, uint32_t min_id, int32_t *out, DevStatus *status, cudaStream_t st) {
+  if (!m) return;
+  k_expand<<<grid_for(m, kBlock, 152u * 64u), kBlock, 0, st>>>(enc, m, pos, first, second, nrules, min_id, out,
+                                                               status);
+}
+
+void launch_inverse_delta(int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav, unsigned long long *desc,
+                          uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  constexpr uint64_t TILE = kBlock * kDeltaItems;
+  k_inverse_delta<kBlock, kDeltaItems><<<(unsigned)((n + TILE - 1) / TILE), kBlock, 0, st>>>(
+      x, n, off, ntrav, desc, tile_counter, status);
+}
+
+uint64_t text_num_tiles(uint64_t n) {
+  constexpr uint64_t TILE = kBlock * kTextItems;
+  return (n + TILE - 1) / TILE;
+}
+
+void launch_emit_text(const int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav, TextMeta meta, char *text,
+                      unsigned long long *desc, uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  k_emit_text<kBlock, kTextItems><<<(unsigned)text_num_tiles(n), kBlock, 0, st>>>(x, n, off, ntrav, meta, text, desc,
+                                                                                  tile_counter, status);
+}
+
+}  // namespace gfz

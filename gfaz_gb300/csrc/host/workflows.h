@@ -1,0 +1,56 @@
+// Host workflows of the GB300 GFAz build: the reference's public operations
+// (compress, streaming decompress, in-memory decompress, extraction,
+// add-haplotypes) with the traversal transform running on the GPU through
+// the device pipeline.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../pipeline.h"
+#include "model.h"
+
+namespace gfz {
+
+struct WalkKey {
+  std::string sample_id;
+  uint32_t hap_index = 0;
+  std::string seq_id;
+  int64_t seq_start = -1, seq_end = -1;
+};
+
+// src/workflows/compression_workflow.cpp:706 compress_gfa
+Compressed compress_gfa(Context &ctx, const std::string &gfa_path, int rounds, uint64_t threshold, int delta_round,
+                        int threads, bool show_stats);
+// Same, from an already parsed graph (the graph's traversals are left as is).
+Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t threshold, int delta_round,
+                          int threads, bool show_stats);
+
+// src/io/gfa_writer.cpp:376 write_gfa_from_compressed_data (H,S,L,J,C,P,W)
+void write_gfa(Context &ctx, const Compressed &c, const std::string &out_path, int threads);
+// Whole GFA text in memory (same bytes as write_gfa).
+std::string gfa_text(Context &ctx, const Compressed &c, int threads);
+
+// src/workflows/decompression_workflow.cpp:255 decompress_gfa
+Graph decompress_graph(Context &ctx, const Compressed &c, int threads);
+
+// src/workflows/extraction_workflow.cpp:207-357
+std::vector<std::string> extract_path_lines(Context &ctx, const Compressed &c, const std::vector<std::string> &names,
+                                            int threads);
+std::vector<std::string> extract_walk_lines(Context &ctx, const Compressed &c, const std::vector<WalkKey> &keys,
+                                            int threads);
+std::vector<std::string> extract_walk_lines_by_name(Context &ctx, const Compressed &c,
+                                                    const std::vector<std::string> &names, int threads);
+
+// src/workflows/add_haplotypes_workflow.cpp:579 add_haplotypes
+void add_haplotypes(Context &ctx, Compressed &c, const std::string &path, int threads);
+
+// Decoded rule columns (zstd + delta decode on the device) and text pieces.
+void decode_rule_columns(Context &ctx, const Compressed &c, Grammar &g);
+TextPieces path_pieces(const std::vector<std::string> &names, const std::vector<std::string> &overlaps,
+                       const std::vector<uint64_t> &off);
+TextPieces walk_pieces(const std::vector<std::string> &samples, const std::vector<uint32_t> &haps,
+                       const std::vector<std::string> &seqids, const std::vector<int64_t> &starts,
+                       const std::vector<int64_t> &ends, const std::vector<uint64_t> &off);
+
+}  // namespace gfz

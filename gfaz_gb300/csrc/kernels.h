@@ -1,0 +1,123 @@
+// Host-callable launchers for the GFAz transform kernels.  Every pointer is a
+// device pointer; every launch goes to `stream`.  Launchers never allocate.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gfz {
+
+// Per-context device status block (zeroed by the owner).
+struct DevStatus {
+  uint32_t err;            // OR of kErr* bits
+  uint32_t aux;            // u32 result slot (max |x| of delta coding)
+  unsigned long long u64[8];  // kernel result slots (see each launcher)
+};
+
+// ---- encode side ----------------------------------------------------------
+// out[i] = in[i] - in[i-1] inside each traversal (first element copied);
+// atomically max-reduces |out| into *max_abs.  in == out is NOT allowed.
+void launch_delta_encode(const int32_t *in, int32_t *out, uint64_t n, const uint64_t *off,
+                         uint64_t ntrav, uint32_t *max_abs, cudaStream_t st);
+// max |x| of the raw stream (delta_round == 0 seed).
+void launch_max_abs(const int32_t *in, uint64_t n, uint32_t *max_abs, cudaStream_t st);
+
+struct PairTable {
+  unsigned long long *keys;  // cap slots, kEmptyKey when free
+  uint32_t *flags;           // kFlag* bits per slot
+  uint32_t *vals;            // final rule id per used slot
+  uint64_t cap;              // power of two
+};
+
+// Inserts every canonical adjacent pair inside a traversal.  Results:
+// status->u64[0] += new distinct keys, u64[1] += keys that became repeated.
+void launch_count_pairs(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav,
+                        PairTable tab, DevStatus *status, bool warp_dedup, cudaStream_t st);
+
+// Greedy left-to-right replacement of candidate pairs; writes the compacted
+// stream with temporary symbols +-(temp_base + slot), the new traversal
+// offsets (ntrav + 1 entries) and status->u64[2] = output length.
+// desc: one u64 per tile, zeroed; tile_counter zeroed.
+void launch_apply(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav, PairTable tab,
+                  int32_t temp_base, int32_t *out, uint64_t *new_off, unsigned long long *desc,
+                  uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+uint64_t apply_num_tiles(uint64_t n);
+
+// Appends (transformed key, slot) of every used slot; count in status->u64[3].
+void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out,
+                         DevStatus *status, cudaStream_t st);
+
+// Stable LSD radix sort of (u64 key, u32 value) pairs on the given byte
+// positions (bit i of byte_mask = sort on byte i).  Ping-pongs between the
+// in/tmp buffers; returns true when the result ended in the tmp buffers.
+// hist must hold 256 * radix_blocks(n) + 1 u32 entries.
+uint64_t radix_blocks(uint64_t n);
+bool radix_sort_pairs(unsigned long long *keys, uint32_t *vals, unsigned long long *keys_tmp,
+                      uint32_t *vals_tmp, uint64_t n, uint32_t byte_mask, uint32_t *hist,
+                      cudaStream_t st);
+// OR / AND reduction of keys into status->u64[4] / u64[5] (pre-set u64[5] to ~0).
+void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status, cudaStream_t st);
+
+// keys sorted (transformed, ascending signed order): vals[slot] = next_id + rank,
+// rulebook[rank] = original key.
+void launch_assign_ids(const unsigned long long *sorted_keys, const uint32_t *sorted_slots, uint64_t u,
+                       uint32_t next_id, PairTable tab, long long *rulebook, cudaStream_t st);
+// Rewrites temporary symbols +-(temp_base + slot) into +-vals[slot].
+void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const uint32_t *vals, cudaStream_t st);
+
+// ---- append encoder (add-haplotypes) -------------------------------------
+// Builds a key -> rule id table from stored rule columns (rules
+// [lo, hi) of the decoded columns get ids start .. start + hi - lo).
+void launch_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi,
+                             uint32_t start, PairTable tab, DevStatus *status, cudaStream_t st);
+// Stack encoder, one thread per traversal (sequential within a traversal).
+// Encodes s[off[t] .. off[t] + len[t]) in place and updates len[t].
+void launch_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, uint64_t ntrav, PairTable tab,
+                         DevStatus *status, cudaStream_t st);
+
+// ---- decode side ------------------------------------------------------------
+// Rule expansion lengths: len[i] for rule min_id + i.  One pass resolves the
+// rules whose children are resolved; status->u64[6] counts rules still open.
+void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
+                          uint32_t *rlen, DevStatus *status, cudaStream_t st);
+// Exclusive scan of the expansion length of every encoded symbol into
+// pos[0..m] (pos[m] = total); desc/tile_counter zeroed.
+void launch_symbol_positions(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules,
+                             const uint32_t *rlen, uint64_t *pos, unsigned long long *desc,
+                             uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+uint64_t scan_num_tiles(uint64_t n);
+// Expands every encoded symbol into out[pos[i] ..).
+void launch_expand(const int32_t *enc, uint64_t m, const uint64_t *pos, const int32_t *first,
+                   const int32_t *second, uint64_t nrules, uint32_t min_id, int32_t *out, DevStatus *status,
+                   cudaStream_t st);
+// In-place inclusive prefix sum inside every traversal (inverse delta).
+void launch_inverse_delta(int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav,
+                          unsigned long long *desc, uint32_t *tile_counter, DevStatus *status,
+                          cudaStream_t st);
+
+// GFA text of P-lines (mode 0) or W-lines (mode 1) for traversals whose
+// steps are x[off[t] .. off[t+1]).  Every non-empty traversal t emits
+// blob[pre_off[t] .. pre_off[t+1]) before its first step and
+// blob[suf_off[t] .. suf_off[t+1]) after its last step; `tail` bytes
+// (lines of trailing empty traversals) follow the last step.  The total
+// text size is written to status->u64[7].  With text == nullptr only the
+// size is computed.
+struct TextMeta {
+  const char *blob;
+  const uint64_t *pre_off;  // ntrav + 1
+  const uint64_t *suf_off;  // ntrav + 1
+  const char *tail;
+  uint64_t tail_len;
+  int mode;
+};
+void launch_emit_text(const int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav, TextMeta meta,
+                      char *text, unsigned long long *desc, uint32_t *tile_counter, DevStatus *status,
+                      cudaStream_t st);
+uint64_t text_num_tiles(uint64_t n);
+
+// Gathers encoded ranges src[starts[r] .. starts[r] + lens[r]) into dst at
+// dst_off[r] (serving batches).
+void launch_gather_ranges(const int32_t *src, const uint64_t *starts, const uint64_t *dst_off, uint64_t nr,
+                          int32_t *dst, cudaStream_t st);
+
+}  // namespace gfz

@@ -1,0 +1,608 @@
+// Device pipeline orchestration for the GFAz transform (see pipeline.h).
+//
+// Compression round loop (src/workflows/compression_workflow.cpp:548-700):
+//   count pairs -> stop if no candidate -> greedy replacement with temporary
+//   symbols -> collect used rules -> stop if none used -> radix sort by the
+//   signed packed key -> final ids next_id + rank -> remap temporaries.
+#include "pipeline.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace gfz {
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw CudaError(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+__global__ void k_split_rules(const long long *rules, uint64_t n, int32_t *first, int32_t *second) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long k = (unsigned long long)rules[i];
+    first[i] = key_first(k);
+    second[i] = key_second(k);
+  }
+}
+
+__global__ void k_gather_pos(const uint64_t *pos, const uint64_t *enc_off, uint64_t ntrav1, uint64_t enc_base,
+                             uint64_t *out_off) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntrav1; t += (uint64_t)gridDim.x * blockDim.x)
+    out_off[t] = pos[enc_off[t] - enc_base];
+}
+
+inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
+  uint64_t g = (n + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g == 0) g = 1;
+  return (unsigned)g;
+}
+
+uint64_t next_pow2(uint64_t x) {
+  uint64_t c = 1;
+  while (c < x) c <<= 1;
+  return c;
+}
+
+constexpr uint64_t kMaxTableCap = 1ULL << 31;
+
+struct Table {
+  DevVec<unsigned long long> keys;
+  DevVec<uint32_t> flags, vals;
+  explicit Table(cudaStream_t st) : keys(st), flags(st), vals(st) {}
+  PairTable view(uint64_t cap) { return PairTable{keys.ptr, flags.ptr, vals.ptr, cap}; }
+  void prepare(uint64_t cap, cudaStream_t st, bool vals_ff = false) {
+    keys.resize(cap);
+    flags.resize(cap);
+    vals.resize(cap);
+    cuda_check(cudaMemsetAsync(keys.ptr, kEmptyByte, cap * sizeof(unsigned long long), st), "table clear");
+    cuda_check(cudaMemsetAsync(flags.ptr, 0, cap * sizeof(uint32_t), st), "table clear");
+    if (vals_ff) cuda_check(cudaMemsetAsync(vals.ptr, 0xFF, cap * sizeof(uint32_t), st), "table clear");
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullptr), counter_(nullptr) {
+  cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  cudaDeviceProp prop;
+  cuda_check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+  sms_ = prop.multiProcessorCount;
+  if (stream) {
+    stream_ = stream;
+  } else {
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    own_stream_ = true;
+  }
+  // keep freed pool memory cached: repeated calls reuse it without syncs
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  desc_ = DevVec<unsigned long long>(stream_);
+  counter_ = DevVec<uint32_t>(stream_);
+  cuda_check(cudaMalloc((void **)&d_status_, sizeof(DevStatus)), "status alloc");
+  cuda_check(cudaMallocHost((void **)&h_status_, sizeof(DevStatus)), "status alloc");
+  std::memset(h_status_, 0, sizeof(DevStatus));
+  cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
+  counter_.resize(1);
+}
+
+Context::~Context() {
+  cudaStreamSynchronize(stream_);
+  for (auto &p : pending_) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : event_pool_) cudaEventDestroy(e);
+  desc_.release();
+  counter_.release();
+  cudaStreamSynchronize(stream_);
+  cudaFree(d_status_);
+  cudaFreeHost(h_status_);
+  if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+void Context::reset_status() {
+  cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
+}
+
+const DevStatus &Context::read_status() {
+  cuda_check(cudaMemcpyAsync(h_status_, d_status_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_),
+             "status read");
+  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  return *h_status_;
+}
+
+void Context::check_status(const char *stage) {
+  const uint32_t e = h_status_->err;
+  if (!e) return;
+  std::string msg = std::string("device error in ") + stage + ":";
+  if (e & kErrTableFull) msg += " pair table full;";
+  if (e & kErrLookupMiss) msg += " counted pair missing from table;";
+  if (e & kErrTimeout) msg += " look-back wait timed out;";
+  if (e & kErrDepth) msg += " rule nesting deeper than 64;";
+  if (e & kErrLength) msg += " length overflow or mismatch;";
+  if (e & kErrRuleCycle) msg += " rule lengths do not resolve (cyclic rulebook);";
+  if (e & kErrBadSymbol) msg += " invalid rule key;";
+  throw std::runtime_error(msg);
+}
+
+unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) {
+  desc_.resize(std::max<uint64_t>(tiles, 1));
+  cuda_check(cudaMemsetAsync(desc_.ptr, 0, std::max<uint64_t>(tiles, 1) * sizeof(unsigned long long), stream_),
+             "descriptor clear");
+  cuda_check(cudaMemsetAsync(counter_.ptr, 0, sizeof(uint32_t), stream_), "counter clear");
+  *counter = counter_.ptr;
+  count_launch(0);
+  return desc_.ptr;
+}
+
+cudaEvent_t Context::take_event() {
+  if (!event_pool_.empty()) {
+    cudaEvent_t e = event_pool_.back();
+    event_pool_.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  return e;
+}
+
+void Context::tbegin(const char *name, double bytes) {
+  launches_++;
+  if (!timing) return;
+  open_name_ = name;
+  open_bytes_ = bytes;
+  open_a_ = take_event();
+  cudaEventRecord(open_a_, stream_);
+}
+
+void Context::tend() {
+  if (!timing || !open_a_) return;
+  cudaEvent_t b = take_event();
+  cudaEventRecord(b, stream_);
+  pending_.push_back(Pending{open_name_, open_a_, b, open_bytes_});
+  open_a_ = nullptr;
+}
+
+std::map<std::string, KernelStat> Context::kernel_stats() {
+  cudaStreamSynchronize(stream_);
+  for (auto &p : pending_) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto &s = stats_[p.name];
+    s.ms += ms;
+    s.launches++;
+    s.bytes += p.bytes;
+    event_pool_.push_back(p.a);
+    event_pool_.push_back(p.b);
+  }
+  pending_.clear();
+  return stats_;
+}
+
+void Context::add_bytes(const char *name, double bytes) {
+  if (timing) stats_[name].bytes += bytes;
+}
+
+void Context::clear_kernel_stats() {
+  kernel_stats();
+  stats_.clear();
+  launches_ = 0;
+}
+
+// Launch bracketed by timing events; `bytes` = algorithmic bytes of the
+// launch (what it must read and write at minimum).
+#define GFZ_TIMED_B(ctx, name, bytes, expr) \
+  do {                                      \
+    (ctx).tbegin(name, (double)(bytes));    \
+    expr;                                   \
+    (ctx).tend();                           \
+  } while (0)
+#define GFZ_TIMED(ctx, name, expr) GFZ_TIMED_B(ctx, name, 0, expr)
+
+// ---------------------------------------------------------------------------
+// Compression
+// ---------------------------------------------------------------------------
+void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
+                       const EncodeParams &p, Grammar &g) {
+  cudaStream_t st = ctx.stream();
+  if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
+  const uint64_t ntrav = h_off.size() - 1;
+  const uint64_t N = h_off.back();
+  for (uint64_t t = 0; t < ntrav; ++t)
+    if (h_off[t + 1] < h_off[t]) throw std::invalid_argument("traversal offsets must be non-decreasing");
+  if (h_off[0] != 0) throw std::invalid_argument("offsets must start at 0");
+  const int dr = std::max(0, p.delta_round);
+  g.ntrav = ntrav;
+  g.delta_round = dr;
+  g.rounds_done = 0;
+  g.nrules = 0;
+
+  DevVec<uint64_t> offA(st), offB(st);
+  offA.resize(ntrav + 1);
+  offB.resize(ntrav + 1);
+  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
+             "offsets upload");
+  DevVec<int32_t> A(st), B(st);
+  A.resize(std::max<uint64_t>(N, 1));
+  B.resize(std::max<uint64_t>(N, 1));
+
+  ctx.reset_status();
+  DevStatus *ds = ctx.dstatus();
+  if (dr == 0) {
+    if (N) cuda_check(cudaMemcpyAsync(A.ptr, d_steps, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+    GFZ_TIMED_B(ctx, "max_abs", 4.0 * N, launch_max_abs(A.ptr, N, &ds->aux, st));
+  } else {
+    GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(d_steps, A.ptr, N, offA.ptr, ntrav, &ds->aux, st));
+    for (int r = 1; r < dr; ++r) {
+      GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(A.ptr, B.ptr, N, offA.ptr, ntrav, &ds->aux, st));
+      A.swap(B);
+    }
+  }
+  const DevStatus &s0 = ctx.read_status();
+  const uint32_t max_abs = s0.aux;
+  if (max_abs == UINT32_MAX)
+    throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
+  uint32_t next_id = max_abs + 1;
+  g.layer_start = next_id;
+
+  DevVec<long long> rules(st);
+  Table tab(st);
+  DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
+  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st);
+
+  uint64_t n = N;
+  uint64_t prev_distinct = 0;
+  for (int round = 0; round < p.rounds; ++round) {
+    if (n < 2) break;
+    uint64_t est = prev_distinct ? prev_distinct * 2 : n / 8;
+    est = std::min(est, n);
+    uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
+    uint64_t distinct = 0, repeated = 0;
+    for (;;) {
+      if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
+      tab.prepare(cap, st);
+      ctx.reset_status();
+      GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
+                launch_count_pairs(A.ptr, n, offA.ptr, ntrav, tab.view(cap), ds, ctx.warp_dedup, st));
+      const DevStatus &s = ctx.read_status();
+      distinct = s.u64[0];
+      repeated = s.u64[1];
+      if ((s.err & kErrTableFull) || distinct * 10 > cap * 7) {
+        cap *= 4;
+        continue;
+      }
+      ctx.check_status("count_pairs");
+      break;
+    }
+    prev_distinct = distinct;
+    if (repeated == 0) break;  // no candidates: stop all rounds
+    if ((uint64_t)next_id + cap >= (1ULL << 31))
+      throw std::overflow_error("Compression workflow error: rule id space exhausted");
+    const int32_t temp_base = (int32_t)next_id;
+    ctx.reset_status();
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(apply_num_tiles(n), &counter);
+    GFZ_TIMED_B(ctx, "apply", 4.0 * n,
+              launch_apply(A.ptr, n, offA.ptr, ntrav, tab.view(cap), temp_base, B.ptr, offB.ptr, desc, counter,
+                           ds, st));
+    ukeys.resize(std::max<uint64_t>(repeated, 1));
+    uslots.resize(std::max<uint64_t>(repeated, 1));
+    GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, ds, st));
+    const DevStatus &s1 = ctx.read_status();
+    ctx.check_status("apply");
+    const uint64_t n_out = s1.u64[2];
+    const uint64_t U = s1.u64[3];
+    ctx.add_bytes("apply", 4.0 * n_out);
+    ctx.add_bytes("collect_used", 12.0 * U);
+    if (U == 0) break;  // no rule used: stop all rounds
+    ukeys_tmp.resize(U);
+    uslots_tmp.resize(U);
+    // OR/AND of the used keys tell which radix passes can be skipped
+    ctx.reset_status();
+    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
+    GFZ_TIMED(ctx, "key_or_and", launch_key_or_and(ukeys.ptr, U, ds, st));
+    const DevStatus &s2 = ctx.read_status();
+    const unsigned long long diff = s2.u64[4] ^ s2.u64[5];
+    uint32_t byte_mask = 0;
+    for (int b = 0; b < 8; ++b)
+      if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
+    hist.resize(256 * radix_blocks(U) + 1);
+    bool in_tmp;
+    GFZ_TIMED(ctx, "radix_sort",
+              in_tmp = radix_sort_pairs(ukeys.ptr, uslots.ptr, ukeys_tmp.ptr, uslots_tmp.ptr, U, byte_mask, hist.ptr,
+                                        st));
+    rules.reserve(g.nrules + U, true);
+    rules.size = g.nrules + U;
+    GFZ_TIMED(ctx, "assign_ids",
+              launch_assign_ids(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr, U, next_id,
+                                tab.view(cap), rules.ptr + g.nrules, st));
+    GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.vals.ptr, st));
+    g.nrules += U;
+    next_id += (uint32_t)U;
+    n = n_out;
+    A.swap(B);
+    offA.swap(offB);
+    g.rounds_done++;
+  }
+  g.next_id = next_id;
+  A.size = n;
+  g.enc = std::move(A);
+  g.off = std::move(offA);
+  g.h_off.resize(ntrav + 1);
+  cuda_check(cudaMemcpyAsync(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
+             "offsets download");
+  rules.size = g.nrules;
+  g.rules = std::move(rules);
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+void rule_columns_delta(Context &ctx, const Grammar &g, DevVec<int32_t> &first, DevVec<int32_t> &second) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t R = g.nrules;
+  first.resize(std::max<uint64_t>(R, 1));
+  second.resize(std::max<uint64_t>(R, 1));
+  first.size = second.size = R;
+  if (!R) return;
+  DevVec<int32_t> tf(st), ts(st);
+  tf.resize(R);
+  ts.resize(R);
+  DevVec<uint64_t> off(st);
+  off.resize(2);
+  const uint64_t h[2] = {0, R};
+  cuda_check(cudaMemcpyAsync(off.ptr, h, sizeof(h), cudaMemcpyHostToDevice, st), "upload");
+  GFZ_TIMED(ctx, "split_rules", (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, tf.ptr, ts.ptr)));
+  ctx.reset_status();
+  GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(tf.ptr, first.ptr, R, off.ptr, 1, &ctx.dstatus()->aux, st));
+  GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(ts.ptr, second.ptr, R, off.ptr, 1, &ctx.dstatus()->aux, st));
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+// ---------------------------------------------------------------------------
+// Decompression
+// ---------------------------------------------------------------------------
+void load_rules(Context &ctx, Grammar &g, const int32_t *first, const int32_t *second, uint64_t nrules,
+                uint32_t min_id) {
+  cudaStream_t st = ctx.stream();
+  g.nrules = nrules;
+  g.layer_start = min_id;
+  g.next_id = min_id + (uint32_t)nrules;
+  g.first.resize(std::max<uint64_t>(nrules, 1));
+  g.second.resize(std::max<uint64_t>(nrules, 1));
+  g.first.size = g.second.size = nrules;
+  g.rlen_ready = false;
+  if (!nrules) return;
+  cuda_check(cudaMemcpyAsync(g.first.ptr, first, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
+  cuda_check(cudaMemcpyAsync(g.second.ptr, second, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
+  // stored columns are delta coded (codec.cpp:88-95): prefix sums on device
+  DevVec<uint64_t> off(st);
+  off.resize(2);
+  const uint64_t h[2] = {0, nrules};
+  cuda_check(cudaMemcpyAsync(off.ptr, h, sizeof(h), cudaMemcpyHostToDevice, st), "upload");
+  ctx.reset_status();
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(scan_num_tiles(nrules), &counter);
+  GFZ_TIMED(ctx, "inverse_delta",
+            launch_inverse_delta(g.first.ptr, nrules, off.ptr, 1, desc, counter, ctx.dstatus(), st));
+  desc = ctx.lookback(scan_num_tiles(nrules), &counter);
+  GFZ_TIMED(ctx, "inverse_delta",
+            launch_inverse_delta(g.second.ptr, nrules, off.ptr, 1, desc, counter, ctx.dstatus(), st));
+  ctx.read_status();
+  ctx.check_status("rule decode");
+}
+
+void load_encoded(Context &ctx, Grammar &g, const int32_t *enc, const std::vector<uint64_t> &off) {
+  cudaStream_t st = ctx.stream();
+  if (off.empty() || off[0] != 0) throw std::invalid_argument("encoded offsets must start at 0");
+  const uint64_t nt = off.size() - 1, m = off.back();
+  g.ntrav = nt;
+  g.h_off = off;
+  g.off.resize(nt + 1);
+  cuda_check(cudaMemcpyAsync(g.off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "offsets upload");
+  g.enc.resize(std::max<uint64_t>(m, 1));
+  g.enc.size = m;
+  if (m) cuda_check(cudaMemcpyAsync(g.enc.ptr, enc, m * 4, cudaMemcpyHostToDevice, st), "stream upload");
+}
+
+static void ensure_rule_lengths(Context &ctx, Grammar &g) {
+  if (g.rlen_ready) return;
+  cudaStream_t st = ctx.stream();
+  const uint64_t R = g.nrules;
+  g.rlen.resize(std::max<uint64_t>(R, 1));
+  if (R) {
+    // the compressor's rulebook (or a compression-side Grammar) provides the
+    // columns: derive them when only packed rules exist
+    if (g.first.size != R) {
+      g.first.resize(R);
+      g.second.resize(R);
+      g.first.size = g.second.size = R;
+      GFZ_TIMED(ctx, "split_rules",
+                (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, g.first.ptr, g.second.ptr)));
+    }
+    cuda_check(cudaMemsetAsync(g.rlen.ptr, 0, R * sizeof(uint32_t), st), "rlen clear");
+    uint64_t prev_open = UINT64_MAX;
+    for (int pass = 0;; ++pass) {
+      ctx.reset_status();
+      GFZ_TIMED(ctx, "rule_len", launch_rule_len_pass(g.first.ptr, g.second.ptr, R, g.layer_start, g.rlen.ptr,
+                                                      ctx.dstatus(), st));
+      const DevStatus &s = ctx.read_status();
+      ctx.check_status("rule lengths");
+      const uint64_t open = s.u64[6];
+      if (open == 0) break;
+      if (open >= prev_open)
+        throw std::runtime_error("rule lengths do not resolve: the rulebook references itself");
+      prev_open = open;
+    }
+  }
+  g.rlen_ready = true;
+}
+
+void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVec<int32_t> &out,
+                       std::vector<uint64_t> &out_off) {
+  cudaStream_t st = ctx.stream();
+  if (t1 < t0 || t1 > g.ntrav) throw std::out_of_range("traversal range out of bounds");
+  ensure_rule_lengths(ctx, g);
+  const uint64_t e0 = g.h_off[t0], e1 = g.h_off[t1];
+  const uint64_t m = e1 - e0;
+  const uint64_t nt = t1 - t0;
+  DevVec<uint64_t> pos(st), d_out_off(st);
+  pos.resize(m + 1);
+  d_out_off.resize(nt + 1);
+  uint64_t total = 0;
+  if (m) {
+    ctx.reset_status();
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(scan_num_tiles(m), &counter);
+    GFZ_TIMED_B(ctx, "symbol_positions", 12.0 * m, launch_symbol_positions(g.enc.ptr + e0, m, g.layer_start, g.nrules,
+                                                               g.rlen.ptr, pos.ptr, desc, counter, ctx.dstatus(), st));
+  } else {
+    cuda_check(cudaMemsetAsync(pos.ptr, 0, sizeof(uint64_t), st), "pos clear");
+  }
+  GFZ_TIMED(ctx, "gather_pos", (k_gather_pos<<<grid_for(nt + 1, 256), 256, 0, st>>>(
+                                   pos.ptr, g.off.ptr + t0, nt + 1, e0, d_out_off.ptr)));
+  out_off.resize(nt + 1);
+  cuda_check(cudaMemcpyAsync(out_off.data(), d_out_off.ptr, (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
+             "offsets download");
+  const DevStatus &s = ctx.read_status();
+  ctx.check_status("expansion offsets");
+  (void)s;
+  total = out_off[nt];
+  out.resize(std::max<uint64_t>(total, 1));
+  out.size = total;
+  if (m) {
+    GFZ_TIMED_B(ctx, "expand", 12.0 * m + 4.0 * total, launch_expand(g.enc.ptr + e0, m, pos.ptr, g.first.ptr, g.second.ptr, g.nrules,
+                                           g.layer_start, out.ptr, ctx.dstatus(), st));
+  }
+  for (int r = 0; r < g.delta_round && total; ++r) {
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(scan_num_tiles(total), &counter);
+    GFZ_TIMED_B(ctx, "inverse_delta", 8.0 * total,
+              launch_inverse_delta(out.ptr, total, d_out_off.ptr, nt, desc, counter, ctx.dstatus(), st));
+  }
+  ctx.read_status();
+  ctx.check_status("expansion");
+}
+
+uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uint64_t> &off,
+                   const TextPieces &pieces, int mode, DevVec<char> &text) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t nt = off.size() - 1;
+  const uint64_t n = off.back();
+  if (n == 0) {
+    // no steps at all: every line is fixed text (all prefixes + tail)
+    std::string all;
+    for (uint64_t t = 0; t < nt; ++t) {
+      all.append(pieces.blob, pieces.pre_off[t], pieces.pre_off[t + 1] - pieces.pre_off[t]);
+      all.append(pieces.blob, pieces.suf_off[t], pieces.suf_off[t + 1] - pieces.suf_off[t]);
+    }
+    all += pieces.tail;
+    text.resize(std::max<uint64_t>(all.size(), 1));
+    text.size = all.size();
+    if (!all.empty())
+      cuda_check(cudaMemcpyAsync(text.ptr, all.data(), all.size(), cudaMemcpyHostToDevice, st), "text upload");
+    cuda_check(cudaStreamSynchronize(st), "stream sync");
+    return all.size();
+  }
+  DevVec<uint64_t> d_off(st), d_pre(st), d_suf(st);
+  DevVec<char> d_blob(st), d_tail(st);
+  d_off.resize(nt + 1);
+  d_pre.resize(nt + 1);
+  d_suf.resize(nt + 1);
+  d_blob.resize(std::max<size_t>(pieces.blob.size(), 1));
+  d_tail.resize(std::max<size_t>(pieces.tail.size(), 1));
+  cuda_check(cudaMemcpyAsync(d_off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  cuda_check(cudaMemcpyAsync(d_pre.ptr, pieces.pre_off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  cuda_check(cudaMemcpyAsync(d_suf.ptr, pieces.suf_off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  if (!pieces.blob.empty())
+    cuda_check(cudaMemcpyAsync(d_blob.ptr, pieces.blob.data(), pieces.blob.size(), cudaMemcpyHostToDevice, st),
+               "upload");
+  if (!pieces.tail.empty())
+    cuda_check(cudaMemcpyAsync(d_tail.ptr, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
+               "upload");
+  const uint64_t bound = n * 12 + pieces.blob.size() + pieces.tail.size() + 64;
+  text.resize(bound);
+  TextMeta meta{d_blob.ptr, d_pre.ptr, d_suf.ptr, d_tail.ptr, (uint64_t)pieces.tail.size(), mode};
+  ctx.reset_status();
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(text_num_tiles(n), &counter);
+  GFZ_TIMED_B(ctx, "emit_text", 4.0 * n,
+            launch_emit_text(x.ptr, n, d_off.ptr, nt, meta, text.ptr, desc, counter, ctx.dstatus(), st));
+  const DevStatus &s = ctx.read_status();
+  ctx.check_status("text emission");
+  text.size = s.u64[7];
+  ctx.add_bytes("emit_text", (double)text.size);
+  return text.size;
+}
+
+uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, const TextPieces &pieces, int mode,
+                     DevVec<char> &text) {
+  DevVec<int32_t> x(ctx.stream());
+  std::vector<uint64_t> off;
+  decode_traversals(ctx, g, t0, t1, x, off);
+  return emit_text(ctx, x, off, pieces, mode, text);
+}
+
+// ---------------------------------------------------------------------------
+// Append encoding
+// ---------------------------------------------------------------------------
+void append_encode(Context &ctx, const int32_t *first, const int32_t *second, uint64_t nrules,
+                   const std::vector<Layer> &layers, int delta_round, std::vector<int32_t> &steps,
+                   const std::vector<uint64_t> &off, std::vector<uint64_t> &lens, uint32_t &max_abs) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t nt = off.size() - 1;
+  const uint64_t N = off.back();
+  DevVec<int32_t> A(st), B(st);
+  A.resize(std::max<uint64_t>(N, 1));
+  B.resize(std::max<uint64_t>(N, 1));
+  DevVec<uint64_t> d_off(st), d_len(st);
+  d_off.resize(nt + 1);
+  d_len.resize(std::max<uint64_t>(nt, 1));
+  cuda_check(cudaMemcpyAsync(d_off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  if (N) cuda_check(cudaMemcpyAsync(B.ptr, steps.data(), N * 4, cudaMemcpyHostToDevice, st), "upload");
+  ctx.reset_status();
+  for (int r = 0; r < delta_round; ++r) {
+    GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(B.ptr, A.ptr, N, d_off.ptr, nt, &ctx.dstatus()->aux, st));
+    A.swap(B);
+  }
+  // the encoded data lives in B after the swaps
+  const DevStatus &s = ctx.read_status();
+  max_abs = s.aux;
+  lens.resize(nt);
+  for (uint64_t t = 0; t < nt; ++t) lens[t] = off[t + 1] - off[t];
+  cuda_check(cudaMemcpyAsync(d_len.ptr, lens.data(), nt * 8, cudaMemcpyHostToDevice, st), "upload");
+  if (nrules && nt) {
+    DevVec<int32_t> df(st), dsn(st);
+    df.resize(nrules);
+    dsn.resize(nrules);
+    cuda_check(cudaMemcpyAsync(df.ptr, first, nrules * 4, cudaMemcpyHostToDevice, st), "upload");
+    cuda_check(cudaMemcpyAsync(dsn.ptr, second, nrules * 4, cudaMemcpyHostToDevice, st), "upload");
+    Table tab(st);
+    for (const Layer &L : layers) {
+      const uint64_t count = (uint64_t)(L.end - L.start);
+      const uint64_t lo = L.k == 0 ? 0 : L.flat_off / (uint64_t)L.k;
+      if (lo + count > nrules) throw std::runtime_error("Add-haplotypes workflow error: rule column is truncated");
+      const uint64_t cap = next_pow2(std::max<uint64_t>(2 * count + 1024, 1u << 12));
+      tab.prepare(cap, st, true);
+      ctx.reset_status();
+      GFZ_TIMED(ctx, "build_rule_table",
+                launch_build_rule_table(df.ptr, dsn.ptr, lo, lo + count, L.start, tab.view(cap), ctx.dstatus(), st));
+      GFZ_TIMED(ctx, "stack_encode",
+                launch_stack_encode(B.ptr, d_off.ptr, d_len.ptr, nt, tab.view(cap), ctx.dstatus(), st));
+      ctx.read_status();
+      ctx.check_status("append encoding");
+    }
+  }
+  cuda_check(cudaMemcpyAsync(lens.data(), d_len.ptr, nt * 8, cudaMemcpyDeviceToHost, st), "download");
+  if (N) cuda_check(cudaMemcpyAsync(steps.data(), B.ptr, N * 4, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+}  // namespace gfz

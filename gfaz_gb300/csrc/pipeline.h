@@ -1,0 +1,210 @@
+// Device pipeline of the GFAz transform: compression (delta + grammar
+// rounds) and decompression (expansion + inverse delta + P/W text) on one
+// GPU stream.  Host code above this layer (container, parser, workflows,
+// C ABI) never touches kernels directly.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace gfz {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+void cuda_check(cudaError_t e, const char *what);
+
+// Growable device array allocated from the stream-ordered pool.
+template <typename T>
+struct DevVec {
+  T *ptr = nullptr;
+  uint64_t size = 0, cap = 0;
+  cudaStream_t st = nullptr;
+  DevVec() = default;
+  explicit DevVec(cudaStream_t s) : st(s) {}
+  DevVec(const DevVec &) = delete;
+  DevVec &operator=(const DevVec &) = delete;
+  DevVec(DevVec &&o) noexcept { swap(o); }
+  DevVec &operator=(DevVec &&o) noexcept {
+    if (this != &o) {
+      release();
+      swap(o);
+    }
+    return *this;
+  }
+  ~DevVec() { release(); }
+  void swap(DevVec &o) noexcept {
+    std::swap(ptr, o.ptr);
+    std::swap(size, o.size);
+    std::swap(cap, o.cap);
+    std::swap(st, o.st);
+  }
+  void release() {
+    if (ptr) cudaFreeAsync(ptr, st);
+    ptr = nullptr;
+    size = cap = 0;
+  }
+  // Ensures capacity >= n (contents are kept when keep = true).
+  void reserve(uint64_t n, bool keep = false) {
+    if (n <= cap) return;
+    T *np = nullptr;
+    cuda_check(cudaMallocAsync((void **)&np, (n ? n : 1) * sizeof(T), st), "device allocation");
+    if (keep && ptr && size)
+      cuda_check(cudaMemcpyAsync(np, ptr, size * sizeof(T), cudaMemcpyDeviceToDevice, st), "device copy");
+    if (ptr) cudaFreeAsync(ptr, st);
+    ptr = np;
+    cap = n;
+  }
+  void resize(uint64_t n, bool keep = false) {
+    reserve(n, keep);
+    size = n;
+  }
+};
+
+struct KernelStat {
+  double ms = 0;
+  uint64_t launches = 0;
+  double bytes = 0;  // algorithmic bytes (input read + output written)
+};
+
+// One context per (device, stream).  Not thread-safe; calls are
+// stream-ordered and synchronous at the C-ABI boundary.
+class Context {
+ public:
+  Context(int device, cudaStream_t stream);
+  ~Context();
+  Context(const Context &) = delete;
+  Context &operator=(const Context &) = delete;
+
+  int device() const { return device_; }
+  cudaStream_t stream() const { return stream_; }
+  int sm_count() const { return sms_; }
+
+  DevStatus *dstatus() { return d_status_; }
+  // Clears the status block (err and result slots) on the stream.
+  void reset_status();
+  // Synchronises the stream and returns the host copy of the status block.
+  const DevStatus &read_status();
+  // Throws when the last read status carries an error bit.
+  void check_status(const char *stage);
+
+  // Zeroed look-back descriptors (n tiles) + tile counter.
+  unsigned long long *lookback(uint64_t tiles, uint32_t **counter);
+
+  // Kernel timing (CUDA events on the context stream).
+  bool timing = false;
+  void tbegin(const char *name, double bytes = 0);
+  void tend();
+  // Adds algorithmic bytes known only after a launch (e.g. output length).
+  void add_bytes(const char *name, double bytes);
+  std::map<std::string, KernelStat> kernel_stats();  // flushes pending events
+  void clear_kernel_stats();
+  uint64_t launches() const { return launches_; }
+  void count_launch(uint64_t n = 1) { launches_ += n; }
+
+  // tuning knobs
+  bool warp_dedup = true;
+
+ private:
+  int device_ = 0, sms_ = 152;
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  DevStatus *d_status_ = nullptr;
+  DevStatus *h_status_ = nullptr;
+  DevVec<unsigned long long> desc_;
+  DevVec<uint32_t> counter_;
+  struct Pending {
+    std::string name;
+    cudaEvent_t a, b;
+    double bytes;
+  };
+  std::vector<Pending> pending_;
+  std::vector<cudaEvent_t> event_pool_;
+  std::string open_name_;
+  double open_bytes_ = 0;
+  cudaEvent_t open_a_ = nullptr;
+  std::map<std::string, KernelStat> stats_;
+  uint64_t launches_ = 0;
+  cudaEvent_t take_event();
+};
+
+// Device-resident grammar: the result of compression, or a rulebook + encoded
+// streams loaded from a container for decompression.
+struct Grammar {
+  explicit Grammar(cudaStream_t st) : enc(st), off(st), rules(st), first(st), second(st), rlen(st) {}
+  DevVec<int32_t> enc;         // encoded traversals back to back
+  DevVec<uint64_t> off;        // ntrav + 1 offsets into enc
+  std::vector<uint64_t> h_off; // host copy of off
+  uint64_t ntrav = 0;
+  DevVec<long long> rules;     // packed rulebook (index = id - layer_start)
+  DevVec<int32_t> first, second;  // decoded rule columns (decode side)
+  DevVec<uint32_t> rlen;       // rule expansion lengths (decode side)
+  uint64_t nrules = 0;
+  uint32_t layer_start = 0, next_id = 0;
+  int delta_round = 1;
+  int rounds_done = 0;
+  bool rlen_ready = false;
+};
+
+struct EncodeParams {
+  int rounds = 8;
+  int delta_round = 1;
+};
+
+// Compresses traversals steps[off[t] .. off[t+1]) (device pointer; ntrav + 1
+// host offsets).  The input is not modified.
+void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
+                       const EncodeParams &p, Grammar &g);
+
+// Splits the packed rulebook into first/second columns on the device and
+// delta-codes each column (compression_utils.cpp:165-193).
+void rule_columns_delta(Context &ctx, const Grammar &g, DevVec<int32_t> &first, DevVec<int32_t> &second);
+
+// Loads decoded rule columns (host) into g.first/second.
+void load_rules(Context &ctx, Grammar &g, const int32_t *first, const int32_t *second, uint64_t nrules,
+                uint32_t min_id);
+
+// Uploads encoded traversals (host data, ntrav + 1 offsets) into g.
+void load_encoded(Context &ctx, Grammar &g, const int32_t *enc, const std::vector<uint64_t> &off);
+
+// Expands traversals [t0, t1) of g (with inverse delta) into out (device),
+// returning expanded offsets (host, t1 - t0 + 1 entries, relative).
+void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVec<int32_t> &out,
+                       std::vector<uint64_t> &out_off);
+
+// Per-traversal text pieces (host) for the text kernel.
+struct TextPieces {
+  std::string blob;
+  std::vector<uint64_t> pre_off, suf_off;  // ntrav + 1
+  std::string tail;
+};
+
+// Emits P (mode 0) or W (mode 1) lines for decoded traversals x/off (device
+// data, host offsets) into a device text buffer; returns the size.
+uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uint64_t> &off,
+                   const TextPieces &pieces, int mode, DevVec<char> &text);
+
+// Decode + text for traversals [t0, t1) of g: the fused convenience path.
+uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, const TextPieces &pieces, int mode,
+                     DevVec<char> &text);
+
+// Append encoding with a stored rulebook (one stack-encoder pass per layer).
+struct Layer {
+  int k;
+  uint32_t start, end;
+  uint64_t flat_off, count;
+};
+// steps: raw appended traversals (host), encoded in place; lens updated.
+// Returns max |delta| seen (for the collision check).
+void append_encode(Context &ctx, const int32_t *first, const int32_t *second, uint64_t nrules,
+                   const std::vector<Layer> &layers, int delta_round, std::vector<int32_t> &steps,
+                   const std::vector<uint64_t> &off, std::vector<uint64_t> &lens, uint32_t &max_abs);
+
+}  // namespace gfz

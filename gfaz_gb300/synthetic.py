@@ -203,8 +203,8 @@ def cfg2_stream(seed: int = 2, n_segments: int = 8_000_000, n_paths: int = 90,
     base += 1
     nseg = int(seg_per_blk.sum())
     thr = {kk: _zipf_thresholds(kk, zipf_s) for kk in (2, 3, 4)}
-    paths = []
-    for p in range(n_paths):
+
+    def one_path(p):
         r = rng_u64(seed, 1000 + p, 2 * nblk)
         hi = r[:nblk] >> np.uint64(32)
         choice = np.zeros(nblk, np.int64)
@@ -220,11 +220,26 @@ def cfg2_stream(seed: int = 2, n_segments: int = 8_000_000, n_paths: int = 90,
         revs = np.zeros(2 * nblk, bool)
         starts[0::2], lengths[0::2] = base, bubble_every
         starts[1::2], lengths[1::2], revs[1::2] = a_start, a_len, rev
-        paths.append(_expand_runs(starts, lengths, revs))
+        return _expand_runs(starts, lengths, revs)
+
+    paths = _parallel_map(one_path, range(n_paths))
     lens = np.array([len(x) for x in paths], dtype=np.uint64)
     off = np.zeros(n_paths + 1, np.uint64)
     np.cumsum(lens, out=off[1:])
     return np.concatenate(paths), off, nseg
+
+
+def _parallel_map(fn, items):
+    """Order-preserving map over a thread pool (numpy releases the GIL in
+    the array kernels used by the generators)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    items = list(items)
+    workers = max(1, min(len(items), os.cpu_count() or 1, 16))
+    if workers == 1:
+        return [fn(x) for x in items]
+    with ThreadPoolExecutor(workers) as ex:
+        return list(ex.map(fn, items))
 
 
 def cfg3_stream(seed: int = 3, n_backbone: int = 1_666_667, n_walks: int = 2000,

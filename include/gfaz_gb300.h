@@ -1,0 +1,205 @@
+/*
+ * gfaz_gb300.h - C ABI of the GB300 GFAz transform library (libgfaz_gb300.so).
+ *
+ * Plain C: opaque handles, plain pointers and sizes, integer status codes.
+ * No exception crosses the boundary; on failure a function returns a
+ * negative gfz_status and gfz_last_error() gives the message (thread-local),
+ * which carries the same prefixes as the reference's exceptions
+ * ("GFAZ serialization error: ", "Extraction workflow error: ", ...).
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * the babyplutokurt/GFAz sources).  Traversal transforms (delta coding,
+ * grammar rounds, expansion, inverse delta, P/W text) run on the GPU; there
+ * is no CPU fallback and calls fail with GFZ_ERR_CUDA when no GPU is usable.
+ * Host-only entry points (container I/O, inspection) work without a GPU.
+ *
+ * Buffers returned through `char **out` / `void **out` are allocated by the
+ * library and released with gfz_free().
+ */
+#ifndef GFAZ_GB300_H
+#define GFAZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GFZ_OK = 0,
+  GFZ_ERR_INVALID = -1,   /* bad argument */
+  GFZ_ERR_IO = -2,        /* file cannot be opened / read / written */
+  GFZ_ERR_FORMAT = -3,    /* malformed .gfaz / GFA / append file */
+  GFZ_ERR_CUDA = -4,      /* CUDA runtime failure or no usable GPU */
+  GFZ_ERR_DEVICE = -5,    /* a kernel reported an error (table full, timeout ...) */
+  GFZ_ERR_NOT_FOUND = -6, /* requested path / walk does not exist */
+  GFZ_ERR_BUFFER = -7,    /* caller buffer too small (*size holds the need) */
+  GFZ_ERR_INTERNAL = -8
+} gfz_status;
+
+#define GFZ_WHERE_HOST 0
+#define GFZ_WHERE_DEVICE 1
+#define GFZ_P_LINES 0
+#define GFZ_W_LINES 1
+
+typedef struct gfz_context gfz_context;       /* one GPU + one CUDA stream */
+typedef struct gfz_compressed gfz_compressed; /* a .gfaz container (host) */
+typedef struct gfz_grammar gfz_grammar;       /* device-resident grammar */
+typedef struct gfz_graph gfz_graph;           /* decompressed graph (host) */
+
+/* ---- library ------------------------------------------------------------ */
+const char *gfz_last_error(void);
+const char *gfz_version(void);
+void gfz_free(void *p);
+/* 1 when a CUDA device is usable (gfa_compression.has_gpu_backend,
+ * src/python/bindings.cpp:94-100). */
+int gfz_has_gpu(void);
+/* zstd library version in use (entropy stage), 0 if unavailable. */
+unsigned gfz_zstd_version(void);
+
+/* ---- contexts ------------------------------------------------------------ */
+/* cuda_stream may be NULL (the context creates its own stream). */
+gfz_status gfz_context_create(int device, void *cuda_stream, gfz_context **out);
+void gfz_context_destroy(gfz_context *ctx);
+/* Records CUDA events around every kernel launch when enabled. */
+gfz_status gfz_context_set_timing(gfz_context *ctx, int enabled);
+/* JSON object {"kernel": {"ms": .., "launches": .., "bytes": ..}, ...} plus
+ * "_launches": total kernels launched since the last reset. */
+gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, size_t *len);
+/* Tuning switch: warp-level de-duplication of pair inserts (default 1). */
+gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
+
+/* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
+/* compress_gfa, include/workflows/compression_workflow.hpp:7-9;
+ * python compress_file, src/python/bindings.cpp:661-667.  threshold is
+ * accepted and, as in the reference, only warns when > 2. */
+gfz_status gfz_compress_file(gfz_context *ctx, const char *gfa_path, int rounds, uint64_t threshold,
+                             int delta_round, int threads, int show_stats, gfz_compressed **out);
+/* serialize_compressed_data, include/codec/serialization.hpp:13-14 */
+gfz_status gfz_serialize(const gfz_compressed *c, const char *path);
+gfz_status gfz_serialize_buffer(const gfz_compressed *c, void **out, size_t *len);
+/* deserialize_compressed_data, include/codec/serialization.hpp:15-16 */
+gfz_status gfz_deserialize(const char *path, gfz_compressed **out);
+gfz_status gfz_deserialize_buffer(const void *data, size_t len, gfz_compressed **out);
+void gfz_compressed_free(gfz_compressed *c);
+/* write_gfa_from_compressed_data, include/io/gfa_writer.hpp:9-11 and the
+ * GPU writer write_gfa_from_compressed_data_gpu,
+ * include/gpu/io/gfa_writer_gpu.hpp:9-12 (streaming order H,S,L,J,C,P,W). */
+gfz_status gfz_write_gfa(gfz_context *ctx, const gfz_compressed *c, const char *out_path, int threads);
+gfz_status gfz_gfa_text(gfz_context *ctx, const gfz_compressed *c, int threads, char **out, size_t *len);
+/* extract_path_lines_by_name, include/workflows/extraction_workflow.hpp:19-21:
+ * lines concatenated in request order. */
+gfz_status gfz_extract_path_lines(gfz_context *ctx, const gfz_compressed *c, const char *const *names, size_t n,
+                                  int threads, char **out, size_t *len);
+typedef struct {
+  const char *sample_id;
+  uint32_t hap_index;
+  const char *seq_id;
+  int64_t seq_start; /* -1 prints '*' */
+  int64_t seq_end;
+} gfz_walk_key;
+/* extract_walk_lines, extraction_workflow.hpp:35-38 */
+gfz_status gfz_extract_walk_lines(gfz_context *ctx, const gfz_compressed *c, const gfz_walk_key *keys, size_t n,
+                                  int threads, char **out, size_t *len);
+/* extract_walk_lines_by_name, extraction_workflow.hpp:40-43 */
+gfz_status gfz_extract_walk_lines_by_name(gfz_context *ctx, const gfz_compressed *c, const char *const *names,
+                                          size_t n, int threads, char **out, size_t *len);
+/* add_haplotypes, include/workflows/add_haplotypes_workflow.hpp:9-10 (in place) */
+gfz_status gfz_add_haplotypes(gfz_context *ctx, gfz_compressed *c, const char *path, int threads);
+/* decompress_gfa, include/workflows/decompression_workflow.hpp:8-9 */
+gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out);
+void gfz_graph_free(gfz_graph *g);
+
+/* ---- container / graph inspection (host only) ---------------------------- */
+typedef struct {
+  uint64_t num_paths, num_walks, num_links, num_jumps, num_containments, num_layers, total_rules;
+  uint32_t min_rule_id, reserved;
+  int32_t delta_round;
+  int32_t reserved2;
+} gfz_container_info;
+gfz_status gfz_compressed_info(const gfz_compressed *c, gfz_container_info *info);
+/* Layer ranges as rows (k, start_id, end_id, flattened_offset, element_count). */
+gfz_status gfz_compressed_layers(const gfz_compressed *c, int64_t *rows, size_t max_rows);
+/* Named u32 vectors: "sequence_lengths", "original_path_lengths",
+ * "walk_lengths", "original_walk_lengths". */
+gfz_status gfz_compressed_u32(const gfz_compressed *c, const char *field, const uint32_t **data, size_t *n);
+/* zstd-decoded bytes of a named block ("rules_first", "rules_second",
+ * "paths", "walks", "names", "name_lengths", ...). */
+gfz_status gfz_compressed_block(const gfz_compressed *c, const char *field, void **out, size_t *len);
+/* Steps (paths then walks share no buffer): kind 0 = paths, 1 = walks. */
+gfz_status gfz_graph_traversals(const gfz_graph *g, int kind, const int32_t **steps, const uint64_t **offsets,
+                                uint64_t *ntrav);
+/* Newline-joined string fields: "path_names", "path_overlaps",
+ * "walk_sample_ids", "walk_seq_ids", "header". */
+gfz_status gfz_graph_strings(const gfz_graph *g, const char *field, char **out, size_t *len);
+gfz_status gfz_graph_walk_numbers(const gfz_graph *g, const uint32_t **haps, const int64_t **starts,
+                                  const int64_t **ends, uint64_t *n);
+gfz_status gfz_graph_counts(const gfz_graph *g, uint64_t *segments, uint64_t *links, uint64_t *jumps,
+                            uint64_t *containments);
+
+/* ---- the transform hot path (device-resident) ---------------------------- */
+/* Replaces the reference GPU compressor's compress_gpu_graph /
+ * run_path_compression_gpu (include/gpu/compression/compression_workflow_gpu.hpp:84-99)
+ * with CPU-identical semantics: delta_round rounds of per-traversal delta
+ * coding, then up to `rounds` grammar rounds.  steps / offsets describe
+ * traversals steps[offsets[t] .. offsets[t+1]) (paths first, then walks);
+ * offsets are host memory (ntrav + 1 entries); steps live where `where`
+ * says.  threshold is accepted and ignored beyond a warning, as in the
+ * reference (src/grammar/rule_generator.cpp:242-246). */
+gfz_status gfz_encode(gfz_context *ctx, const int32_t *steps, const uint64_t *offsets, uint64_t ntrav, int rounds,
+                      uint64_t threshold, int delta_round, int where, gfz_grammar **out);
+typedef struct {
+  uint64_t ntrav, encoded_len, num_rules;
+  uint32_t layer_start, next_id;
+  int32_t rounds_done, delta_round;
+} gfz_grammar_info;
+gfz_status gfz_grammar_info_get(const gfz_grammar *g, gfz_grammar_info *info);
+/* Copies the encoded stream (encoded_len), its offsets (ntrav + 1, host) and
+ * the packed rulebook (num_rules int64 keys, index = id - layer_start).  Any
+ * pointer may be NULL. */
+gfz_status gfz_grammar_copy(gfz_context *ctx, const gfz_grammar *g, int32_t *encoded, uint64_t *offsets,
+                            int64_t *rules, int where);
+/* Rule columns as stored in the container: first/second halves of each key,
+ * each delta coded over the rulebook (compression_utils.cpp:165-193). */
+gfz_status gfz_grammar_rule_columns(gfz_context *ctx, const gfz_grammar *g, int32_t *first, int32_t *second,
+                                    int where);
+/* Decompression side: loads a stored rulebook (delta-coded columns) and
+ * encoded traversals.  Replaces prepare_gpu_traversal_rulebook /
+ * decompress_to_gpu_layout (include/gpu/decompression/decompression_workflow_gpu.hpp:46-48). */
+gfz_status gfz_grammar_load(gfz_context *ctx, const int32_t *encoded, const uint64_t *offsets, uint64_t ntrav,
+                            const int32_t *rules_first, const int32_t *rules_second, uint64_t num_rules,
+                            uint32_t min_rule_id, int delta_round, int where, gfz_grammar **out);
+void gfz_grammar_free(gfz_grammar *g);
+/* Expansion + inverse delta of traversals [t0, t1).  out receives the steps
+ * (capacity `cap` elements), offsets_out (host, t1 - t0 + 1 entries) their
+ * offsets; *n_out is the number of steps.  GFZ_ERR_BUFFER when cap is too
+ * small. */
+gfz_status gfz_decode(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64_t t1, int32_t *out, uint64_t cap,
+                      uint64_t *n_out, uint64_t *offsets_out, int where);
+/* Line metadata for text emission.  P: names + overlaps (NULL entry or NULL
+ * array = ""); W: names are sample ids, plus hap/seq_id/start/end. */
+typedef struct {
+  int mode; /* GFZ_P_LINES or GFZ_W_LINES */
+  const char *const *names;
+  const char *const *overlaps;
+  const uint32_t *hap_indices;
+  const char *const *seq_ids;
+  const int64_t *seq_starts;
+  const int64_t *seq_ends;
+} gfz_line_meta;
+/* Expansion + inverse delta + GFA text of traversals [t0, t1) (the rolling
+ * writer's path, src/gpu/decompression/path_decompression_gpu_rolling.cpp:215-370
+ * and format_*_line_numeric, src/io/gfa_write_utils.cpp:238-290).  With
+ * out == NULL the text stays in a device buffer owned by `g`
+ * (gfz_grammar_text gives its address); otherwise it is copied to out
+ * (capacity cap bytes, host or device per `where`). */
+gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64_t t1, const gfz_line_meta *meta,
+                           char *out, uint64_t cap, uint64_t *size, int where);
+gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFAZ_GB300_H */
