@@ -123,6 +123,70 @@ __device__ __forceinline__ unsigned long long lookback_sum(unsigned long long *d
   return excl;
 }
 
+// Warp-parallel decoupled look-back, executed by all 32 lanes of one warp.
+// Lane l inspects tile (tile - 1 - l - 32k); the aggregates between the tile
+// and the nearest inclusive descriptor are combined with an order-preserving
+// shuffle reduction.  Op supplies the scan monoid:
+//   T  aggregate (a function of the incoming state); S concrete state
+//   identity(), compose(a, b) = "a then b", apply(f, s), initial()
+//   encode_agg/decode_agg, encode_incl/decode_incl (62-bit payloads)
+//   shfl_down(T, o), shfl(S, src)
+// Publishes this tile's aggregate, then its inclusive state, and returns the
+// exclusive state (the state before this tile) on every lane.
+template <class Op>
+__device__ __forceinline__ typename Op::S warp_lookback(unsigned long long *desc, uint64_t tile,
+                                                        const typename Op::T &agg, uint32_t *err) {
+  using T = typename Op::T;
+  using S = typename Op::S;
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {
+    const S s0 = Op::initial();
+    if (lane == 0) st_release(desc, kDescIncl | (Op::encode_incl(Op::apply(agg, s0)) & kDescPayload));
+    return s0;
+  }
+  if (lane == 0) st_release(desc + tile, kDescAgg | (Op::encode_agg(agg) & kDescPayload));
+  T acc = Op::identity();
+  int64_t base = (int64_t)tile - 1;
+  for (;;) {
+    const int64_t j = base - lane;
+    unsigned long long d = kDescIncl | (Op::encode_incl(Op::initial()) & kDescPayload);
+    if (j >= 0) d = wait_desc(desc, (uint64_t)j, err);
+    const uint32_t incl = __ballot_sync(0xffffffffu, (d & kDescMask) == kDescIncl);
+    const int L = incl ? __ffs(incl) - 1 : 32;
+    T f = lane < L ? Op::decode_agg(d & kDescPayload) : Op::identity();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T other = Op::shfl_down(f, o);
+      if (lane + o < 32) f = Op::compose(other, f);
+    }
+    const T window = Op::shfl0(f);
+    acc = Op::compose(window, acc);
+    if (L < 32) {
+      const unsigned long long dl = __shfl_sync(0xffffffffu, d, L);
+      const S excl = Op::apply(acc, Op::decode_incl(dl & kDescPayload));
+      if (lane == 0) st_release(desc + tile, kDescIncl | (Op::encode_incl(Op::apply(agg, excl)) & kDescPayload));
+      return excl;
+    }
+    base -= 32;
+  }
+}
+
+// u64 running sum.
+struct SumOp {
+  using T = unsigned long long;
+  using S = unsigned long long;
+  __device__ static T identity() { return 0; }
+  __device__ static T compose(T a, T b) { return a + b; }
+  __device__ static S apply(T f, S s) { return s + f; }
+  __device__ static S initial() { return 0; }
+  __device__ static unsigned long long encode_agg(T a) { return a; }
+  __device__ static T decode_agg(unsigned long long d) { return d; }
+  __device__ static unsigned long long encode_incl(S s) { return s; }
+  __device__ static S decode_incl(unsigned long long d) { return d; }
+  __device__ static T shfl_down(T a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+  __device__ static T shfl0(T a) { return __shfl_sync(0xffffffffu, a, 0); }
+};
+
 // Dynamic tile index: guarantees that every tile a block waits on has
 // already been claimed by a running (or finished) block.
 __device__ __forceinline__ uint32_t claim_tile(uint32_t *counter) {
@@ -161,6 +225,12 @@ __device__ __forceinline__ uint64_t mark_heads(const uint64_t *off, uint64_t ntr
   }
   return tlo;
 }
+
+// Padded shared-memory index: one spare word per 32, so that both striped
+// access (consecutive i per lane) and blocked access (lane t reading
+// t*ITEMS + k) hit 32 distinct banks.
+__device__ __forceinline__ uint32_t padi(uint32_t i) { return i + (i >> 5); }
+__host__ __device__ constexpr uint32_t padded_size(uint32_t n) { return n + (n >> 5) + 1; }
 
 __device__ __forceinline__ bool bit_at(const uint32_t *bits, uint32_t b) {
   return (bits[b >> 5] >> (b & 31)) & 1u;

@@ -90,24 +90,27 @@ __global__ void __launch_bounds__(BLOCK) k_symbol_positions(const int32_t *__res
                                                             unsigned long long *desc, uint32_t *tile_counter,
                                                             DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ uint32_t sl[TILE];
+  __shared__ uint32_t sl[padded_size(TILE)];
   __shared__ unsigned long long s_excl;
   const uint32_t tile = claim_tile(tile_counter);
   const uint64_t base = (uint64_t)tile * TILE;
   const uint32_t len = (uint32_t)min((uint64_t)TILE, m - base);
   for (uint32_t j = threadIdx.x; j < len; j += BLOCK) {
     const uint32_t a = abs32(enc[base + j]);
-    sl[j] = is_rule(a, min_id, nrules) ? rlen[a - min_id] : 1u;
+    sl[padi(j)] = is_rule(a, min_id, nrules) ? rlen[a - min_id] : 1u;
   }
   __syncthreads();
   unsigned long long mine = 0;
   const uint32_t j0 = threadIdx.x * ITEMS;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k)
-    if (j0 + k < len) mine += sl[j0 + k];
+    if (j0 + k < len) mine += sl[padi(j0 + k)];
   unsigned long long total;
   unsigned long long ex = block_excl_sum<BLOCK>(mine, total);
-  if (threadIdx.x == 0) s_excl = lookback_sum(desc, tile, total, &status->err);
+  if (threadIdx.x < 32) {
+    const unsigned long long e = warp_lookback<SumOp>(desc, tile, total, &status->err);
+    if (threadIdx.x == 0) s_excl = e;
+  }
   __syncthreads();
   unsigned long long p = s_excl + ex;
   // write through shared memory for coalesced stores
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(BLOCK) k_symbol_positions(const int32_t *__res
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
     vals[k] = p;
-    if (j0 + k < len) p += sl[j0 + k];
+    if (j0 + k < len) p += sl[padi(j0 + k)];
   }
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k)
@@ -175,6 +178,28 @@ struct SegAgg {
 __device__ __forceinline__ SegAgg seg_compose(const SegAgg &a, const SegAgg &b) {
   return b.f ? b : SegAgg{a.f, a.sum + b.sum};
 }
+// Segmented-sum monoid for the look-back: state = running value at the
+// end of the previous tile (wrapping int32 arithmetic).
+struct SegOp {
+  using T = SegAgg;
+  using S = uint32_t;
+  __device__ static T identity() { return SegAgg{0u, 0u}; }
+  __device__ static T compose(const T &a, const T &b) { return seg_compose(a, b); }
+  __device__ static S apply(const T &f, S s) { return f.f ? f.sum : s + f.sum; }
+  __device__ static S initial() { return 0u; }
+  __device__ static unsigned long long encode_agg(const T &a) {
+    return ((unsigned long long)a.f << 32) | a.sum;
+  }
+  __device__ static T decode_agg(unsigned long long d) { return SegAgg{(uint32_t)(d >> 32) & 1u, (uint32_t)d}; }
+  __device__ static unsigned long long encode_incl(S s) { return s; }
+  __device__ static S decode_incl(unsigned long long d) { return (uint32_t)d; }
+  __device__ static T shfl_down(const T &a, int o) {
+    return SegAgg{__shfl_down_sync(0xffffffffu, a.f, o), __shfl_down_sync(0xffffffffu, a.sum, o)};
+  }
+  __device__ static T shfl0(const T &a) {
+    return SegAgg{__shfl_sync(0xffffffffu, a.f, 0), __shfl_sync(0xffffffffu, a.sum, 0)};
+  }
+};
 
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n, const uint64_t *__restrict__ off,
@@ -182,7 +207,7 @@ __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n,
                                                          uint32_t *tile_counter, DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   constexpr int NW = BLOCK / 32;
-  __shared__ uint32_t sv[TILE];
+  __shared__ uint32_t sv[padded_size(TILE)];
   __shared__ uint32_t hb[TILE / 32 + 2];
   __shared__ uint64_t s_tlo;
   __shared__ SegAgg s_w[NW];
@@ -191,7 +216,7 @@ __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n,
   const uint64_t base = (uint64_t)tile * TILE;
   const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
   for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
-  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[j] = (uint32_t)x[base + j];
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[padi(j)] = (uint32_t)x[base + j];
   mark_heads(off, ntrav, base, len, hb, &s_tlo);
   __syncthreads();
   const uint32_t j0 = threadIdx.x * ITEMS;
@@ -200,8 +225,8 @@ __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n,
   for (int k = 0; k < ITEMS; ++k) {
     const uint32_t j = j0 + k;
     if (j < len) {
-      if (bit_at(hb, j)) a = SegAgg{1u, sv[j]};
-      else a.sum += sv[j];
+      if (bit_at(hb, j)) a = SegAgg{1u, sv[padi(j)]};
+      else a.sum += sv[padi(j)];
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -221,22 +246,9 @@ __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n,
     total = seg_compose(total, s_w[w]);
   }
   ex = seg_compose(wpre, ex);
-  if (threadIdx.x == 0) {
-    uint32_t carry = 0;
-    if (tile == 0) {
-      st_release(desc, kDescIncl | total.sum);
-    } else {
-      st_release(desc + tile, kDescAgg | ((unsigned long long)total.f << 32) | total.sum);
-      uint64_t j = tile;
-      while (j > 0) {
-        --j;
-        const unsigned long long d = wait_desc(desc, j, &status->err);
-        carry += (uint32_t)d;
-        if ((d & kDescMask) == kDescIncl || ((d >> 32) & 1u)) break;
-      }
-      st_release(desc + tile, kDescIncl | (uint32_t)(total.f ? total.sum : carry + total.sum));
-    }
-    s_carry = carry;
+  if (warp == 0) {
+    const uint32_t carry = warp_lookback<SegOp>(desc, tile, total, &status->err);
+    if (lane == 0) s_carry = carry;
   }
   __syncthreads();
   uint32_t run = ex.f ? ex.sum : s_carry + ex.sum;
@@ -244,12 +256,12 @@ __global__ void __launch_bounds__(BLOCK) k_inverse_delta(int32_t *x, uint64_t n,
   for (int k = 0; k < ITEMS; ++k) {
     const uint32_t j = j0 + k;
     if (j < len) {
-      run = bit_at(hb, j) ? sv[j] : run + sv[j];
-      sv[j] = run;
+      run = bit_at(hb, j) ? sv[padi(j)] : run + sv[padi(j)];
+      sv[padi(j)] = run;
     }
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) x[base + j] = (int32_t)sv[j];
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) x[base + j] = (int32_t)sv[padi(j)];
 }
 
 // ---------------------------------------------------------------------------
@@ -321,13 +333,13 @@ __global__ void __launch_bounds__(BLOCK) k_emit_text(const int32_t *__restrict__
                                                      char *__restrict__ text, unsigned long long *desc,
                                                      uint32_t *tile_counter, DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ int32_t sv[TILE];
+  __shared__ int32_t sv[padded_size(TILE)];
   __shared__ __align__(16) char sbuf[kTextBuf + 32];
   __shared__ unsigned long long s_off;
   const uint32_t tile = claim_tile(tile_counter);
   const uint64_t base = (uint64_t)tile * TILE;
   const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
-  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[j] = x[base + j];
+  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[padi(j)] = x[base + j];
   __syncthreads();
   const uint32_t j0 = threadIdx.x * ITEMS;
   const bool pmode = meta.mode == 0;
@@ -347,14 +359,17 @@ __global__ void __launch_bounds__(BLOCK) k_emit_text(const int32_t *__restrict__
       const bool fst = p == __ldg(off + tt);
       const bool lst = p + 1 == __ldg(off + tt + 1);
       flags |= ((uint32_t)fst << (2 * k)) | ((uint32_t)lst << (2 * k + 1));
-      mine += dec_digits(abs32(sv[j])) + 1u + ((pmode && !lst) ? 1u : 0u);
+      mine += dec_digits(abs32(sv[padi(j)])) + 1u + ((pmode && !lst) ? 1u : 0u);
       if (fst) mine += meta.pre_off[tt + 1] - meta.pre_off[tt];
       if (lst) mine += meta.suf_off[tt + 1] - meta.suf_off[tt];
     }
   }
   unsigned long long total;
   const unsigned long long ex = block_excl_sum<BLOCK>(mine, total);
-  if (threadIdx.x == 0) s_off = lookback_sum(desc, tile, total, &status->err);
+  if (threadIdx.x < 32) {
+    const unsigned long long e = warp_lookback<SumOp>(desc, tile, total, &status->err);
+    if (threadIdx.x == 0) s_off = e;
+  }
   __syncthreads();
   const unsigned long long toff = s_off;
   const bool last_tile = base + len == n;
@@ -376,7 +391,7 @@ __global__ void __launch_bounds__(BLOCK) k_emit_text(const int32_t *__restrict__
         const uint64_t a = meta.pre_off[tt], b = meta.pre_off[tt + 1];
         for (uint64_t q = a; q < b; ++q) dst[o++] = meta.blob[q];
       }
-      const int32_t v = sv[j];
+      const int32_t v = sv[padi(j)];
       const uint32_t av = abs32(v), nd = dec_digits(av);
       if (pmode) {
         put_dec(dst + o, av, nd);

@@ -180,6 +180,32 @@ __device__ __forceinline__ unsigned long long par_encode(const ParAgg &a) {
 __device__ __forceinline__ ParAgg par_decode(unsigned long long d) {
   return ParAgg{(uint32_t)(d & 3u), (uint32_t)((d >> 2) & 0xFFFFFFu), (uint32_t)((d >> 26) & 0xFFFFFFu)};
 }
+// Run-parity monoid for the look-back: state = (x after the tile, replaced
+// positions so far).
+struct ParState {
+  uint32_t x;
+  unsigned long long c;
+};
+struct ParOp {
+  using T = ParAgg;
+  using S = ParState;
+  __device__ static T identity() { return par_identity(); }
+  __device__ static T compose(const T &a, const T &b) { return par_compose(a, b); }
+  __device__ static S apply(const T &f, const S &s) { return S{par_x(f, s.x), s.c + par_c(f, s.x)}; }
+  __device__ static S initial() { return S{0u, 0ull}; }
+  __device__ static unsigned long long encode_agg(const T &a) { return par_encode(a); }
+  __device__ static T decode_agg(unsigned long long d) { return par_decode(d); }
+  __device__ static unsigned long long encode_incl(const S &s) { return (unsigned long long)s.x | (s.c << 1); }
+  __device__ static S decode_incl(unsigned long long d) { return S{(uint32_t)(d & 1u), d >> 1}; }
+  __device__ static T shfl_down(const T &a, int o) {
+    return T{__shfl_down_sync(0xffffffffu, a.xo, o), __shfl_down_sync(0xffffffffu, a.c0, o),
+             __shfl_down_sync(0xffffffffu, a.c1, o)};
+  }
+  __device__ static T shfl0(const T &a) {
+    return T{__shfl_sync(0xffffffffu, a.xo, 0), __shfl_sync(0xffffffffu, a.c0, 0), __shfl_sync(0xffffffffu, a.c1, 0)};
+  }
+};
+
 __device__ __forceinline__ ParAgg par_shfl_up(const ParAgg &a, int delta) {
   ParAgg r;
   r.xo = __shfl_up_sync(0xffffffffu, a.xo, delta);
@@ -198,10 +224,10 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
   constexpr int NW = BLOCK / 32;
   static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
   static_assert(32 % ITEMS == 0, "a thread's candidate bits must sit in one bitmap word");
-  __shared__ int32_t sv[TILE + 1];
-  __shared__ int32_t so[TILE];
-  __shared__ uint32_t sslot[TILE];  // table slot | orientation bit (31)
-  __shared__ uint16_t lidx[TILE];
+  __shared__ int32_t sv[padded_size(TILE + 1)];
+  __shared__ int32_t so[padded_size(TILE)];
+  __shared__ uint32_t sslot[padded_size(TILE)];  // table slot | orientation bit (31)
+  __shared__ uint16_t lidx[padded_size(TILE)];
   __shared__ uint32_t hb[TILE / 32 + 2];
   __shared__ uint32_t scand[TILE / 32];  // candidate positions
   __shared__ uint32_t sused[TILE / 32];  // slot already flagged used
@@ -219,7 +245,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
     sused[j] = 0;
   }
   const uint32_t ld = len + (base + len < n ? 1u : 0u);
-  for (uint32_t j = threadIdx.x; j < ld; j += BLOCK) sv[j] = s[base + j];
+  for (uint32_t j = threadIdx.x; j < ld; j += BLOCK) sv[padi(j)] = s[base + j];
   const uint64_t tlo = mark_heads(off, ntrav, base, len, hb, &s_tlo);
   __syncthreads();
 
@@ -238,7 +264,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
       hs[k] = 0;
       cur[k] = kEmptyKey;
       if (j < len && !bit_at(hb, j + 1)) {
-        const unsigned long long key = pack2(sv[j], sv[j + 1]);
+        const unsigned long long key = pack2(sv[padi(j)], sv[padi(j + 1)]);
         const unsigned long long r = rev2(key);
         const bool fwd = key_le(key, r);
         ck[k] = fwd ? key : r;
@@ -267,7 +293,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
       const uint32_t j = threadIdx.x + k * BLOCK;
       const uint32_t fl = tab.flags[hs[k]];
       if (fl & kFlagRepeated) {
-        sslot[j] = (uint32_t)hs[k] | (((fwdb >> k) & 1u) << 31);
+        sslot[padi(j)] = (uint32_t)hs[k] | (((fwdb >> k) & 1u) << 31);
         atomicOr(&scand[j >> 5], 1u << (j & 31));
         if (fl & kFlagUsed) atomicOr(&sused[j >> 5], 1u << (j & 31));
       }
@@ -312,33 +338,12 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
   }
   excl = par_compose(wpre, excl);
 
-  if (threadIdx.x == 0) {
-    uint32_t in_x = 0;
-    unsigned long long in_c = 0;
-    if (tile == 0) {
-      st_release(desc, kDescIncl | ((unsigned long long)par_x(total, 0)) |
-                           ((unsigned long long)par_c(total, 0) << 1));
-    } else {
-      st_release(desc + tile, kDescAgg | par_encode(total));
-      ParAgg acc = par_identity();
-      uint64_t j = tile;
-      while (j > 0) {
-        --j;
-        const unsigned long long d = wait_desc(desc, j, &status->err);
-        if ((d & kDescMask) == kDescIncl) {
-          const uint32_t x = (uint32_t)(d & 1u);
-          const unsigned long long c = (d & kDescPayload) >> 1;
-          in_x = par_x(acc, x);
-          in_c = c + par_c(acc, x);
-          break;
-        }
-        acc = par_compose(par_decode(d), acc);
-      }
-      const unsigned long long out_c = in_c + par_c(total, in_x);
-      st_release(desc + tile, kDescIncl | (unsigned long long)par_x(total, in_x) | (out_c << 1));
+  if (warp == 0) {
+    const ParState in = warp_lookback<ParOp>(desc, tile, total, &status->err);
+    if (lane == 0) {
+      s_in_x = in.x;
+      s_in_c = in.c;
     }
-    s_in_x = in_x;
-    s_in_c = in_c;
   }
   __syncthreads();
   const uint32_t in_x = s_in_x;
@@ -369,16 +374,16 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
     if ((keptbits >> k) & 1u) {
       const uint32_t j = j0 + k;
       const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
-      int32_t v = sv[j];
+      int32_t v = sv[padi(j)];
       if ((xbits >> k) & 1u) {
-        const uint32_t sl = sslot[j];
+        const uint32_t sl = sslot[padi(j)];
         const uint32_t slot = sl & 0x7FFFFFFFu;
         const int32_t sym = temp_base + (int32_t)slot;
         v = (sl >> 31) ? sym : neg32(sym);
         if (!bit_at(sused, j)) atomicOr(&tab.flags[slot], kFlagUsed);
       }
-      so[lo] = v;
-      lidx[j] = (uint16_t)lo;
+      so[padi(lo)] = v;
+      lidx[padi(j)] = (uint16_t)lo;
     }
   }
   __syncthreads();
@@ -388,11 +393,11 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
   const uint32_t tile_rep = par_c(total, in_x);
   const uint32_t kept = len - in_x - tile_rep + par_x(total, in_x);
   const uint64_t out_base = base - in_c + in_x;
-  for (uint32_t j = threadIdx.x; j < kept; j += BLOCK) out[out_base + j] = so[j];
+  for (uint32_t j = threadIdx.x; j < kept; j += BLOCK) out[out_base + j] = so[padi(j)];
   const bool last_tile = base + len == n;
   for (uint64_t t = tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
     const uint64_t q = off[t];
-    if (q < base + len) new_off[t] = out_base + lidx[q - base];
+    if (q < base + len) new_off[t] = out_base + lidx[padi((uint32_t)(q - base))];
     else if (last_tile && q == n) new_off[t] = out_base + kept;
     else break;
   }

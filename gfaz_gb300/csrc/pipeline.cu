@@ -7,6 +7,8 @@
 #include "pipeline.h"
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "common.cuh"
@@ -47,6 +49,17 @@ uint64_t next_pow2(uint64_t x) {
 }
 
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
+
+// GFA_COMPRESSION_DEBUG=1 (the reference's debug switch) prints per-round
+// grammar statistics to stderr.
+bool debug_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = std::getenv("GFA_COMPRESSION_DEBUG");
+    on = (e && e[0] && e[0] != '0') ? 1 : 0;
+  }
+  return on == 1;
+}
 
 struct Table {
   DevVec<unsigned long long> keys;
@@ -326,6 +339,10 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
               launch_assign_ids(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr, U, next_id,
                                 tab.view(cap), rules.ptr + g.nrules, st));
     GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.vals.ptr, st));
+    if (debug_enabled())
+      fprintf(stderr, "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu\n",
+              round + 1, (unsigned long long)n, (unsigned long long)cap, (unsigned long long)distinct,
+              (unsigned long long)repeated, (unsigned long long)U, (unsigned long long)n_out);
     g.nrules += U;
     next_id += (uint32_t)U;
     n = n_out;
