@@ -94,7 +94,9 @@ SIGNATURES = {
     "gfz_decode": (I, [P, P, U64, U64, P, U64, PU64, P, I]),
     "gfz_decode_text": (I, [P, P, U64, U64, ctypes.POINTER(LineMeta), P, U64, PU64, I]),
     "gfz_grammar_text": (I, [P, PP, PU64]),
+    "gfz_inverse_delta_noalloc": (I, [P, P, U64, P, U64, I, P]),
 }
+NOALLOC_MAX_STEPS = 1 << 26
 
 _lib = None
 

@@ -12,6 +12,7 @@
 
 #include "host/model.h"
 #include "host/workflows.h"
+#include "noalloc.h"
 #include "pipeline.h"
 
 struct gfz_context {
@@ -610,6 +611,14 @@ gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint
     require(g && device_text && size, "NULL argument");
     *device_text = g->text.ptr;
     *size = g->text_size;
+  });
+}
+
+gfz_status gfz_inverse_delta_noalloc(const int32_t *steps_in, int32_t *steps_out, uint64_t n, const uint64_t *offsets,
+                                     uint64_t ntrav, int delta_round, void *cuda_stream) {
+  return guard([&] {
+    gfz::inverse_delta_noalloc(steps_in, steps_out, n, offsets, ntrav, delta_round,
+                               static_cast<cudaStream_t>(cuda_stream));
   });
 }
 

@@ -198,6 +198,29 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
                            char *out, uint64_t cap, uint64_t *size, int where);
 gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size);
 
+/* Allocation-free inverse delta.  This entry point has no counterpart in the
+ * reference.  It is for callers that may not allocate device memory: hosts
+ * whose own pool allocator holds nearly all of HBM, plug-ins that such a host
+ * forbids to allocate, and latency-bound loops that cannot afford the device
+ * synchronisation cudaMalloc/cudaFree can cause.  It undoes `delta_round`
+ * rounds of per-traversal delta coding (the inverse-delta step of
+ * gfz_decode) of `n` steps from `steps_in` into `steps_out` on `cuda_stream`
+ * (NULL = legacy default stream), with `offsets` (ntrav + 1 entries, from 0
+ * to n) marking the traversals.  All three buffers are the caller's device
+ * memory on the current device; steps_in == steps_out decodes in place.
+ * The call allocates nothing: its scratch is a fixed 131,328-byte device
+ * array that every GPU loading this library holds until exit, so n is
+ * limited to GFZ_NOALLOC_MAX_STEPS (67,108,864); larger n fails with
+ * GFZ_ERR_INVALID.  The first call on each device does a one-time set-up
+ * (it looks up the array's device address) and should come before any
+ * stream capture.  All calls on a device share the array, which keeps the
+ * last call's contents (each call clears what must start at zero); calls
+ * whose GPU work overlaps race on it and must be serialised by the caller.
+ * Returns after `cuda_stream` has finished the work. */
+#define GFZ_NOALLOC_MAX_STEPS 67108864ull
+gfz_status gfz_inverse_delta_noalloc(const int32_t *steps_in, int32_t *steps_out, uint64_t n, const uint64_t *offsets,
+                                     uint64_t ntrav, int delta_round, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
