@@ -240,10 +240,6 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
   const uint64_t base = (uint64_t)tile * TILE;
   const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
   for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
-  for (uint32_t j = threadIdx.x; j < TILE / 32; j += BLOCK) {
-    scand[j] = 0;
-    sused[j] = 0;
-  }
   const uint32_t ld = len + (base + len < n ? 1u : 0u);
   for (uint32_t j = threadIdx.x; j < ld; j += BLOCK) sv[padi(j)] = s[base + j];
   const uint64_t tlo = mark_heads(off, ntrav, base, len, hb, &s_tlo);
@@ -287,15 +283,19 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
         cur[k] = tab.keys[hs[k]];
       }
     }
+    // lanes of a warp cover one aligned 32-position word per k: build the
+    // candidate / already-used bitmap words with ballots
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
-      if (ck[k] == kEmptyKey) continue;
       const uint32_t j = threadIdx.x + k * BLOCK;
-      const uint32_t fl = tab.flags[hs[k]];
-      if (fl & kFlagRepeated) {
-        sslot[padi(j)] = (uint32_t)hs[k] | (((fwdb >> k) & 1u) << 31);
-        atomicOr(&scand[j >> 5], 1u << (j & 31));
-        if (fl & kFlagUsed) atomicOr(&sused[j >> 5], 1u << (j & 31));
+      const uint32_t fl = ck[k] != kEmptyKey ? tab.flags[hs[k]] : 0u;
+      const bool cand = (fl & kFlagRepeated) != 0;
+      if (cand) sslot[padi(j)] = (uint32_t)hs[k] | (((fwdb >> k) & 1u) << 31);
+      const uint32_t cw = __ballot_sync(0xffffffffu, cand);
+      const uint32_t uw = __ballot_sync(0xffffffffu, cand && (fl & kFlagUsed));
+      if ((threadIdx.x & 31) == 0) {
+        scand[j >> 5] = cw;
+        sused[j >> 5] = uw;
       }
     }
   }
@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
   const uint32_t kept_base = j0 - in_x - c_init + x_init;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
+    uint32_t mark = 0xFFFFFFFFu;  // slot to flag as used (none)
     if ((keptbits >> k) & 1u) {
       const uint32_t j = j0 + k;
       const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
@@ -380,11 +381,15 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
         const uint32_t slot = sl & 0x7FFFFFFFu;
         const int32_t sym = temp_base + (int32_t)slot;
         v = (sl >> 31) ? sym : neg32(sym);
-        if (!bit_at(sused, j)) atomicOr(&tab.flags[slot], kFlagUsed);
+        if (!bit_at(sused, j)) mark = slot;
       }
       so[padi(lo)] = v;
       lidx[padi(j)] = (uint16_t)lo;
     }
+    // one store per distinct slot in the warp; every writer stores the same
+    // value (candidate slots only ever gain the used flag here)
+    const uint32_t peers = __match_any_sync(0xffffffffu, mark);
+    if (mark != 0xFFFFFFFFu && (peers & lanemask_lt()) == 0) tab.flags[mark] = kFlagRepeated | kFlagUsed;
   }
   __syncthreads();
   // positions consumed inside the tile: the carried-in one (in_x) plus the
