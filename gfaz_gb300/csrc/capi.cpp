@@ -211,6 +211,10 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     require(name, "name is NULL");
     gfz::Context &c = ctx_of(ctx);
     if (std::string(name) == "warp_dedup") c.warp_dedup = value != 0;
+    else if (std::string(name) == "first_table_cap") {
+      require(value >= 0 && (value & (value - 1)) == 0, "first_table_cap must be 0 or a power of two");
+      c.first_table_cap = (uint64_t)value;
+    }
     else throw std::invalid_argument(std::string("unknown option: ") + name);
   });
 }

@@ -21,133 +21,259 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ uint32_t warp_max_u32(uint32_t v) {
-  return __reduce_max_sync(0xffffffffu, v);
+// Max-reduces v over the block into *dst with one global atomic per block
+// (one per warp would serialise on the single address).  All threads call it.
+template <int BLOCK>
+__device__ __forceinline__ void block_max_to(uint32_t v, uint32_t *dst) {
+  __shared__ uint32_t s_max;
+  if (threadIdx.x == 0) s_max = 0;
+  __syncthreads();
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(&s_max, v);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_max) atomicMax(dst, s_max);
 }
 
 // ---------------------------------------------------------------------------
 // Delta encode + max |x|
 // ---------------------------------------------------------------------------
+// One tile of BLOCK * ITEMS steps per block.  The tile and the step before it
+// are staged in shared memory; each thread then turns 4 consecutive steps
+// into deltas and writes them as one 16-byte vector.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_delta_encode(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                                         uint64_t n, const uint64_t *__restrict__ off,
                                                         uint64_t ntrav, uint32_t *max_abs) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ int32_t sv[TILE + 1];
+  __shared__ __align__(16) int32_t sv[TILE + 4];  // sv[4 + j] = in[base + j], sv[3] = in[base - 1]
   __shared__ uint32_t hb[TILE / 32 + 2];
   __shared__ uint64_t s_tlo;
   const uint64_t base = (uint64_t)blockIdx.x * TILE;
   const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
   for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
-  if (threadIdx.x == 0) sv[0] = base ? in[base - 1] : 0;
-  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) sv[1 + j] = in[base + j];
+  if (threadIdx.x == 0) sv[3] = base ? in[base - 1] : 0;
+  stage_in<BLOCK, TILE>(in + base, len, sv + 4);
   mark_heads(off, ntrav, base, len, hb, &s_tlo);
   __syncthreads();
   uint32_t mx = 0;
-  for (uint32_t j = threadIdx.x; j < len; j += BLOCK) {
-    int32_t v = sv[1 + j];
-    if (!bit_at(hb, j)) v = (int32_t)((uint32_t)v - (uint32_t)sv[j]);
-    out[base + j] = v;
-    mx = max(mx, abs32(v));
+  const bool vec = len == TILE && (reinterpret_cast<uintptr_t>(out + base) & 15u) == 0;
+  for (uint32_t g = threadIdx.x; 4 * g < len; g += BLOCK) {
+    const uint32_t j = 4 * g;
+    const int4 c = *reinterpret_cast<const int4 *>(&sv[4 + j]);
+    const uint32_t h = (hb[j >> 5] >> (j & 31)) & 0xFu;  // traversal starts among the 4
+    int4 d;
+    d.x = (h & 1u) ? c.x : (int32_t)((uint32_t)c.x - (uint32_t)sv[3 + j]);
+    d.y = (h & 2u) ? c.y : (int32_t)((uint32_t)c.y - (uint32_t)c.x);
+    d.z = (h & 4u) ? c.z : (int32_t)((uint32_t)c.z - (uint32_t)c.y);
+    d.w = (h & 8u) ? c.w : (int32_t)((uint32_t)c.w - (uint32_t)c.z);
+    if (vec) {
+      reinterpret_cast<int4 *>(out + base)[g] = d;
+      mx = max(mx, max(max(abs32(d.x), abs32(d.y)), max(abs32(d.z), abs32(d.w))));
+    } else {
+      const int32_t dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (j + e < len) {
+          out[base + j + e] = dv[e];
+          mx = max(mx, abs32(dv[e]));
+        }
+    }
   }
-  mx = warp_max_u32(mx);
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_abs, mx);
+  block_max_to<BLOCK>(mx, max_abs);
 }
 
-__global__ void k_max_abs(const int32_t *__restrict__ in, uint64_t n, uint32_t *max_abs) {
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_max_abs(const int32_t *__restrict__ in, uint64_t n, uint32_t *max_abs) {
   uint32_t mx = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
     mx = max(mx, abs32(in[i]));
-  mx = warp_max_u32(mx);
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_abs, mx);
+  block_max_to<BLOCK>(mx, max_abs);
 }
 
 // ---------------------------------------------------------------------------
-// Open-addressed pair table
+// Open-addressed pair table (linear probing over 16-byte slots)
 // ---------------------------------------------------------------------------
 constexpr uint32_t kMaxProbe = 4096;
+
+__device__ __forceinline__ void load_slot(const PairSlot *p, unsigned long long &key, uint32_t &flags) {
+  const ulonglong2 w = *reinterpret_cast<const ulonglong2 *>(p);
+  key = w.x;
+  flags = (uint32_t)w.y;
+}
+
+__global__ void k_table_clear(PairTable tab, uint32_t val_init) {
+  const uint4 empty = make_uint4((uint32_t)kEmptyKey, (uint32_t)(kEmptyKey >> 32), 0u, val_init);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tab.cap; i += (uint64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<uint4 *>(tab.slots)[i] = empty;
+}
 
 struct InsertCounts {
   uint32_t fresh = 0, repeated = 0;
 };
 
-__device__ __forceinline__ void mark_repeated(uint32_t *flags, uint64_t h, InsertCounts &c) {
-  if (!(flags[h] & kFlagRepeated)) {
-    uint32_t old = atomicOr(&flags[h], kFlagRepeated);
-    if (!(old & kFlagRepeated)) c.repeated++;
-  }
+// Sets the repeated flag; counts the key if this call set it.
+__device__ __forceinline__ void mark_repeated(PairSlot *slot, InsertCounts &c) {
+  const uint32_t old = atomicOr(&slot->flags, kFlagRepeated);
+  if (!(old & kFlagRepeated)) c.repeated++;
 }
 
-// Inserts a canonical key; `known_repeat` marks it repeated unconditionally
-// (another occurrence was seen in the same warp).  Returns false when the
-// probe bound is exceeded.
-__device__ __forceinline__ bool table_insert(const PairTable &tab, unsigned long long key, bool known_repeat,
-                                             InsertCounts &c) {
-  const uint64_t mask = tab.cap - 1;
-  uint64_t h = hash64(key) & mask;
+// Inserts one occurrence of canonical `key` starting at slot h, whose
+// contents (cur, fl) were already loaded.  `more` = the caller folded a
+// second occurrence into this call.  Returns false when the probe bound is
+// exceeded.
+__device__ __forceinline__ bool insert_at(const PairTable &tab, unsigned long long key, bool more, uint32_t h,
+                                          unsigned long long cur, uint32_t fl, InsertCounts &c) {
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
   for (uint32_t p = 0; p < kMaxProbe; ++p) {
-    unsigned long long cur = tab.keys[h];
     if (cur == kEmptyKey) {
-      unsigned long long old = atomicCAS(&tab.keys[h], kEmptyKey, key);
+      const unsigned long long old = atomicCAS(&tab.slots[h].key, kEmptyKey, key);
       if (old == kEmptyKey) {
         c.fresh++;
-        if (known_repeat) mark_repeated(tab.flags, h, c);
+        if (more) mark_repeated(&tab.slots[h], c);
         return true;
       }
       cur = old;
+      fl = 0;
     }
     if (cur == key) {
-      mark_repeated(tab.flags, h, c);
+      // a stale flag word can only miss bits, so a set bit needs no atomic
+      if (!(fl & kFlagRepeated)) mark_repeated(&tab.slots[h], c);
       return true;
     }
     h = (h + 1) & mask;
+    load_slot(&tab.slots[h], cur, fl);
   }
   return false;
 }
 
-template <int BLOCK, int ITEMS, bool DEDUP>
-__global__ void __launch_bounds__(BLOCK) k_count_pairs(const int32_t *__restrict__ s, uint64_t n,
-                                                       const uint64_t *__restrict__ off, uint64_t ntrav,
-                                                       PairTable tab, DevStatus *status) {
-  constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ int32_t sv[TILE + 1];
-  __shared__ uint32_t hb[TILE / 32 + 2];
-  __shared__ uint64_t s_tlo;
-  __shared__ uint32_t s_fresh, s_rep;
-  const uint64_t base = (uint64_t)blockIdx.x * TILE;
-  const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
-  for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
-  if (threadIdx.x == 0) { s_fresh = 0; s_rep = 0; }
-  const uint32_t ld = len + (base + len < n ? 1u : 0u);
-  for (uint32_t j = threadIdx.x; j < ld; j += BLOCK) sv[j] = s[base + j];
-  mark_heads(off, ntrav, base, len, hb, &s_tlo);
-  __syncthreads();
-  InsertCounts c;
-  bool abort = (*(volatile uint32_t *)&status->err & kErrTableFull) != 0;
-#pragma unroll 4
+// The ITEMS + 1 steps a thread looks at: positions j0 .. j0 + ITEMS of the
+// staged tile (two 16-byte shared loads plus one element).
+template <int ITEMS>
+__device__ __forceinline__ void thread_steps(const int32_t *sv, uint32_t j0, int32_t (&v)[ITEMS + 1]) {
+  static_assert(ITEMS == 8, "eight consecutive steps per thread");
+  const int4 a = *reinterpret_cast<const int4 *>(&sv[j0]);
+  const int4 b = *reinterpret_cast<const int4 *>(&sv[j0 + 4]);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  v[8] = sv[j0 + 8];
+}
+
+// Counts one staged tile: thread t handles the pairs starting at positions
+// j0 = t * ITEMS .. j0 + ITEMS - 1.  A run of equal keys inside a thread is
+// inserted once (flagged repeated when longer than one); with DEDUP the
+// lanes of a warp also fold equal keys of the same item index.
+template <int ITEMS, bool DEDUP>
+__device__ __forceinline__ void count_tile(const int32_t *sv, const uint32_t *hb, uint32_t len, const PairTable &tab,
+                                           DevStatus *status, InsertCounts &c) {
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  int32_t v[ITEMS + 1];
+  thread_steps<ITEMS>(sv, j0, v);
+  const uint32_t hd = bits_from(hb, j0);  // bit k: position j0 + k starts a traversal
+  unsigned long long key[ITEMS];
+  uint32_t validb = 0, sameb = 0;
+#pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
-    const uint32_t j = threadIdx.x + k * BLOCK;
-    const bool valid = j < len && !bit_at(hb, j + 1);
-    unsigned long long key = valid ? canon2(pack2(sv[j], sv[j + 1])) : kEmptyKey;
-    bool leader = valid, rep = false;
-    if (DEDUP) {
-      const uint32_t m = __match_any_sync(0xffffffffu, key);
-      leader = valid && (m & lanemask_lt()) == 0;
-      rep = __popc(m) > 1;
+    const bool valid = j0 + k < len && !((hd >> (k + 1)) & 1u);
+    key[k] = canon2(pack2(v[k], v[k + 1]));
+    validb |= (uint32_t)valid << k;
+    if (k > 0) sameb |= (uint32_t)(key[k] == key[k - 1]) << k;
+  }
+  // drop a position whose key equals its valid predecessor's; the first of
+  // the run then carries the extra occurrence
+  const uint32_t dropped = validb & (validb << 1) & sameb;
+  uint32_t insb = validb & ~dropped;
+  uint32_t moreb = insb & (dropped >> 1);
+  if (DEDUP) {
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const bool ins = (insb >> k) & 1u;
+      const uint32_t m = __match_any_sync(0xffffffffu, ins ? key[k] : kEmptyKey);
+      if (ins && (m & lanemask_lt()) != 0) insb &= ~(1u << k);  // a lower lane inserts it
+      else if (ins && __popc(m) > 1) moreb |= 1u << k;
     }
-    if (leader && !abort) {
-      if (!table_insert(tab, key, rep, c)) {
+  }
+  if ((*(volatile uint32_t *)&status->err & kErrTableFull) != 0) insb = 0;
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
+  uint32_t h[ITEMS];
+  unsigned long long cur[ITEMS];
+  uint32_t fl[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    h[k] = hash_pair(key[k]) & mask;
+    cur[k] = kEmptyKey;
+    fl[k] = 0;
+    if ((insb >> k) & 1u) load_slot(&tab.slots[h[k]], cur[k], fl[k]);
+  }
+  bool abort = false;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    if (((insb >> k) & 1u) && !abort) {
+      if (!insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], c)) {
         atomicOr(&status->err, kErrTableFull);
         abort = true;
       }
     }
   }
-  if (c.fresh) atomicAdd(&s_fresh, c.fresh);
-  if (c.repeated) atomicAdd(&s_rep, c.repeated);
+}
+
+// Persistent: block b counts tiles b, b + gridDim.x, ..., the next tile
+// streaming into the other pipeline stage while this one is counted.
+template <int BLOCK, int ITEMS, bool DEDUP>
+__global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restrict__ s, uint64_t n,
+                                                          const uint32_t *__restrict__ heads, uint64_t head_words,
+                                                          PairTable tab, DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  __shared__ __align__(128) TilePipe<TILE> P;
+  __shared__ uint32_t s_fresh, s_rep;
+  const uint64_t ntiles = (n + TILE - 1) / TILE;
+  uint64_t tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&P.bar[0], 1);
+    mbar_init(&P.bar[1], 1);
+    mbar_init_fence();
+    s_fresh = 0;
+    s_rep = 0;
+  }
+  __syncthreads();
+  uint32_t phases = 0;
+  bool bulk_cur = pipe_issue<BLOCK, TILE>(P, 0, tile, s, n, heads, head_words);
+  InsertCounts c;
+  for (int b = 0;; b ^= 1) {
+    const uint64_t next = tile + gridDim.x;
+    const bool has_next = next < ntiles;
+    const bool bulk_next = has_next && pipe_issue<BLOCK, TILE>(P, b ^ 1, next, s, n, heads, head_words);
+    if (!pipe_wait<TILE>(P, b, bulk_cur, phases)) {
+      // a bulk copy did not land: report, let the other stage's copy finish
+      if (threadIdx.x == 0) atomicOr(&status->err, kErrTimeout);
+      if (bulk_next) mbar_wait(&P.bar[b ^ 1], (phases >> (b ^ 1)) & 1u);
+      return;
+    }
+    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - tile * TILE);
+    count_tile<ITEMS, DEDUP>(P.sv[b], P.hb[b], len, tab, status, c);
+    pipe_release();
+    if (!has_next) break;
+    tile = next;
+    bulk_cur = bulk_next;
+  }
+  const uint32_t f = __reduce_add_sync(0xffffffffu, c.fresh);
+  const uint32_t r = __reduce_add_sync(0xffffffffu, c.repeated);
+  if ((threadIdx.x & 31) == 0) {
+    if (f) atomicAdd(&s_fresh, f);
+    if (r) atomicAdd(&s_rep, r);
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     if (s_fresh) atomicAdd(&status->u64[0], (unsigned long long)s_fresh);
     if (s_rep) atomicAdd(&status->u64[1], (unsigned long long)s_rep);
+  }
+}
+
+// Traversal-head bitmap: bit off[t] for every t <= ntrav (bits cleared).
+__global__ void k_head_bits(const uint64_t *__restrict__ off, uint64_t ntrav, uint32_t *bits) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntrav; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = off[t];
+    atomicOr(&bits[q >> 5], 1u << (q & 31));
   }
 }
 
@@ -214,199 +340,225 @@ __device__ __forceinline__ ParAgg par_shfl_up(const ParAgg &a, int delta) {
   return r;
 }
 
+// First traversal starting at or after each tile: tile_trav[k] = the first
+// t with off[t] >= k * tile (off sorted, off[ntrav] = n).
+__global__ void k_tile_trav(const uint64_t *__restrict__ off, uint64_t ntrav, uint64_t ntiles, uint32_t tile,
+                            uint64_t *tile_trav) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < ntiles; k += (uint64_t)gridDim.x * blockDim.x)
+    tile_trav[k] = lower_bound_u64(off, ntrav, k * (uint64_t)tile);
+}
+
+// Greedy replacement, one tile per block.  The tile index is claimed when
+// the block starts (so every tile a look-back waits on belongs to a block
+// that is already running and publishes its aggregate as soon as its
+// lookups are done; claiming further ahead would make later tiles wait on
+// tiles whose blocks are still busy elsewhere), then the tile and its head
+// bits arrive by bulk copy.
+//
+// Thread t owns positions j0 = t * ITEMS .. j0 + ITEMS - 1.  It looks up the
+// pairs starting there (one 16-byte slot load each, all issued together),
+// keeps the candidate bits, slots and steps in registers, takes part in the
+// block scan and the decoupled look-back of the run-parity recurrence, then
+// scatters its kept symbols into a shared staging buffer aligned like the
+// output, which the block writes out as 16-byte vectors.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, uint64_t n,
-                                                 const uint64_t *__restrict__ off, uint64_t ntrav, PairTable tab,
+                                                 const uint32_t *__restrict__ heads, uint64_t head_words,
+                                                 const uint64_t *__restrict__ off, uint64_t ntrav,
+                                                 const uint64_t *__restrict__ tile_trav, PairTable tab,
                                                  int32_t temp_base, int32_t *__restrict__ out,
                                                  uint64_t *__restrict__ new_off, unsigned long long *desc,
                                                  uint32_t *tile_counter, DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   constexpr int NW = BLOCK / 32;
   static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
-  static_assert(32 % ITEMS == 0, "a thread's candidate bits must sit in one bitmap word");
-  __shared__ int32_t sv[padded_size(TILE + 1)];
-  __shared__ int32_t so[padded_size(TILE)];
-  __shared__ uint32_t sslot[padded_size(TILE)];  // table slot | orientation bit (31)
-  __shared__ uint16_t lidx[padded_size(TILE)];
-  __shared__ uint32_t hb[TILE / 32 + 2];
-  __shared__ uint32_t scand[TILE / 32];  // candidate positions
-  __shared__ uint32_t sused[TILE / 32];  // slot already flagged used
-  __shared__ uint64_t s_tlo;
+  static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
+  __shared__ __align__(128) TilePipe<TILE> P;  // stage 0 only
+  __shared__ __align__(16) int32_t so[TILE + 4];
+  __shared__ __align__(16) uint16_t lidx[TILE];  // output index (in the tile) of each kept position
   __shared__ ParAgg s_warp[NW];
   __shared__ uint32_t s_in_x;
   __shared__ unsigned long long s_in_c;
+  __shared__ uint32_t s_tile;
+  __shared__ uint64_t s_tlo;
 
-  const uint32_t tile = claim_tile(tile_counter);
-  const uint64_t base = (uint64_t)tile * TILE;
-  const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
-  for (uint32_t j = threadIdx.x; j < TILE / 32 + 2; j += BLOCK) hb[j] = 0;
-  const uint32_t ld = len + (base + len < n ? 1u : 0u);
-  for (uint32_t j = threadIdx.x; j < ld; j += BLOCK) sv[padi(j)] = s[base + j];
-  const uint64_t tlo = mark_heads(off, ntrav, base, len, hb, &s_tlo);
-  __syncthreads();
-
-  // Phase A: candidate lookup for positions j = tid + k * BLOCK; the ITEMS
-  // first probes are issued back to back, then collisions are resolved.
-  {
-    const uint64_t mask = tab.cap - 1;
-    unsigned long long ck[ITEMS];
-    uint64_t hs[ITEMS];
-    unsigned long long cur[ITEMS];
-    uint32_t fwdb = 0;
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const uint32_t j = threadIdx.x + k * BLOCK;
-      ck[k] = kEmptyKey;
-      hs[k] = 0;
-      cur[k] = kEmptyKey;
-      if (j < len && !bit_at(hb, j + 1)) {
-        const unsigned long long key = pack2(sv[padi(j)], sv[padi(j + 1)]);
-        const unsigned long long r = rev2(key);
-        const bool fwd = key_le(key, r);
-        ck[k] = fwd ? key : r;
-        fwdb |= (uint32_t)fwd << k;
-        hs[k] = hash64(ck[k]) & mask;
-        cur[k] = tab.keys[hs[k]];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      if (ck[k] == kEmptyKey) continue;
-      uint32_t p = 0;
-      while (cur[k] != ck[k]) {
-        if (cur[k] == kEmptyKey || ++p >= kMaxProbe) {
-          atomicOr(&status->err, kErrLookupMiss);
-          ck[k] = kEmptyKey;
-          break;
-        }
-        hs[k] = (hs[k] + 1) & mask;
-        cur[k] = tab.keys[hs[k]];
-      }
-    }
-    // lanes of a warp cover one aligned 32-position word per k: build the
-    // candidate / already-used bitmap words with ballots
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const uint32_t j = threadIdx.x + k * BLOCK;
-      const uint32_t fl = ck[k] != kEmptyKey ? tab.flags[hs[k]] : 0u;
-      const bool cand = (fl & kFlagRepeated) != 0;
-      if (cand) sslot[padi(j)] = (uint32_t)hs[k] | (((fwdb >> k) & 1u) << 31);
-      const uint32_t cw = __ballot_sync(0xffffffffu, cand);
-      const uint32_t uw = __ballot_sync(0xffffffffu, cand && (fl & kFlagUsed));
-      if ((threadIdx.x & 31) == 0) {
-        scand[j >> 5] = cw;
-        sused[j >> 5] = uw;
-      }
-    }
+  if (threadIdx.x == 0) {
+    mbar_init(&P.bar[0], 1);
+    mbar_init_fence();
+    s_tile = atomicAdd(tile_counter, 1u);
   }
   __syncthreads();
-
-  // Phase B: the run-parity recurrence over my ITEMS consecutive positions
-  const uint32_t j0 = threadIdx.x * ITEMS;
-  const uint32_t cbits = j0 < TILE ? (scand[j0 >> 5] >> (j0 & 31)) & ((1u << ITEMS) - 1u) : 0u;
-
-  // thread aggregate
-  ParAgg a;
-  {
-    uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const uint32_t c = (cbits >> k) & 1u;
-      x0 = c & (x0 ^ 1u);
-      x1 = c & (x1 ^ 1u);
-      c0 += x0;
-      c1 += x1;
-    }
-    a = ParAgg{x0 | (x1 << 1), c0, c1};
-  }
-  // block exclusive scan
+  const uint64_t tile = s_tile;
+  uint32_t phases = 0;
+  const bool bulk = pipe_issue<BLOCK, TILE>(P, 0, tile, s, n, heads, head_words);
+  if (threadIdx.x == 0) s_tlo = tile_trav[tile];
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  ParAgg inc = a;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    ParAgg o = par_shfl_up(inc, d);
-    if (lane >= d) inc = par_compose(o, inc);
-  }
-  ParAgg excl = par_shfl_up(inc, 1);
-  if (lane == 0) excl = par_identity();
-  if (lane == 31) s_warp[warp] = inc;
-  __syncthreads();
-  ParAgg wpre = par_identity(), total = par_identity();
-  for (int w = 0; w < NW; ++w) {
-    if (w == warp) wpre = total;
-    total = par_compose(total, s_warp[w]);
-  }
-  excl = par_compose(wpre, excl);
-
-  if (warp == 0) {
-    const ParState in = warp_lookback<ParOp>(desc, tile, total, &status->err);
-    if (lane == 0) {
-      s_in_x = in.x;
-      s_in_c = in.c;
-    }
-  }
-  __syncthreads();
-  const uint32_t in_x = s_in_x;
-  const unsigned long long in_c = s_in_c;
-  // Replay the recurrence over my positions from the carried-in state: which
-  // positions are kept (not consumed) and which kept ones are replaced.
-  const uint32_t x_init = par_x(excl, in_x);
-  const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
-  uint32_t keptbits = 0, xbits = 0;
+  const uint32_t j0 = threadIdx.x * ITEMS;
   {
-    uint32_t x = x_init;
+    const int b = 0;
+    if (!pipe_wait<TILE>(P, b, bulk, phases)) {
+      if (threadIdx.x == 0) atomicOr(&status->err, kErrTimeout);
+      return;
+    }
+    const int32_t *sv = P.sv[b];
+    const uint32_t *hb = P.hb[b];
+    const uint64_t base = tile * TILE;
+    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
+
+    // ---- lookups: candidate (repeated) and already-used bits per position
+    int32_t v[ITEMS + 1];
+    thread_steps<ITEMS>(sv, j0, v);
+    const uint32_t hd = bits_from(hb, j0);
+    unsigned long long key[ITEMS];
+    uint32_t slot[ITEMS];
+    uint32_t fwdb = 0, validb = 0;
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
-      if (j0 + k < len) {
-        const uint32_t prev = x;
-        x = ((cbits >> k) & 1u) & (prev ^ 1u);
-        keptbits |= (prev ^ 1u) << k;
-        xbits |= x << k;
-      }
+      const bool valid = j0 + k < len && !((hd >> (k + 1)) & 1u);
+      const unsigned long long f = pack2(v[k], v[k + 1]);
+      const unsigned long long r = pack2(neg32(v[k + 1]), neg32(v[k]));
+      const bool fw = key_le(f, r);
+      key[k] = fw ? f : r;
+      fwdb |= (uint32_t)fw << k;
+      validb |= (uint32_t)valid << k;
+      slot[k] = hash_pair(key[k]) & mask;
     }
-  }
-  // kept positions of the tile before j0: j0 minus the consumed ones, i.e.
-  // the carried-in position plus the partner of every replaced position
-  // before j0 except a replaced j0 - 1, whose partner is j0 itself
-  const uint32_t kept_base = j0 - in_x - c_init + x_init;
+    uint32_t cbits = 0, ubits = 0;
+    {
+      unsigned long long cur[ITEMS];
+      uint32_t fl[ITEMS];
 #pragma unroll
-  for (int k = 0; k < ITEMS; ++k) {
-    uint32_t mark = 0xFFFFFFFFu;  // slot to flag as used (none)
-    if ((keptbits >> k) & 1u) {
-      const uint32_t j = j0 + k;
-      const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
-      int32_t v = sv[padi(j)];
-      if ((xbits >> k) & 1u) {
-        const uint32_t sl = sslot[padi(j)];
-        const uint32_t slot = sl & 0x7FFFFFFFu;
-        const int32_t sym = temp_base + (int32_t)slot;
-        v = (sl >> 31) ? sym : neg32(sym);
-        if (!bit_at(sused, j)) mark = slot;
+      for (int k = 0; k < ITEMS; ++k) {
+        cur[k] = key[k];
+        fl[k] = 0;
+        if ((validb >> k) & 1u) load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
       }
-      so[padi(lo)] = v;
-      lidx[padi(j)] = (uint16_t)lo;
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        uint32_t p = 0;
+        while (cur[k] != key[k]) {
+          if (cur[k] == kEmptyKey || ++p >= kMaxProbe) {
+            atomicOr(&status->err, kErrLookupMiss);
+            fl[k] = 0;
+            break;
+          }
+          slot[k] = (slot[k] + 1) & mask;
+          load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
+        }
+        cbits |= (uint32_t)((fl[k] & kFlagRepeated) != 0) << k;
+        ubits |= (uint32_t)((fl[k] & kFlagUsed) != 0) << k;
+      }
     }
-    // one store per distinct slot in the warp; every writer stores the same
-    // value (candidate slots only ever gain the used flag here)
-    const uint32_t peers = __match_any_sync(0xffffffffu, mark);
-    if (mark != 0xFFFFFFFFu && (peers & lanemask_lt()) == 0) tab.flags[mark] = kFlagRepeated | kFlagUsed;
+
+    // ---- run-parity recurrence: thread aggregate, block scan, look-back
+    ParAgg a;
+    {
+      uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t c = (cbits >> k) & 1u;
+        x0 = c & (x0 ^ 1u);
+        x1 = c & (x1 ^ 1u);
+        c0 += x0;
+        c1 += x1;
+      }
+      a = ParAgg{x0 | (x1 << 1), c0, c1};
+    }
+    ParAgg inc = a;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      ParAgg o = par_shfl_up(inc, d);
+      if (lane >= d) inc = par_compose(o, inc);
+    }
+    ParAgg excl = par_shfl_up(inc, 1);
+    if (lane == 0) excl = par_identity();
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    ParAgg wpre = par_identity(), total = par_identity();
+    for (int w = 0; w < NW; ++w) {
+      if (w == warp) wpre = total;
+      total = par_compose(total, s_warp[w]);
+    }
+    excl = par_compose(wpre, excl);
+    if (warp == 0) {
+      const ParState in = warp_lookback<ParOp>(desc, tile, total, &status->err);
+      if (lane == 0) {
+        s_in_x = in.x;
+        s_in_c = in.c;
+      }
+    }
+    __syncthreads();
+    const uint32_t in_x = s_in_x;
+    const unsigned long long in_c = s_in_c;
+    // replay from the carried-in state: kept (not consumed) and replaced bits
+    const uint32_t x_init = par_x(excl, in_x);
+    const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
+    uint32_t keptbits = 0, xbits = 0;
+    {
+      uint32_t x = x_init;
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        if (j0 + k < len) {
+          const uint32_t prev = x;
+          x = ((cbits >> k) & 1u) & (prev ^ 1u);
+          keptbits |= (prev ^ 1u) << k;
+          xbits |= x << k;
+        }
+      }
+    }
+    // kept positions of the tile before j0: j0 minus the consumed ones (the
+    // carried-in position and the partner of every replaced position before
+    // j0, except a replaced j0 - 1 whose partner is j0 itself)
+    const uint32_t kept_base = j0 - in_x - c_init + x_init;
+    const uint64_t out_base = base - in_c + in_x;
+    const uint32_t shift = (uint32_t)(((reinterpret_cast<uintptr_t>(out) >> 2) + out_base) & 3u);
+
+    // ---- scatter kept symbols; record output indices
+    uint32_t lpk[ITEMS / 2];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
+      if ((keptbits >> k) & 1u) {
+        int32_t val = v[k];
+        if ((xbits >> k) & 1u) {
+          const int32_t sym = temp_base + (int32_t)slot[k];
+          val = ((fwdb >> k) & 1u) ? sym : neg32(sym);
+        }
+        so[shift + lo] = val;
+      }
+      if (k & 1) lpk[k >> 1] |= lo << 16;
+      else lpk[k >> 1] = lo & 0xFFFFu;
+    }
+    *reinterpret_cast<uint4 *>(&lidx[j0]) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
+    // rules chosen here whose slot was not yet flagged used: one flag update
+    // per distinct slot per warp (frequent pairs hit one slot from every lane)
+    const uint32_t need = xbits & ~ubits;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const bool nk = (need >> k) & 1u;
+      if (__any_sync(0xffffffffu, nk)) {
+        const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
+        if (nk && (peers & lanemask_lt()) == 0) atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+      }
+    }
+    __syncthreads();
+
+    // ---- write out: positions consumed inside the tile are the carried-in
+    // one (in_x) plus the partner of every replaced position except a
+    // replaced last position, whose partner opens the next tile (x_out)
+    const uint32_t tile_rep = par_c(total, in_x);
+    const uint32_t kept = len - in_x - tile_rep + par_x(total, in_x);
+    stage_out_phased<BLOCK>(out + out_base, so, shift, kept);
+    const bool last_tile = base + len == n;
+    for (uint64_t t = s_tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
+      const uint64_t q = off[t];
+      if (q < base + len) new_off[t] = out_base + lidx[(uint32_t)(q - base)];
+      else if (last_tile && q == n) new_off[t] = out_base + kept;
+      else break;
+    }
+    if (last_tile && threadIdx.x == 0) status->u64[2] = out_base + kept;
   }
-  __syncthreads();
-  // positions consumed inside the tile: the carried-in one (in_x) plus the
-  // partner of every replaced position except a replaced last position,
-  // whose partner opens the next tile (x_out)
-  const uint32_t tile_rep = par_c(total, in_x);
-  const uint32_t kept = len - in_x - tile_rep + par_x(total, in_x);
-  const uint64_t out_base = base - in_c + in_x;
-  for (uint32_t j = threadIdx.x; j < kept; j += BLOCK) out[out_base + j] = so[padi(j)];
-  const bool last_tile = base + len == n;
-  for (uint64_t t = tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
-    const uint64_t q = off[t];
-    if (q < base + len) new_off[t] = out_base + lidx[padi((uint32_t)(q - base))];
-    else if (last_tile && q == n) new_off[t] = out_base + kept;
-    else break;
-  }
-  if (last_tile && threadIdx.x == 0) status->u64[2] = out_base + kept;
 }
 
 // ---------------------------------------------------------------------------
@@ -414,11 +566,14 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
 // ---------------------------------------------------------------------------
 constexpr unsigned long long kSignFlip = 0x8000000000000000ULL;
 
-__global__ void k_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out,
+__global__ void k_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
                                DevStatus *status) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tab.cap;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const bool used = (tab.flags[i] & kFlagUsed) != 0;
+    unsigned long long key;
+    uint32_t fl;
+    load_slot(&tab.slots[i], key, fl);
+    const bool used = (fl & kFlagUsed) != 0;
     const uint32_t act = __activemask();
     const uint32_t m = __ballot_sync(act, used);
     if (!m) continue;
@@ -428,8 +583,12 @@ __global__ void k_collect_used(PairTable tab, unsigned long long *keys_out, uint
     basepos = __shfl_sync(act, basepos, leader);
     if (used) {
       const uint64_t p = basepos + __popc(m & lanemask_lt());
-      keys_out[p] = tab.keys[i] ^ kSignFlip;
-      slots_out[p] = (uint32_t)i;
+      if (p < cap_out) {
+        keys_out[p] = key ^ kSignFlip;
+        slots_out[p] = (uint32_t)i;
+      } else {
+        atomicOr(&status->err, kErrLength);
+      }
     }
   }
 }
@@ -537,20 +696,37 @@ __global__ void __launch_bounds__(kBlock) k_radix_scatter(const unsigned long lo
 __global__ void k_assign_ids(const unsigned long long *sorted_keys, const uint32_t *sorted_slots, uint64_t u,
                              uint32_t next_id, PairTable tab, long long *rulebook) {
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < u; r += (uint64_t)gridDim.x * blockDim.x) {
-    tab.vals[sorted_slots[r]] = next_id + (uint32_t)r;
+    tab.slots[sorted_slots[r]].val = next_id + (uint32_t)r;
     rulebook[r] = (long long)(sorted_keys[r] ^ kSignFlip);
   }
 }
 
-__global__ void k_remap(int32_t *s, uint64_t n, int32_t temp_base, const uint32_t *__restrict__ vals) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const int32_t v = s[i];
-    const uint32_t a = abs32(v);
-    if (a >= (uint32_t)temp_base) {
-      const int32_t f = (int32_t)vals[a - (uint32_t)temp_base];
-      s[i] = v < 0 ? neg32(f) : f;
+__device__ __forceinline__ int32_t remap_one(int32_t v, int32_t temp_base, const PairSlot *__restrict__ slots) {
+  const uint32_t a = abs32(v);
+  if (a < (uint32_t)temp_base) return v;
+  const int32_t f = (int32_t)slots[a - (uint32_t)temp_base].val;
+  return v < 0 ? neg32(f) : f;
+}
+
+// 16-byte vectors when s is 16-byte aligned (VEC), single steps otherwise.
+template <bool VEC>
+__global__ void k_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlot *__restrict__ slots) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  uint64_t done = 0;
+  if (VEC) {
+    int4 *s4 = reinterpret_cast<int4 *>(s);
+    for (uint64_t g = t0; g < n / 4; g += stride) {
+      int4 x = s4[g];
+      x.x = remap_one(x.x, temp_base, slots);
+      x.y = remap_one(x.y, temp_base, slots);
+      x.z = remap_one(x.z, temp_base, slots);
+      x.w = remap_one(x.w, temp_base, slots);
+      s4[g] = x;
     }
+    done = n & ~3ull;
   }
+  for (uint64_t i = done + t0; i < n; i += stride) s[i] = remap_one(s[i], temp_base, slots);
 }
 
 // ---------------------------------------------------------------------------
@@ -558,7 +734,7 @@ __global__ void k_remap(int32_t *s, uint64_t n, int32_t temp_base, const uint32_
 // ---------------------------------------------------------------------------
 __global__ void k_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi,
                                    uint32_t start, PairTable tab, DevStatus *status) {
-  const uint64_t mask = tab.cap - 1;
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
   for (uint64_t i = lo + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < hi;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const unsigned long long key = pack2(first[i], second[i]);
@@ -566,16 +742,16 @@ __global__ void k_build_rule_table(const int32_t *first, const int32_t *second, 
       atomicOr(&status->err, kErrBadSymbol);
       continue;
     }
-    uint64_t h = hash64(key) & mask;
+    uint32_t h = hash_pair(key) & mask;
     for (uint32_t p = 0;; ++p) {
       if (p >= kMaxProbe) {
         atomicOr(&status->err, kErrTableFull);
         break;
       }
-      unsigned long long old = atomicCAS(&tab.keys[h], kEmptyKey, key);
+      const unsigned long long old = atomicCAS(&tab.slots[h].key, kEmptyKey, key);
       if (old == kEmptyKey || old == key) {
         // the first stored occurrence keeps its id (emplace semantics)
-        atomicMin(&tab.vals[h], start + (uint32_t)(i - lo));
+        atomicMin(&tab.slots[h].val, start + (uint32_t)(i - lo));
         break;
       }
       h = (h + 1) & mask;
@@ -585,15 +761,15 @@ __global__ void k_build_rule_table(const int32_t *first, const int32_t *second, 
 
 __device__ __forceinline__ bool table_find(const PairTable &tab, unsigned long long key, uint32_t &id) {
   if (key == kEmptyKey) return false;
-  const uint64_t mask = tab.cap - 1;
-  uint64_t h = hash64(key) & mask;
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
+  uint32_t h = hash_pair(key) & mask;
   for (uint32_t p = 0; p < kMaxProbe; ++p) {
-    const unsigned long long cur = tab.keys[h];
-    if (cur == key) {
-      id = tab.vals[h];
+    const ulonglong2 w = *reinterpret_cast<const ulonglong2 *>(&tab.slots[h]);
+    if (w.x == key) {
+      id = (uint32_t)(w.y >> 32);
       return true;
     }
-    if (cur == kEmptyKey) return false;
+    if (w.x == kEmptyKey) return false;
     h = (h + 1) & mask;
   }
   return false;
@@ -651,7 +827,7 @@ inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
 // Launchers
 // ---------------------------------------------------------------------------
 constexpr int kDeltaItems = 16;
-constexpr int kCountItems = 16;
+constexpr int kCountItems = 8;
 constexpr int kApplyItems = 8;
 
 void launch_delta_encode(const int32_t *in, int32_t *out, uint64_t n, const uint64_t *off, uint64_t ntrav,
@@ -664,18 +840,40 @@ void launch_delta_encode(const int32_t *in, int32_t *out, uint64_t n, const uint
 
 void launch_max_abs(const int32_t *in, uint64_t n, uint32_t *max_abs, cudaStream_t st) {
   if (!n) return;
-  k_max_abs<<<grid_for(n, kBlock), kBlock, 0, st>>>(in, n, max_abs);
+  k_max_abs<kBlock><<<grid_for(n, kBlock), kBlock, 0, st>>>(in, n, max_abs);
 }
 
-void launch_count_pairs(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav, PairTable tab,
-                        DevStatus *status, bool warp_dedup, cudaStream_t st) {
+// Resident blocks of a persistent kernel: SMs x blocks per SM.
+template <typename K>
+unsigned persistent_grid(K kernel, int block, uint64_t tiles) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+  uint64_t g = (uint64_t)(sms > 0 ? sms : 1) * (uint64_t)(per_sm > 0 ? per_sm : 1);
+  if (g > tiles) g = tiles;
+  return (unsigned)(g ? g : 1);
+}
+
+uint64_t head_words(uint64_t n) { return (n + 1 + 31) / 32 + 8; }
+
+void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaStream_t st) {
+  k_head_bits<<<grid_for(ntrav + 1, kBlock), kBlock, 0, st>>>(off, ntrav, bits);
+}
+
+void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
+                        bool warp_dedup, cudaStream_t st) {
   if (!n) return;
   constexpr uint64_t TILE = kBlock * kCountItems;
-  const unsigned g = (unsigned)((n + TILE - 1) / TILE);
-  if (warp_dedup)
-    k_count_pairs<kBlock, kCountItems, true><<<g, kBlock, 0, st>>>(s, n, off, ntrav, tab, status);
-  else
-    k_count_pairs<kBlock, kCountItems, false><<<g, kBlock, 0, st>>>(s, n, off, ntrav, tab, status);
+  const uint64_t tiles = (n + TILE - 1) / TILE;
+  const uint64_t hw = head_words(n);
+  if (warp_dedup) {
+    auto k = k_count_pairs<kBlock, kCountItems, true>;
+    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status);
+  } else {
+    auto k = k_count_pairs<kBlock, kCountItems, false>;
+    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status);
+  }
 }
 
 uint64_t apply_num_tiles(uint64_t n) {
@@ -683,17 +881,25 @@ uint64_t apply_num_tiles(uint64_t n) {
   return (n + TILE - 1) / TILE;
 }
 
-void launch_apply(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav, PairTable tab,
-                  int32_t temp_base, int32_t *out, uint64_t *new_off, unsigned long long *desc,
-                  uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
-  if (!n) return;
-  k_apply<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
-      s, n, off, ntrav, tab, temp_base, out, new_off, desc, tile_counter, status);
+void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st) {
+  const uint64_t tiles = apply_num_tiles(n);
+  if (!tiles) return;
+  k_tile_trav<<<grid_for(tiles, kBlock), kBlock, 0, st>>>(off, ntrav, tiles, kBlock * kApplyItems, tile_trav);
 }
 
-void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, DevStatus *status,
-                         cudaStream_t st) {
-  k_collect_used<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, keys_out, slots_out, status);
+void launch_apply(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
+                  const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
+                  unsigned long long *desc, uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  const uint64_t tiles = apply_num_tiles(n);
+  k_apply<kBlock, kApplyItems><<<(unsigned)tiles, kBlock, 0, st>>>(s, n, heads, head_words(n), off, ntrav, tile_trav,
+                                                                   tab, temp_base, out, new_off, desc, tile_counter,
+                                                                   status);
+}
+
+void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
+                         DevStatus *status, cudaStream_t st) {
+  k_collect_used<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, keys_out, slots_out, cap_out, status);
 }
 
 void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status, cudaStream_t st) {
@@ -728,9 +934,16 @@ void launch_assign_ids(const unsigned long long *sorted_keys, const uint32_t *so
   k_assign_ids<<<grid_for(u, kBlock), kBlock, 0, st>>>(sorted_keys, sorted_slots, u, next_id, tab, rulebook);
 }
 
-void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const uint32_t *vals, cudaStream_t st) {
+void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlot *slots, cudaStream_t st) {
   if (!n) return;
-  k_remap<<<grid_for(n, kBlock), kBlock, 0, st>>>(s, n, temp_base, vals);
+  if ((reinterpret_cast<uintptr_t>(s) & 15u) == 0)
+    k_remap<true><<<grid_for((n + 3) / 4, kBlock), kBlock, 0, st>>>(s, n, temp_base, slots);
+  else
+    k_remap<false><<<grid_for(n, kBlock), kBlock, 0, st>>>(s, n, temp_base, slots);
+}
+
+void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st) {
+  k_table_clear<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, val_init);
 }
 
 void launch_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi, uint32_t start,

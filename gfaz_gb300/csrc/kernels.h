@@ -22,29 +22,48 @@ void launch_delta_encode(const int32_t *in, int32_t *out, uint64_t n, const uint
 // max |x| of the raw stream (delta_round == 0 seed).
 void launch_max_abs(const int32_t *in, uint64_t n, uint32_t *max_abs, cudaStream_t st);
 
-struct PairTable {
-  unsigned long long *keys;  // cap slots, kEmptyKey when free
-  uint32_t *flags;           // kFlag* bits per slot
-  uint32_t *vals;            // final rule id per used slot
-  uint64_t cap;              // power of two
+// One hash slot: the canonical key (kEmptyKey when free), its kFlag* bits
+// and the final rule id, in one 16-byte word so that a lookup is one load.
+struct alignas(16) PairSlot {
+  unsigned long long key;
+  uint32_t flags;
+  uint32_t val;
 };
+struct PairTable {
+  PairSlot *slots;  // cap slots
+  uint64_t cap;     // power of two, at most 2^31
+};
+// Sets every slot to {kEmptyKey, 0, val_init}.
+void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st);
 
-// Inserts every canonical adjacent pair inside a traversal.  Results:
-// status->u64[0] += new distinct keys, u64[1] += keys that became repeated.
-void launch_count_pairs(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav,
-                        PairTable tab, DevStatus *status, bool warp_dedup, cudaStream_t st);
+// Traversal-head bitmap of an n-step stream: head_words(n) words (padded
+// for tile staging); bit q set <=> some off[t] == q (t <= ntrav, so bit n is
+// set).  launch_head_bits sets the bits of a cleared bitmap.
+uint64_t head_words(uint64_t n);
+void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaStream_t st);
+
+// Inserts every canonical adjacent pair inside a traversal (heads: the
+// stream's head bitmap).  Results: status->u64[0] += new distinct keys,
+// u64[1] += keys that became repeated.
+void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
+                        bool warp_dedup, cudaStream_t st);
 
 // Greedy left-to-right replacement of candidate pairs; writes the compacted
 // stream with temporary symbols +-(temp_base + slot), the new traversal
 // offsets (ntrav + 1 entries) and status->u64[2] = output length.
-// desc: one u64 per tile, zeroed; tile_counter zeroed.
-void launch_apply(const int32_t *s, uint64_t n, const uint64_t *off, uint64_t ntrav, PairTable tab,
-                  int32_t temp_base, int32_t *out, uint64_t *new_off, unsigned long long *desc,
-                  uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+// heads: the stream's head bitmap; tile_trav: launch_tile_trav's table;
+// desc: one u64 per tile (apply_num_tiles), zeroed; tile_counter zeroed.
+void launch_apply(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
+                  const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
+                  unsigned long long *desc, uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
 uint64_t apply_num_tiles(uint64_t n);
+// tile_trav[k] = first traversal t with off[t] >= k * (apply tile), for the
+// apply_num_tiles(n) tiles.
+void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st);
 
 // Appends (transformed key, slot) of every used slot; count in status->u64[3].
-void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out,
+// Outputs beyond cap_out entries are dropped and flag kErrLength.
+void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
                          DevStatus *status, cudaStream_t st);
 
 // Stable LSD radix sort of (u64 key, u32 value) pairs on the given byte
@@ -62,8 +81,8 @@ void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *st
 // rulebook[rank] = original key.
 void launch_assign_ids(const unsigned long long *sorted_keys, const uint32_t *sorted_slots, uint64_t u,
                        uint32_t next_id, PairTable tab, long long *rulebook, cudaStream_t st);
-// Rewrites temporary symbols +-(temp_base + slot) into +-vals[slot].
-void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const uint32_t *vals, cudaStream_t st);
+// Rewrites temporary symbols +-(temp_base + slot) into +-slots[slot].val.
+void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlot *slots, cudaStream_t st);
 
 // ---- append encoder (add-haplotypes) -------------------------------------
 // Builds a key -> rule id table from stored rule columns (rules

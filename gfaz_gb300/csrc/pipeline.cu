@@ -62,17 +62,13 @@ bool debug_enabled() {
 }
 
 struct Table {
-  DevVec<unsigned long long> keys;
-  DevVec<uint32_t> flags, vals;
-  explicit Table(cudaStream_t st) : keys(st), flags(st), vals(st) {}
-  PairTable view(uint64_t cap) { return PairTable{keys.ptr, flags.ptr, vals.ptr, cap}; }
-  void prepare(uint64_t cap, cudaStream_t st, bool vals_ff = false) {
-    keys.resize(cap);
-    flags.resize(cap);
-    vals.resize(cap);
-    cuda_check(cudaMemsetAsync(keys.ptr, kEmptyByte, cap * sizeof(unsigned long long), st), "table clear");
-    cuda_check(cudaMemsetAsync(flags.ptr, 0, cap * sizeof(uint32_t), st), "table clear");
-    if (vals_ff) cuda_check(cudaMemsetAsync(vals.ptr, 0xFF, cap * sizeof(uint32_t), st), "table clear");
+  DevVec<PairSlot> slots;
+  explicit Table(cudaStream_t st) : slots(st) {}
+  PairTable view(uint64_t cap) { return PairTable{slots.ptr, cap}; }
+  // every slot {kEmptyKey, 0, val_init}
+  void prepare(uint64_t cap, cudaStream_t st, uint32_t val_init = 0) {
+    slots.resize(cap);
+    launch_table_clear(view(cap), val_init, st);
   }
 };
 
@@ -270,22 +266,29 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   DevVec<long long> rules(st);
   Table tab(st);
   DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
-  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st);
+  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st);
+  DevVec<uint64_t> tile_trav(st);
 
   uint64_t n = N;
   uint64_t prev_distinct = 0;
   for (int round = 0; round < p.rounds; ++round) {
     if (n < 2) break;
-    uint64_t est = prev_distinct ? prev_distinct * 2 : n / 8;
+    // first round: at most 4M distinct pairs expected (delta-coded
+    // traversals repeat few pairs); the table grows when it runs fuller
+    uint64_t est = prev_distinct ? prev_distinct * 2 : std::min<uint64_t>(n / 8, 1u << 22);
     est = std::min(est, n);
     uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
+    if (round == 0 && ctx.first_table_cap) cap = ctx.first_table_cap;
     uint64_t distinct = 0, repeated = 0;
+    heads.resize(head_words(n));
+    cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(n) * sizeof(uint32_t), st), "head bitmap clear");
+    GFZ_TIMED(ctx, "head_bits", launch_head_bits(offA.ptr, ntrav, heads.ptr, st));
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       tab.prepare(cap, st);
       ctx.reset_status();
       GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
-                launch_count_pairs(A.ptr, n, offA.ptr, ntrav, tab.view(cap), ds, ctx.warp_dedup, st));
+                launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, ctx.warp_dedup, st));
       const DevStatus &s = ctx.read_status();
       distinct = s.u64[0];
       repeated = s.u64[1];
@@ -304,12 +307,14 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     ctx.reset_status();
     uint32_t *counter;
     unsigned long long *desc = ctx.lookback(apply_num_tiles(n), &counter);
+    tile_trav.resize(std::max<uint64_t>(apply_num_tiles(n), 1));
+    GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, tile_trav.ptr, st));
     GFZ_TIMED_B(ctx, "apply", 4.0 * n,
-              launch_apply(A.ptr, n, offA.ptr, ntrav, tab.view(cap), temp_base, B.ptr, offB.ptr, desc, counter,
-                           ds, st));
+              launch_apply(A.ptr, n, heads.ptr, offA.ptr, ntrav, tile_trav.ptr, tab.view(cap), temp_base, B.ptr,
+                           offB.ptr, desc, counter, ds, st));
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
-    GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, ds, st));
+    GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, std::max<uint64_t>(repeated, 1), ds, st));
     const DevStatus &s1 = ctx.read_status();
     ctx.check_status("apply");
     const uint64_t n_out = s1.u64[2];
@@ -338,7 +343,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     GFZ_TIMED(ctx, "assign_ids",
               launch_assign_ids(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr, U, next_id,
                                 tab.view(cap), rules.ptr + g.nrules, st));
-    GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.vals.ptr, st));
+    GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
     if (debug_enabled())
       fprintf(stderr, "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu\n",
               round + 1, (unsigned long long)n, (unsigned long long)cap, (unsigned long long)distinct,
@@ -607,7 +612,7 @@ void append_encode(Context &ctx, const int32_t *first, const int32_t *second, ui
       const uint64_t lo = L.k == 0 ? 0 : L.flat_off / (uint64_t)L.k;
       if (lo + count > nrules) throw std::runtime_error("Add-haplotypes workflow error: rule column is truncated");
       const uint64_t cap = next_pow2(std::max<uint64_t>(2 * count + 1024, 1u << 12));
-      tab.prepare(cap, st, true);
+      tab.prepare(cap, st, 0xFFFFFFFFu);
       ctx.reset_status();
       GFZ_TIMED(ctx, "build_rule_table",
                 launch_build_rule_table(df.ptr, dsn.ptr, lo, lo + count, L.start, tab.view(cap), ctx.dstatus(), st));

@@ -110,7 +110,8 @@ class Context {
   void count_launch(uint64_t n = 1) { launches_ += n; }
 
   // tuning knobs
-  bool warp_dedup = true;
+  bool warp_dedup = false;
+  uint64_t first_table_cap = 0;  // pair-table slots of the first round (0 = automatic)
 
  private:
   int device_ = 0, sms_ = 152;

@@ -67,7 +67,10 @@ gfz_status gfz_context_set_timing(gfz_context *ctx, int enabled);
 /* JSON object {"kernel": {"ms": .., "launches": .., "bytes": ..}, ...} plus
  * "_launches": total kernels launched since the last reset. */
 gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, size_t *len);
-/* Tuning switch: warp-level de-duplication of pair inserts (default 1). */
+/* Tuning switches: "warp_dedup" = warp-level de-duplication of pair inserts
+ * (default 0); "first_table_cap" = pair-table slots of the first grammar
+ * round, a power of two (default 0 = sized automatically; the table grows
+ * when it fills either way). */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
