@@ -596,11 +596,9 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
     require(g && meta && size, "NULL argument");
     require(t0 <= t1 && t1 <= g->g.ntrav, "traversal range out of bounds");
     gfz::Context &c = ctx_of(ctx);
-    gfz::DevVec<int32_t> x(c.stream());
-    std::vector<uint64_t> off;
-    gfz::decode_traversals(c, g->g, t0, t1, x, off);
-    const gfz::TextPieces pieces = pieces_from_meta(meta, off);
-    g->text_size = gfz::emit_text(c, x, off, pieces, meta->mode, g->text);
+    g->text_size = gfz::decode_text(
+        c, g->g, t0, t1, [&](const std::vector<uint64_t> &off) { return pieces_from_meta(meta, off); }, meta->mode,
+        g->text);
     *size = g->text_size;
     if (out) {
       if (cap < g->text_size) throw std::length_error("output buffer too small");

@@ -55,6 +55,11 @@ __device__ __forceinline__ unsigned long long canon2(unsigned long long k) {
   return key_le(k, r) ? k : r;
 }
 
+// Symbol |x| = a is rule min_id + r for r < nrules; anything else is a step.
+__device__ __forceinline__ bool is_rule(uint32_t a, uint32_t min_id, uint64_t nrules) {
+  return a >= min_id && (uint64_t)(a - min_id) < nrules;
+}
+
 // 32-bit slot hash of a packed key: the halves are combined with an odd
 // (golden-ratio) multiplier, then mixed by MurmurHash3's 32-bit finaliser
 // (Appleby, public domain).  Cheaper than a 64-bit mix and ample for tables
@@ -177,6 +182,30 @@ __device__ __forceinline__ typename Op::S warp_lookback(unsigned long long *desc
     }
     base -= 32 * K;
   }
+}
+
+// Block-wide exclusive sum of a u64 per thread; also returns the total.
+template <int BLOCK>
+__device__ __forceinline__ unsigned long long block_excl_sum(unsigned long long v, unsigned long long &total) {
+  __shared__ unsigned long long s_w[BLOCK / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long inc = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long o = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += o;
+  }
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  unsigned long long pre = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < BLOCK / 32; ++w) {
+    if (w == warp) pre = tot;
+    tot += s_w[w];
+  }
+  total = tot;
+  __syncthreads();
+  return pre + inc - v;
 }
 
 // u64 running sum.

@@ -582,10 +582,8 @@ std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
     const auto names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
     const auto ovs = split_strings(unzstd_str(c.overlaps), unzstd_u32(c.overlap_lengths), true, kWriterErr);
     const std::vector<uint64_t> off(g.h_off.begin(), g.h_off.begin() + (ptrdiff_t)ls.np + 1);
-    DevVec<int32_t> x(ctx.stream());
-    std::vector<uint64_t> xoff;
-    decode_traversals(ctx, g, 0, ls.np, x, xoff);
-    const uint64_t n = emit_text(ctx, x, xoff, path_pieces(names, ovs, xoff), 0, text);
+    const uint64_t n = decode_text(
+        ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0, text);
     download_text(ctx, text, n, out);
   }
   if (ls.nw) {
@@ -595,10 +593,10 @@ std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
     const auto seqids = split_strings(unzstd_str(c.walk_seq_ids), unzstd_u32(c.walk_seq_id_lengths), true, kWriterErr);
     const auto starts = unvarint_i64(c.walk_seq_starts, c.walk_lengths.size());
     const auto ends = unvarint_i64(c.walk_seq_ends, c.walk_lengths.size());
-    DevVec<int32_t> x(ctx.stream());
-    std::vector<uint64_t> xoff;
-    decode_traversals(ctx, g, ls.np, ls.np + ls.nw, x, xoff);
-    const uint64_t n = emit_text(ctx, x, xoff, walk_pieces(samples, haps, seqids, starts, ends, xoff), 1, text);
+    const uint64_t n = decode_text(
+        ctx, g, ls.np, ls.np + ls.nw,
+        [&](const std::vector<uint64_t> &xoff) { return walk_pieces(samples, haps, seqids, starts, ends, xoff); }, 1,
+        text);
     download_text(ctx, text, n, out);
   }
   return out;
@@ -705,11 +703,10 @@ std::vector<std::string> decode_selected(Context &ctx, const Compressed &c, cons
   Grammar g(ctx.stream());
   decode_rule_columns(ctx, c, g);
   load_encoded(ctx, g, sel.data(), soff);
-  DevVec<int32_t> x(ctx.stream());
-  std::vector<uint64_t> xoff;
-  decode_traversals(ctx, g, 0, idx.size(), x, xoff);
   DevVec<char> text(ctx.stream());
-  const uint64_t n = emit_text(ctx, x, xoff, make_pieces(pre, suf, xoff), mode, text);
+  const uint64_t n = decode_text(
+      ctx, g, 0, idx.size(), [&](const std::vector<uint64_t> &xoff) { return make_pieces(pre, suf, xoff); }, mode,
+      text);
   std::string s;
   download_text(ctx, text, n, s);
   return split_lines(s, idx.size());

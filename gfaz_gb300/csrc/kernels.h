@@ -139,4 +139,61 @@ uint64_t text_num_tiles(uint64_t n);
 void launch_gather_ranges(const int32_t *src, const uint64_t *starts, const uint64_t *dst_off, uint64_t nr,
                           int32_t *dst, cudaStream_t st);
 
+// ---- prefix-sum expansion decoder (expand_kernels.cu) ----------------------
+// Rule r (id min_id + r) expands to rlen[r] steps whose inclusive prefix
+// sums are rpre[roff[r] .. roff[r] + rlen[r]).
+struct RulePrefixView {
+  const uint32_t *rlen;
+  const uint64_t *roff;  // nrules + 1
+  const int32_t *rpre;
+  uint32_t min_id;
+  uint64_t nrules;
+};
+// Encoded symbols expanding to output steps [0, total): symbol i covers
+// [pos[i], pos[i + 1]); rec[i] = {symbol, prefix buffer base, rule length
+// (0 for a plain step), S_i = sum of the expansions before it in its
+// traversal}; tile_sym from launch_tile_symbols.
+struct ExpandSource {
+  const int4 *rec;
+  const uint64_t *pos;  // m + 1
+  const uint64_t *tile_sym;
+  uint64_t m, total;
+  RulePrefixView rules;
+};
+// Output traversals off[0 .. ntrav] (off[ntrav] = total), their head bitmap
+// (launch_head_bits over off) and the text pieces.
+struct TextSource {
+  const uint64_t *off;
+  uint64_t ntrav;
+  const uint32_t *heads;
+  TextMeta meta;
+};
+// One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
+// waiting, zero before pass 1).  status->u64[6] += rules still waiting.
+void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
+                             uint32_t *built, uint32_t pass, DevStatus *status, cudaStream_t st);
+// out[0 .. n] = exclusive scan of in[0 .. n) (out[n] = total); desc: one u64
+// per excl_scan_tiles(n) tile (at least one), zeroed; tile_counter zeroed.
+uint64_t excl_scan_tiles(uint64_t n);
+void launch_excl_scan_u32(const uint32_t *in, uint64_t n, uint64_t *out, unsigned long long *desc,
+                          uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+void launch_excl_scan_u64(const uint64_t *in, uint64_t n, uint64_t *out, unsigned long long *desc,
+                          uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+// rec[i] = {enc[i], base, length, total of its expansion} and, unless tot is
+// null, tot[i] = that total; launch_symbol_exclusive then turns rec[i].w
+// into incl[i] - total (incl: inclusive segmented sums of tot).
+void launch_symbol_records(const int32_t *enc, uint64_t m, RulePrefixView rv, int4 *rec, int32_t *tot,
+                           cudaStream_t st);
+void launch_symbol_exclusive(int4 *rec, const int32_t *incl, uint64_t m, cudaStream_t st);
+// Output tiles of the expansion kernels and the symbol at each tile start
+// (expand_num_tiles(total) + 1 entries).
+uint64_t expand_num_tiles(uint64_t total);
+void launch_tile_symbols(const uint64_t *pos, uint64_t m, uint64_t total, uint64_t *tile_sym, cudaStream_t st);
+// Decoded steps (delta = delta_round, 0 or 1) of every output position.
+void launch_expand_steps(const ExpandSource &E, int delta, int32_t *out, cudaStream_t st);
+// P/W text: bytes per output tile, then the text of each tile at tile_off.
+void launch_text_lengths(const ExpandSource &E, const TextSource &T, int delta, uint64_t *tile_len, cudaStream_t st);
+void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *tile_off, char *text,
+                       cudaStream_t st);
+
 }  // namespace gfz

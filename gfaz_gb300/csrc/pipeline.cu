@@ -275,7 +275,9 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     if (n < 2) break;
     // first round: at most 4M distinct pairs expected (delta-coded
     // traversals repeat few pairs); the table grows when it runs fuller
-    uint64_t est = prev_distinct ? prev_distinct * 2 : std::min<uint64_t>(n / 8, 1u << 22);
+    // later rounds: distinct pairs grow by up to ~3x per round as rules
+    // pair with each other
+    uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
     est = std::min(est, n);
     uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
     if (round == 0 && ctx.first_table_cap) cap = ctx.first_table_cap;
@@ -292,7 +294,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
       const DevStatus &s = ctx.read_status();
       distinct = s.u64[0];
       repeated = s.u64[1];
-      if ((s.err & kErrTableFull) || distinct * 10 > cap * 7) {
+      if ((s.err & kErrTableFull) || distinct * 10 > cap * 8) {
         cap *= 4;
         continue;
       }
@@ -401,6 +403,7 @@ void load_rules(Context &ctx, Grammar &g, const int32_t *first, const int32_t *s
   g.second.resize(std::max<uint64_t>(nrules, 1));
   g.first.size = g.second.size = nrules;
   g.rlen_ready = false;
+  g.rpre_state = 0;
   if (!nrules) return;
   cuda_check(cudaMemcpyAsync(g.first.ptr, first, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
   cuda_check(cudaMemcpyAsync(g.second.ptr, second, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
@@ -467,11 +470,138 @@ static void ensure_rule_lengths(Context &ctx, Grammar &g) {
   g.rlen_ready = true;
 }
 
+// Rule prefix buffers larger than this (in steps) are not built; decoding
+// then expands symbol by symbol.
+constexpr uint64_t kMaxPrefixSteps = 1ull << 31;
+
+// Builds g.roff / g.rpre once per grammar (see expand_kernels.cu); false when
+// the buffer would exceed kMaxPrefixSteps.
+static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
+  if (g.rpre_state) return g.rpre_state > 0;
+  ensure_rule_lengths(ctx, g);
+  cudaStream_t st = ctx.stream();
+  const uint64_t R = g.nrules;
+  g.roff.resize(R + 1);
+  ctx.reset_status();
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
+  GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(g.rlen.ptr, R, g.roff.ptr, desc, counter, ctx.dstatus(), st));
+  uint64_t steps = 0;
+  cuda_check(cudaMemcpyAsync(&steps, g.roff.ptr + R, sizeof(steps), cudaMemcpyDeviceToHost, st), "prefix size");
+  ctx.read_status();
+  ctx.check_status("rule prefix offsets");
+  if (steps > kMaxPrefixSteps) {
+    g.rpre_state = -1;
+    return false;
+  }
+  g.rpre.resize(std::max<uint64_t>(steps, 1));
+  if (R) {
+    DevVec<uint32_t> built(st);
+    built.resize(R);
+    cuda_check(cudaMemsetAsync(built.ptr, 0, R * sizeof(uint32_t), st), "prefix clear");
+    const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, R};
+    uint64_t prev_open = UINT64_MAX;
+    for (uint32_t pass = 1;; ++pass) {
+      ctx.reset_status();
+      GFZ_TIMED_B(ctx, "rule_prefix", 0,
+                  launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, built.ptr, pass, ctx.dstatus(),
+                                          st));
+      const DevStatus &s = ctx.read_status();
+      ctx.check_status("rule prefix");
+      const uint64_t open = s.u64[6];
+      if (open == 0) break;
+      if (open >= prev_open) throw std::runtime_error("rule expansions do not resolve: the rulebook references itself");
+      prev_open = open;
+    }
+  }
+  g.rpre_state = 1;
+  return true;
+}
+
+// Device data of one expansion: symbol positions, output offsets, symbol
+// sums (delta_round 1) and the symbol at each output tile.
+struct ExpandPlan {
+  explicit ExpandPlan(cudaStream_t st) : pos(st), out_off(st), tile_sym(st), rec(st) {}
+  DevVec<uint64_t> pos, out_off, tile_sym;
+  DevVec<int4> rec;
+  std::vector<uint64_t> h_out_off;
+  uint64_t m = 0, total = 0;
+  ExpandSource source(const Grammar &g) const {
+    return ExpandSource{rec.ptr, pos.ptr, tile_sym.ptr, m, total,
+                        RulePrefixView{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, g.nrules}};
+  }
+};
+
+// The prefix decoder applies to delta_round 0 and 1 with a buildable
+// prefix buffer; other streams expand symbol by symbol.
+static bool prefix_decodable(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1) {
+  if (g.delta_round > 1) return false;
+  if (g.h_off[t1] == g.h_off[t0]) return false;  // no symbols: nothing to expand
+  return ensure_rule_prefix(ctx, g);
+}
+
+static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, ExpandPlan &P) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t e0 = g.h_off[t0], e1 = g.h_off[t1];
+  const uint64_t m = e1 - e0, nt = t1 - t0;
+  P.m = m;
+  P.pos.resize(m + 1);
+  P.out_off.resize(nt + 1);
+  ctx.reset_status();
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(scan_num_tiles(m), &counter);
+  GFZ_TIMED_B(ctx, "symbol_positions", 12.0 * m, launch_symbol_positions(g.enc.ptr + e0, m, g.layer_start, g.nrules,
+                                                             g.rlen.ptr, P.pos.ptr, desc, counter, ctx.dstatus(), st));
+  GFZ_TIMED(ctx, "gather_pos", (k_gather_pos<<<grid_for(nt + 1, 256), 256, 0, st>>>(
+                                   P.pos.ptr, g.off.ptr + t0, nt + 1, e0, P.out_off.ptr)));
+  P.h_out_off.resize(nt + 1);
+  cuda_check(cudaMemcpyAsync(P.h_out_off.data(), P.out_off.ptr, (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                             st),
+             "offsets download");
+  ctx.read_status();
+  ctx.check_status("expansion offsets");
+  P.total = P.h_out_off[nt];
+  const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, g.nrules};
+  P.rec.resize(m);
+  if (g.delta_round == 1) {
+    // S_i: segmented (per traversal) exclusive sums of the symbol totals
+    DevVec<int32_t> sums(st);
+    sums.resize(m);
+    DevVec<uint64_t> loc(st);
+    std::vector<uint64_t> h_loc(nt + 1);
+    for (uint64_t t = 0; t <= nt; ++t) h_loc[t] = g.h_off[t0 + t] - e0;
+    loc.resize(nt + 1);
+    cuda_check(cudaMemcpyAsync(loc.ptr, h_loc.data(), (nt + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
+               "offsets upload");
+    GFZ_TIMED_B(ctx, "symbol_sums", 24.0 * m, launch_symbol_records(g.enc.ptr + e0, m, rv, P.rec.ptr, sums.ptr, st));
+    desc = ctx.lookback(scan_num_tiles(m), &counter);
+    GFZ_TIMED_B(ctx, "symbol_sums", 8.0 * m,
+                launch_inverse_delta(sums.ptr, m, loc.ptr, nt, desc, counter, ctx.dstatus(), st));
+    GFZ_TIMED_B(ctx, "symbol_sums", 36.0 * m, launch_symbol_exclusive(P.rec.ptr, sums.ptr, m, st));
+  } else {
+    GFZ_TIMED_B(ctx, "symbol_sums", 20.0 * m, launch_symbol_records(g.enc.ptr + e0, m, rv, P.rec.ptr, nullptr, st));
+  }
+  P.tile_sym.resize(expand_num_tiles(P.total) + 1);
+  GFZ_TIMED(ctx, "tile_symbols", launch_tile_symbols(P.pos.ptr, m, P.total, P.tile_sym.ptr, st));
+}
+
 void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVec<int32_t> &out,
                        std::vector<uint64_t> &out_off) {
   cudaStream_t st = ctx.stream();
   if (t1 < t0 || t1 > g.ntrav) throw std::out_of_range("traversal range out of bounds");
   ensure_rule_lengths(ctx, g);
+  if (prefix_decodable(ctx, g, t0, t1)) {
+    ExpandPlan P(st);
+    plan_expansion(ctx, g, t0, t1, P);
+    out.resize(std::max<uint64_t>(P.total, 1));
+    out.size = P.total;
+    const ExpandSource E = P.source(g);
+    GFZ_TIMED_B(ctx, "expand_steps", 8.0 * P.total, launch_expand_steps(E, g.delta_round, out.ptr, st));
+    ctx.read_status();
+    ctx.check_status("expansion");
+    out_off = std::move(P.h_out_off);
+    return;
+  }
   const uint64_t e0 = g.h_off[t0], e1 = g.h_off[t1];
   const uint64_t m = e1 - e0;
   const uint64_t nt = t1 - t0;
@@ -564,12 +694,76 @@ uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uin
   return text.size;
 }
 
-uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, const TextPieces &pieces, int mode,
+// Text pieces on the device.
+struct DevPieces {
+  explicit DevPieces(cudaStream_t st) : pre(st), suf(st), blob(st), tail(st) {}
+  DevVec<uint64_t> pre, suf;
+  DevVec<char> blob, tail;
+  void upload(const TextPieces &p, cudaStream_t st) {
+    const uint64_t n1 = p.pre_off.size();
+    pre.resize(n1);
+    suf.resize(n1);
+    blob.resize(std::max<size_t>(p.blob.size(), 1));
+    tail.resize(std::max<size_t>(p.tail.size(), 1));
+    cuda_check(cudaMemcpyAsync(pre.ptr, p.pre_off.data(), n1 * 8, cudaMemcpyHostToDevice, st), "upload");
+    cuda_check(cudaMemcpyAsync(suf.ptr, p.suf_off.data(), n1 * 8, cudaMemcpyHostToDevice, st), "upload");
+    if (!p.blob.empty())
+      cuda_check(cudaMemcpyAsync(blob.ptr, p.blob.data(), p.blob.size(), cudaMemcpyHostToDevice, st), "upload");
+    if (!p.tail.empty())
+      cuda_check(cudaMemcpyAsync(tail.ptr, p.tail.data(), p.tail.size(), cudaMemcpyHostToDevice, st), "upload");
+  }
+};
+
+uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
+                     const std::function<TextPieces(const std::vector<uint64_t> &)> &make_pieces, int mode,
                      DevVec<char> &text) {
-  DevVec<int32_t> x(ctx.stream());
-  std::vector<uint64_t> off;
-  decode_traversals(ctx, g, t0, t1, x, off);
-  return emit_text(ctx, x, off, pieces, mode, text);
+  cudaStream_t st = ctx.stream();
+  if (t1 < t0 || t1 > g.ntrav) throw std::out_of_range("traversal range out of bounds");
+  ensure_rule_lengths(ctx, g);
+  if (!prefix_decodable(ctx, g, t0, t1)) {
+    DevVec<int32_t> x(st);
+    std::vector<uint64_t> off;
+    decode_traversals(ctx, g, t0, t1, x, off);
+    return emit_text(ctx, x, off, make_pieces(off), mode, text);
+  }
+  ExpandPlan P(st);
+  plan_expansion(ctx, g, t0, t1, P);
+  const uint64_t nt = t1 - t0;
+  const TextPieces pieces = make_pieces(P.h_out_off);
+  DevPieces dp(st);
+  dp.upload(pieces, st);
+  DevVec<uint32_t> heads(st);
+  heads.resize(head_words(P.total));
+  cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(P.total) * sizeof(uint32_t), st), "head bitmap clear");
+  GFZ_TIMED(ctx, "head_bits", launch_head_bits(P.out_off.ptr, nt, heads.ptr, st));
+  const TextMeta meta{dp.blob.ptr, dp.pre.ptr, dp.suf.ptr, dp.tail.ptr, (uint64_t)pieces.tail.size(), mode};
+  const TextSource T{P.out_off.ptr, nt, heads.ptr, meta};
+  const ExpandSource E = P.source(g);
+  const uint64_t tiles = expand_num_tiles(P.total);
+  DevVec<uint64_t> tile_len(st), tile_off(st);
+  tile_len.resize(tiles);
+  tile_off.resize(tiles + 1);
+  ctx.reset_status();
+  GFZ_TIMED_B(ctx, "text_lengths", 4.0 * P.total, launch_text_lengths(E, T, g.delta_round, tile_len.ptr, st));
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(tiles), &counter);
+  GFZ_TIMED(ctx, "text_scan",
+            launch_excl_scan_u64(tile_len.ptr, tiles, tile_off.ptr, desc, counter, ctx.dstatus(), st));
+  uint64_t body = 0;
+  cuda_check(cudaMemcpyAsync(&body, tile_off.ptr + tiles, sizeof(body), cudaMemcpyDeviceToHost, st), "text size");
+  ctx.read_status();
+  ctx.check_status("text lengths");
+  const uint64_t size = body + pieces.tail.size();
+  text.resize(std::max<uint64_t>(size, 1));
+  text.size = size;
+  GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
+              launch_text_write(E, T, g.delta_round, tile_off.ptr, text.ptr, st));
+  if (!pieces.tail.empty())
+    cuda_check(cudaMemcpyAsync(text.ptr + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
+               "text tail");
+  ctx.read_status();
+  ctx.check_status("text emission");
+  return size;
 }
 
 // ---------------------------------------------------------------------------

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -139,7 +140,8 @@ class Context {
 // Device-resident grammar: the result of compression, or a rulebook + encoded
 // streams loaded from a container for decompression.
 struct Grammar {
-  explicit Grammar(cudaStream_t st) : enc(st), off(st), rules(st), first(st), second(st), rlen(st) {}
+  explicit Grammar(cudaStream_t st)
+      : enc(st), off(st), rules(st), first(st), second(st), rlen(st), roff(st), rpre(st) {}
   DevVec<int32_t> enc;         // encoded traversals back to back
   DevVec<uint64_t> off;        // ntrav + 1 offsets into enc
   std::vector<uint64_t> h_off; // host copy of off
@@ -147,11 +149,14 @@ struct Grammar {
   DevVec<long long> rules;     // packed rulebook (index = id - layer_start)
   DevVec<int32_t> first, second;  // decoded rule columns (decode side)
   DevVec<uint32_t> rlen;       // rule expansion lengths (decode side)
+  DevVec<uint64_t> roff;       // rule prefix buffer: offsets (nrules + 1)
+  DevVec<int32_t> rpre;        // inclusive prefix sums of every rule's expansion
   uint64_t nrules = 0;
   uint32_t layer_start = 0, next_id = 0;
   int delta_round = 1;
   int rounds_done = 0;
   bool rlen_ready = false;
+  int rpre_state = 0;          // 0 not built, 1 built, -1 too large (per-symbol expansion instead)
 };
 
 struct EncodeParams {
@@ -192,8 +197,10 @@ struct TextPieces {
 uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uint64_t> &off,
                    const TextPieces &pieces, int mode, DevVec<char> &text);
 
-// Decode + text for traversals [t0, t1) of g: the fused convenience path.
-uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, const TextPieces &pieces, int mode,
+// Decode + text for traversals [t0, t1) of g.  `pieces` builds the text
+// pieces from the decoded traversal offsets (t1 - t0 + 1 entries, from 0).
+uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
+                     const std::function<TextPieces(const std::vector<uint64_t> &)> &pieces, int mode,
                      DevVec<char> &text);
 
 // Append encoding with a stored rulebook (one stack-encoder pass per layer).

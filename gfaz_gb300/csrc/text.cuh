@@ -1,0 +1,71 @@
+// Device helpers for GFA P/W text: decimal digits, traversal lookup and
+// staged byte copies (the formats of format_*_line_numeric,
+// src/io/gfa_write_utils.cpp:238-290).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gfz {
+
+__device__ __forceinline__ uint32_t dec_digits(uint32_t v) {
+  uint32_t d = 1;
+  d += v >= 10u;
+  d += v >= 100u;
+  d += v >= 1000u;
+  d += v >= 10000u;
+  d += v >= 100000u;
+  d += v >= 1000000u;
+  d += v >= 10000000u;
+  d += v >= 100000000u;
+  d += v >= 1000000000u;
+  return d;
+}
+
+__device__ __forceinline__ void put_dec(char *dst, uint32_t v, uint32_t nd) {
+  for (uint32_t i = nd; i-- > 0;) {
+    dst[i] = (char)('0' + v % 10u);
+    v /= 10u;
+  }
+}
+
+// Largest t with off[t] <= p (p < off[ntrav]).
+__device__ __forceinline__ uint64_t trav_of(const uint64_t *off, uint64_t ntrav, uint64_t p) {
+  uint64_t lo = 0, hi = ntrav;  // answer in [0, ntrav)
+  while (hi - lo > 1) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= p) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Copies len bytes from a 16-byte aligned shared buffer (with >= 16 bytes of
+// slack after len) to global memory using 16-byte stores where aligned.
+template <int BLOCK>
+__device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, char *dst) {
+  const uint32_t mis = (uint32_t)((uintptr_t)dst & 15u);
+  uint32_t head = (16u - mis) & 15u;
+  if (head > len) head = len;
+  for (uint32_t i = threadIdx.x; i < head; i += BLOCK) dst[i] = sbuf[i];
+  const uint32_t body = (len - head) >> 4;
+  const uint32_t *sw = reinterpret_cast<const uint32_t *>(sbuf);
+  const uint32_t r = head & 3u, sh = 8u * r;
+  for (uint32_t v = threadIdx.x; v < body; v += BLOCK) {
+    const uint32_t o = head + 16u * v;
+    const uint32_t w = o >> 2;
+    uint4 val;
+    if (r == 0) {
+      val = make_uint4(sw[w], sw[w + 1], sw[w + 2], sw[w + 3]);
+    } else {
+      const uint32_t a0 = sw[w], a1 = sw[w + 1], a2 = sw[w + 2], a3 = sw[w + 3], a4 = sw[w + 4];
+      val = make_uint4(__funnelshift_r(a0, a1, sh), __funnelshift_r(a1, a2, sh), __funnelshift_r(a2, a3, sh),
+                       __funnelshift_r(a3, a4, sh));
+    }
+    *reinterpret_cast<uint4 *>(dst + o) = val;
+  }
+  for (uint32_t i = head + 16u * body + threadIdx.x; i < len; i += BLOCK) dst[i] = sbuf[i];
+}
+
+constexpr uint32_t kTextBuf = 28 * 1024;
+
+}  // namespace gfz
