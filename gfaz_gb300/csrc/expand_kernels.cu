@@ -53,8 +53,8 @@ __device__ __forceinline__ uint32_t child_prefix(int32_t c, uint32_t o, const Ru
 // pre_second) and records built[R] = pass.  Rules still waiting are counted
 // in status->u64[6].
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
-                                   RulePrefixView rv, int32_t *rpre, uint32_t *built, uint32_t pass,
-                                   DevStatus *status) {
+                                   RulePrefixView rv, int32_t *rpre, int4 *rstat, int delta, uint32_t *built,
+                                   uint32_t pass, DevStatus *status) {
   __shared__ uint32_t s_open;
   if (threadIdx.x == 0) s_open = 0;
   __syncthreads();
@@ -78,12 +78,30 @@ __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int3
       continue;
     }
     const uint64_t b = rv.roff[i];
-    uint32_t last = 0;
-    for (uint32_t o = 0; o < lf; ++o) {
-      last = child_prefix(f, o, rv);
-      rpre[b + o] = (int32_t)last;
+    const uint32_t L = lf + lg;
+    // value ranges for the text length shortcut: delta 1: prefix values
+    // (all, and {0} plus all but the last); delta 0: expansion values
+    int32_t mnA = INT32_MAX, mxA = INT32_MIN, mnB = 0, mxB = 0;
+    uint32_t prev = 0, tf = 0;
+    for (uint32_t o = 0; o < L; ++o) {
+      uint32_t x;
+      if (o < lf) {
+        x = child_prefix(f, o, rv);
+        tf = x;
+      } else {
+        x = tf + child_prefix(g, o - lf, rv);
+      }
+      rpre[b + o] = (int32_t)x;
+      const int32_t y = delta ? (int32_t)x : (int32_t)(x - prev);
+      prev = x;
+      mnA = min(mnA, y);
+      mxA = max(mxA, y);
+      if (delta && o + 1 < L) {
+        mnB = min(mnB, y);
+        mxB = max(mxB, y);
+      }
     }
-    for (uint32_t o = 0; o < lg; ++o) rpre[b + lf + o] = (int32_t)(last + child_prefix(g, o, rv));
+    rstat[i] = make_int4(mnA, mxA, mnB, mxB);
     built[i] = pass;
   }
   open = __reduce_add_sync(0xffffffffu, open);
@@ -128,14 +146,6 @@ __global__ void __launch_bounds__(BLOCK) k_excl_scan(const T *__restrict__ in, u
 // ---------------------------------------------------------------------------
 // Encoded symbols
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t symbol_total(int32_t v, const RulePrefixView &rv) {
-  const uint32_t a = abs32(v);
-  if (!is_rule(a, rv.min_id, rv.nrules)) return (uint32_t)v;
-  const uint64_t r = a - rv.min_id;
-  const uint32_t tot = (uint32_t)rv.rpre[rv.roff[r] + rv.rlen[r] - 1];
-  return v > 0 ? tot : 0u - tot;
-}
-
 // rec[i] = {symbol, prefix buffer base, rule length (0 for a step), total of
 // its expansion}; tot[i] = that total again (scanned in place afterwards).
 __global__ void k_symbol_records(const int32_t *__restrict__ enc, uint64_t m, RulePrefixView rv, int4 *rec,
@@ -309,109 +319,230 @@ __global__ void __launch_bounds__(BLOCK) k_expand_steps(ExpandSource E, int32_t 
 // ---------------------------------------------------------------------------
 // Text
 // ---------------------------------------------------------------------------
-// Text bytes of one step: the number, its orientation mark and (P lines,
-// not last) the comma.
-__device__ __forceinline__ uint32_t step_text_len(int32_t v, bool pmode, bool last) {
-  return dec_digits(abs32(v)) + 1u + ((pmode && !last) ? 1u : 0u);
+__device__ __forceinline__ bool head_at(const uint32_t *heads, uint64_t q) { return (heads[q >> 5] >> (q & 31)) & 1u; }
+
+// Digit count shared by every value in [lo, hi] (exact, no wrap-around), or
+// 0 when the values differ in length or the range leaves int32.
+__device__ __forceinline__ uint32_t uniform_digits(long long lo, long long hi) {
+  if (lo < INT32_MIN || hi > INT32_MAX) return 0;
+  uint32_t a, b;
+  if (lo >= 0) {
+    a = dec_digits((uint32_t)lo);
+    b = dec_digits((uint32_t)hi);
+  } else if (hi <= 0) {
+    a = dec_digits((uint32_t)(-lo));
+    b = dec_digits((uint32_t)(-hi));
+  } else {
+    a = 1;
+    b = dec_digits((uint32_t)max(-lo, hi));
+  }
+  return a == b ? a : 0u;
 }
 
-// Per-thread text length of steps p0 .. p0 + ITEMS - 1; fst/lst bits of
-// those steps come from the output head bitmap.
-template <int ITEMS>
-__device__ __forceinline__ unsigned long long thread_text_len(const int32_t (&val)[ITEMS], uint32_t cnt, uint64_t p0,
-                                                              const TextSource &T, uint32_t &hd) {
-  hd = 0;
-  if (!cnt) return 0;
-  const uint64_t w = p0 >> 5;
-  const unsigned long long two = ((unsigned long long)T.heads[w + 1] << 32) | T.heads[w];
-  hd = (uint32_t)(two >> (p0 & 31));  // bit k: step p0 + k starts a traversal (ITEMS <= 31)
-  const bool pmode = T.meta.mode == 0;
-  unsigned long long len = 0;
-#pragma unroll
-  for (int k = 0; k < ITEMS; ++k) {
-    if ((uint32_t)k < cnt) {
-      const bool fst = (hd >> k) & 1u, lst = (hd >> (k + 1)) & 1u;
-      len += step_text_len(val[k], pmode, lst);
-      if (fst | lst) {
-        const uint64_t t = trav_of(T.off, T.ntrav, p0 + k);
-        if (fst) len += T.meta.pre_off[t + 1] - T.meta.pre_off[t];
-        if (lst) len += T.meta.suf_off[t + 1] - T.meta.suf_off[t];
-      }
-    }
+// The digit count all steps of symbol r share (0 if they differ); rtot is
+// the rule total when r is a reversed rule (delta 1).
+template <int DELTA>
+__device__ __forceinline__ uint32_t symbol_digits(const int4 &r, uint32_t rtot, const RulePrefixView &rv) {
+  const int32_t v = r.x;
+  const uint32_t L = (uint32_t)r.z;
+  if (L == 0) return dec_digits(abs32(DELTA ? (int32_t)((uint32_t)r.w + (uint32_t)v) : v));
+  const int4 st = rv.rstat[abs32(v) - rv.min_id];
+  if (DELTA) {
+    if (v > 0) return uniform_digits((long long)r.w + st.x, (long long)r.w + st.y);
+    const long long base = (long long)r.w - (long long)(int32_t)rtot;
+    return uniform_digits(base + st.z, base + st.w);
   }
+  return v > 0 ? uniform_digits(st.x, st.y) : uniform_digits(-(long long)st.y, -(long long)st.x);
+}
+
+// Text bytes of steps [from, to) of symbol r (none of them the last step of
+// its traversal): digits plus the orientation mark and, in P lines, a comma.
+template <int DELTA>
+__device__ __forceinline__ unsigned long long steps_text(const int4 &r, uint32_t rtot, uint32_t dig, uint32_t from,
+                                                         uint32_t to, bool pmode, const int32_t *__restrict__ rpre) {
+  const uint32_t per = pmode ? 2u : 1u;
+  if (dig) return (unsigned long long)(to - from) * (dig + per);
+  unsigned long long len = 0;
+  for (uint32_t o = from; o < to; ++o) len += dec_digits(abs32(symbol_step<DELTA>(r, rtot, o, rpre))) + per;
   return len;
 }
 
-template <int BLOCK, int ITEMS, int DELTA>
-__global__ void __launch_bounds__(BLOCK) k_text_lengths(ExpandSource E, TextSource T, uint64_t *tile_len) {
-  constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ SymStage S;
-  const uint64_t tile = blockIdx.x;
-  stage_symbols<BLOCK>(E, tile, S);
-  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
-  int32_t val[ITEMS];
-  const uint32_t cnt = thread_values<ITEMS, DELTA>(E, S, tile, p0, val);
-  uint32_t hd;
-  unsigned long long len = thread_text_len<ITEMS>(val, cnt, p0, T, hd);
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) len += __shfl_xor_sync(0xffffffffu, len, d);
-  __shared__ unsigned long long s_w[BLOCK / 32];
-  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = len;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long t = 0;
-    for (int w = 0; w < BLOCK / 32; ++w) t += s_w[w];
-    tile_len[tile] = t;
+__device__ __forceinline__ uint64_t pre_len(const TextSource &T, uint64_t t) { return T.meta.pre_off[t + 1] - T.meta.pre_off[t]; }
+__device__ __forceinline__ uint64_t suf_len(const TextSource &T, uint64_t t) { return T.meta.suf_off[t + 1] - T.meta.suf_off[t]; }
+
+template <int DELTA>
+__device__ __forceinline__ uint32_t reversed_total(const int4 &r, const int32_t *__restrict__ rpre) {
+  return (DELTA && r.x < 0 && r.z != 0) ? (uint32_t)rpre[(uint32_t)r.y + (uint32_t)r.z - 1] : 0u;
+}
+
+// slen[i]: the line prefix (first symbol of a traversal), the steps, and the
+// line suffix (last symbol); sdig[i]: the shared digit count or 0.
+template <int DELTA>
+__global__ void k_symbol_text(ExpandSource E, TextSource T, uint64_t *slen, uint8_t *sdig) {
+  const bool pmode = T.meta.mode == 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E.m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int4 r = E.rec[i];
+    const uint64_t start = E.pos[i], end = E.pos[i + 1];
+    const uint32_t rtot = reversed_total<DELTA>(r, E.rules.rpre);
+    const uint32_t dig = symbol_digits<DELTA>(r, rtot, E.rules);
+    unsigned long long len = steps_text<DELTA>(r, rtot, dig, 0, (uint32_t)(end - start), pmode, E.rules.rpre);
+    const bool fst = head_at(T.heads, start), lst = head_at(T.heads, end);
+    if (fst | lst) {
+      const uint64_t t = trav_of(T.off, T.ntrav, start);
+      if (fst) len += pre_len(T, t);
+      if (lst) len += suf_len(T, t) - (pmode ? 1ull : 0ull);  // no comma after the last step
+    }
+    slen[i] = len;
+    sdig[i] = (uint8_t)dig;
   }
 }
 
+// Text offset of output step p (p < total) held by symbol r (index i,
+// steps from `start`): where the text of p begins, before the line prefix
+// if p opens its traversal.
+template <int DELTA>
+__device__ __forceinline__ unsigned long long step_offset(const ExpandSource &E, const TextSource &T,
+                                                          const uint64_t *soff, const uint8_t *sdig, uint64_t i,
+                                                          const int4 &r, uint64_t start, uint64_t p, bool pmode) {
+  unsigned long long o = soff[i];
+  if (p == start) return o;
+  if (head_at(T.heads, start)) o += pre_len(T, trav_of(T.off, T.ntrav, start));
+  const uint32_t rtot = reversed_total<DELTA>(r, E.rules.rpre);
+  return o + steps_text<DELTA>(r, rtot, sdig[i], 0, (uint32_t)(p - start), pmode, E.rules.rpre);
+}
+
 template <int BLOCK, int ITEMS, int DELTA>
-__global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ tile_off,
-                                                      char *__restrict__ text) {
+__global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ soff,
+                                                      const uint8_t *__restrict__ sdig, char *__restrict__ text) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
-  __shared__ __align__(16) char sbuf[kTextBuf + 32];
+  constexpr uint32_t kWords = kTextBuf / 4 + 8;
+  __shared__ __align__(16) uint32_t sbuf[kWords];
   __shared__ SymStage S;
+  __shared__ unsigned long long s_t0, s_t1;
   const uint64_t tile = blockIdx.x;
+  const bool pmode = T.meta.mode == 0;
   stage_symbols<BLOCK>(E, tile, S);
-  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  const uint64_t P0 = tile * TILE;
+  if (threadIdx.x == 0) {
+    // text range of the tile: [offset of its first step, offset of the next tile's)
+    const uint64_t i0 = E.tile_sym[tile];
+    const int4 r0 = E.rec[i0];
+    s_t0 = step_offset<DELTA>(E, T, soff, sdig, i0, r0, E.pos[i0], P0, pmode);
+    const uint64_t P1 = P0 + TILE;
+    if (P1 >= E.total) {
+      s_t1 = soff[E.m];
+    } else {
+      const uint64_t i1 = E.tile_sym[tile + 1];
+      const int4 r1 = E.rec[i1];
+      s_t1 = step_offset<DELTA>(E, T, soff, sdig, i1, r1, E.pos[i1], P1, pmode);
+    }
+  }
+  const uint64_t p0 = P0 + (uint64_t)threadIdx.x * ITEMS;
   int32_t val[ITEMS];
   const uint32_t cnt = thread_values<ITEMS, DELTA>(E, S, tile, p0, val);
-  uint32_t hd;
-  const unsigned long long mine = thread_text_len<ITEMS>(val, cnt, p0, T, hd);
-  unsigned long long total;
-  const unsigned long long ex = block_excl_sum<BLOCK>(mine, total);
-  const uint64_t toff = tile_off[tile];
-  const bool staged = total <= kTextBuf;
-  char *dst = staged ? sbuf + ex : text + toff + ex;
-  const bool pmode = T.meta.mode == 0;
-  uint32_t o = 0;
-#pragma unroll
+  // my first symbol again, for my text offset and the shared digit counts
+  uint64_t i = 0, start = 0, end = 0;
+  int4 r = make_int4(0, 0, 0, 0);
+  unsigned long long my = 0;
+  if (cnt) {
+    if (S.staged) {
+      uint32_t lo = 0, hi = S.cnt - 1;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (S.pos[mid] <= p0) lo = mid; else hi = mid - 1;
+      }
+      i = S.lo + lo;
+      start = S.pos[lo];
+      end = S.pos[lo + 1];
+      r = S.rec[lo];
+    } else {
+      uint64_t lo = E.tile_sym[tile], hi = E.tile_sym[tile + 1];
+      while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) >> 1;
+        if (E.pos[mid] <= p0) lo = mid; else hi = mid - 1;
+      }
+      i = lo;
+      start = E.pos[lo];
+      end = E.pos[lo + 1];
+      r = E.rec[lo];
+    }
+    my = step_offset<DELTA>(E, T, soff, sdig, i, r, start, p0, pmode);
+  }
+  __syncthreads();
+  const unsigned long long t0 = s_t0, total = s_t1 - s_t0;
+  const uint32_t hd = cnt ? (uint32_t)((((unsigned long long)T.heads[(p0 >> 5) + 1] << 32) | T.heads[p0 >> 5]) >> (p0 & 31)) : 0u;
+  if (total <= kTextBuf) {
+    const uint32_t nw = (uint32_t)(total / 4) + 2;
+    for (uint32_t k = threadIdx.x; k < nw; k += BLOCK) sbuf[k] = 0;
+    __syncthreads();
+    WordWriter wr;
+    wr.init(sbuf, cnt ? (uint32_t)(my - t0) : 0u, nw);
+    uint32_t dig = sdig[i];
+#pragma unroll 1  // a rolled loop keeps the kernel inside the instruction cache
+    for (int k = 0; k < ITEMS; ++k) {
+      if ((uint32_t)k < cnt) {
+        const uint64_t p = p0 + k;
+        if (p >= end) {  // next symbol
+          ++i;
+          end = E.pos[i + 1];
+          dig = sdig[i];
+        }
+        const bool fst = (hd >> k) & 1u, lst = (hd >> (k + 1)) & 1u;
+        uint64_t t = 0;
+        if (fst | lst) t = trav_of(T.off, T.ntrav, p);
+        if (fst)
+          for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) wr.put((uint8_t)T.meta.blob[q], 1);
+        const int32_t v = val[k];
+        const uint32_t av = abs32(v), nd = dig ? dig : dec_digits(av);
+        if (pmode) {
+          wr.put_dec(av, nd);
+          const uint32_t mark = v < 0 ? '-' : '+';
+          if (lst) wr.put(mark, 1);
+          else wr.put(mark | ((uint32_t)',' << 8), 2);
+        } else {
+          wr.put(v < 0 ? '<' : '>', 1);
+          wr.put_dec(av, nd);
+        }
+        if (lst)
+          for (uint64_t q = T.meta.suf_off[t]; q < T.meta.suf_off[t + 1]; ++q) wr.put((uint8_t)T.meta.blob[q], 1);
+      }
+    }
+    wr.finish();
+    if (wr.overflow) atomicOr(T.err, kErrLength);
+    __syncthreads();
+    if (t0 + total <= T.cap) block_copy_out<BLOCK>(reinterpret_cast<const char *>(sbuf), (uint32_t)total, text + t0);
+    else if (threadIdx.x == 0) atomicOr(T.err, kErrLength);
+    return;
+  }
+  // a tile with very long line pieces: bytes straight to global memory
+  // (each thread's bytes end where the next thread's begin)
+  unsigned long long o = my;
+  char dec[10];
+  auto put = [&](char c) {
+    if (o < T.cap) text[o] = c;
+    else atomicOr(T.err, kErrLength);
+    ++o;
+  };
+#pragma unroll 1
   for (int k = 0; k < ITEMS; ++k) {
     if ((uint32_t)k < cnt) {
       const bool fst = (hd >> k) & 1u, lst = (hd >> (k + 1)) & 1u;
       uint64_t t = 0;
       if (fst | lst) t = trav_of(T.off, T.ntrav, p0 + k);
       if (fst)
-        for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) dst[o++] = T.meta.blob[q];
+        for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) put(T.meta.blob[q]);
       const int32_t v = val[k];
       const uint32_t av = abs32(v), nd = dec_digits(av);
+      put_dec(dec, av, nd);
+      if (!pmode) put(v < 0 ? '<' : '>');
+      for (uint32_t q = 0; q < nd; ++q) put(dec[q]);
       if (pmode) {
-        put_dec(dst + o, av, nd);
-        o += nd;
-        dst[o++] = v < 0 ? '-' : '+';
-        if (!lst) dst[o++] = ',';
-      } else {
-        dst[o++] = v < 0 ? '<' : '>';
-        put_dec(dst + o, av, nd);
-        o += nd;
+        put(v < 0 ? '-' : '+');
+        if (!lst) put(',');
       }
       if (lst)
-        for (uint64_t q = T.meta.suf_off[t]; q < T.meta.suf_off[t + 1]; ++q) dst[o++] = T.meta.blob[q];
+        for (uint64_t q = T.meta.suf_off[t]; q < T.meta.suf_off[t + 1]; ++q) put(T.meta.blob[q]);
     }
-  }
-  if (staged) {
-    __syncthreads();
-    block_copy_out<BLOCK>(sbuf, (uint32_t)total, text + toff);
   }
 }
 
@@ -431,10 +562,11 @@ uint64_t excl_scan_tiles(uint64_t n) {
 }
 
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
-                             uint32_t *built, uint32_t pass, DevStatus *status, cudaStream_t st) {
+                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status,
+                             cudaStream_t st) {
   if (!rv.nrules) return;
-  k_rule_prefix_pass<<<grid_for(rv.nrules, kBlock, 152u * 32u), kBlock, 0, st>>>(first, second, rv, rpre, built, pass,
-                                                                                 status);
+  k_rule_prefix_pass<<<grid_for(rv.nrules, kBlock, 152u * 32u), kBlock, 0, st>>>(first, second, rv, rpre, rstat,
+                                                                                 delta, built, pass, status);
 }
 
 void launch_excl_scan_u32(const uint32_t *in, uint64_t n, uint64_t *out, unsigned long long *desc,
@@ -475,23 +607,23 @@ void launch_expand_steps(const ExpandSource &E, int delta, int32_t *out, cudaStr
     k_expand_steps<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, out);
 }
 
-void launch_text_lengths(const ExpandSource &E, const TextSource &T, int delta, uint64_t *tile_len, cudaStream_t st) {
-  const uint64_t nt = expand_num_tiles(E.total);
-  if (!nt) return;
+void launch_symbol_text(const ExpandSource &E, const TextSource &T, int delta, uint64_t *slen, uint8_t *sdig,
+                        cudaStream_t st) {
+  if (!E.m) return;
   if (delta)
-    k_text_lengths<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, tile_len);
+    k_symbol_text<1><<<grid_for(E.m, kBlock), kBlock, 0, st>>>(E, T, slen, sdig);
   else
-    k_text_lengths<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, tile_len);
+    k_symbol_text<0><<<grid_for(E.m, kBlock), kBlock, 0, st>>>(E, T, slen, sdig);
 }
 
-void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *tile_off, char *text,
-                       cudaStream_t st) {
+void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
+                       const uint8_t *sdig, char *text, cudaStream_t st) {
   const uint64_t nt = expand_num_tiles(E.total);
   if (!nt) return;
   if (delta)
-    k_text_write<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, tile_off, text);
+    k_text_write<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, soff, sdig, text);
   else
-    k_text_write<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, tile_off, text);
+    k_text_write<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, soff, sdig, text);
 }
 
 }  // namespace gfz

@@ -142,10 +142,14 @@ void launch_gather_ranges(const int32_t *src, const uint64_t *starts, const uint
 // ---- prefix-sum expansion decoder (expand_kernels.cu) ----------------------
 // Rule r (id min_id + r) expands to rlen[r] steps whose inclusive prefix
 // sums are rpre[roff[r] .. roff[r] + rlen[r]).
+// rstat[r] = value ranges of the rule's expansion for text lengths: with
+// delta_round 1 {min, max} of its prefix values and {min, max} of 0 and all
+// prefix values but the last; with delta_round 0 {min, max} of its steps.
 struct RulePrefixView {
   const uint32_t *rlen;
   const uint64_t *roff;  // nrules + 1
   const int32_t *rpre;
+  const int4 *rstat;
   uint32_t min_id;
   uint64_t nrules;
 };
@@ -167,11 +171,14 @@ struct TextSource {
   uint64_t ntrav;
   const uint32_t *heads;
   TextMeta meta;
+  uint64_t cap;   // bytes of the text buffer
+  uint32_t *err;  // kErrLength when the text would not fit where its lengths say
 };
 // One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
 // waiting, zero before pass 1).  status->u64[6] += rules still waiting.
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
-                             uint32_t *built, uint32_t pass, DevStatus *status, cudaStream_t st);
+                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status,
+                             cudaStream_t st);
 // out[0 .. n] = exclusive scan of in[0 .. n) (out[n] = total); desc: one u64
 // per excl_scan_tiles(n) tile (at least one), zeroed; tile_counter zeroed.
 uint64_t excl_scan_tiles(uint64_t n);
@@ -191,9 +198,12 @@ uint64_t expand_num_tiles(uint64_t total);
 void launch_tile_symbols(const uint64_t *pos, uint64_t m, uint64_t total, uint64_t *tile_sym, cudaStream_t st);
 // Decoded steps (delta = delta_round, 0 or 1) of every output position.
 void launch_expand_steps(const ExpandSource &E, int delta, int32_t *out, cudaStream_t st);
-// P/W text: bytes per output tile, then the text of each tile at tile_off.
-void launch_text_lengths(const ExpandSource &E, const TextSource &T, int delta, uint64_t *tile_len, cudaStream_t st);
-void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *tile_off, char *text,
-                       cudaStream_t st);
+// P/W text: slen[i] = text bytes of symbol i (with the line pieces around
+// it) and sdig[i] = the digit count all its steps share (0: they differ);
+// then, with soff = exclusive scan of slen, the text of every output tile.
+void launch_symbol_text(const ExpandSource &E, const TextSource &T, int delta, uint64_t *slen, uint8_t *sdig,
+                        cudaStream_t st);
+void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
+                       const uint8_t *sdig, char *text, cudaStream_t st);
 
 }  // namespace gfz

@@ -495,17 +495,18 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
     return false;
   }
   g.rpre.resize(std::max<uint64_t>(steps, 1));
+  g.rstat.resize(std::max<uint64_t>(R, 1));
   if (R) {
     DevVec<uint32_t> built(st);
     built.resize(R);
     cuda_check(cudaMemsetAsync(built.ptr, 0, R * sizeof(uint32_t), st), "prefix clear");
-    const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, R};
+    const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, R};
     uint64_t prev_open = UINT64_MAX;
     for (uint32_t pass = 1;; ++pass) {
       ctx.reset_status();
       GFZ_TIMED_B(ctx, "rule_prefix", 0,
-                  launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, built.ptr, pass, ctx.dstatus(),
-                                          st));
+                  launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, g.rstat.ptr,
+                                          g.delta_round == 1 ? 1 : 0, built.ptr, pass, ctx.dstatus(), st));
       const DevStatus &s = ctx.read_status();
       ctx.check_status("rule prefix");
       const uint64_t open = s.u64[6];
@@ -528,7 +529,7 @@ struct ExpandPlan {
   uint64_t m = 0, total = 0;
   ExpandSource source(const Grammar &g) const {
     return ExpandSource{rec.ptr, pos.ptr, tile_sym.ptr, m, total,
-                        RulePrefixView{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, g.nrules}};
+                        RulePrefixView{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, g.nrules}};
   }
 };
 
@@ -561,7 +562,7 @@ static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, E
   ctx.read_status();
   ctx.check_status("expansion offsets");
   P.total = P.h_out_off[nt];
-  const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.layer_start, g.nrules};
+  const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, g.nrules};
   P.rec.resize(m);
   if (g.delta_round == 1) {
     // S_i: segmented (per traversal) exclusive sums of the symbol totals
@@ -737,27 +738,30 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(P.total) * sizeof(uint32_t), st), "head bitmap clear");
   GFZ_TIMED(ctx, "head_bits", launch_head_bits(P.out_off.ptr, nt, heads.ptr, st));
   const TextMeta meta{dp.blob.ptr, dp.pre.ptr, dp.suf.ptr, dp.tail.ptr, (uint64_t)pieces.tail.size(), mode};
-  const TextSource T{P.out_off.ptr, nt, heads.ptr, meta};
+  TextSource T{P.out_off.ptr, nt, heads.ptr, meta, 0, &ctx.dstatus()->err};
   const ExpandSource E = P.source(g);
-  const uint64_t tiles = expand_num_tiles(P.total);
-  DevVec<uint64_t> tile_len(st), tile_off(st);
-  tile_len.resize(tiles);
-  tile_off.resize(tiles + 1);
+  // text bytes per symbol, their offsets, then the text of every output tile
+  DevVec<uint64_t> slen(st), soff(st);
+  DevVec<uint8_t> sdig(st);
+  slen.resize(P.m);
+  soff.resize(P.m + 1);
+  sdig.resize(P.m);
   ctx.reset_status();
-  GFZ_TIMED_B(ctx, "text_lengths", 4.0 * P.total, launch_text_lengths(E, T, g.delta_round, tile_len.ptr, st));
+  GFZ_TIMED_B(ctx, "symbol_text", 24.0 * P.m, launch_symbol_text(E, T, g.delta_round, slen.ptr, sdig.ptr, st));
   uint32_t *counter;
-  unsigned long long *desc = ctx.lookback(excl_scan_tiles(tiles), &counter);
-  GFZ_TIMED(ctx, "text_scan",
-            launch_excl_scan_u64(tile_len.ptr, tiles, tile_off.ptr, desc, counter, ctx.dstatus(), st));
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(P.m), &counter);
+  GFZ_TIMED_B(ctx, "symbol_text", 16.0 * P.m,
+              launch_excl_scan_u64(slen.ptr, P.m, soff.ptr, desc, counter, ctx.dstatus(), st));
   uint64_t body = 0;
-  cuda_check(cudaMemcpyAsync(&body, tile_off.ptr + tiles, sizeof(body), cudaMemcpyDeviceToHost, st), "text size");
+  cuda_check(cudaMemcpyAsync(&body, soff.ptr + P.m, sizeof(body), cudaMemcpyDeviceToHost, st), "text size");
   ctx.read_status();
   ctx.check_status("text lengths");
   const uint64_t size = body + pieces.tail.size();
   text.resize(std::max<uint64_t>(size, 1));
   text.size = size;
+  T.cap = body;
   GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
-              launch_text_write(E, T, g.delta_round, tile_off.ptr, text.ptr, st));
+              launch_text_write(E, T, g.delta_round, soff.ptr, sdig.ptr, text.ptr, st));
   if (!pieces.tail.empty())
     cuda_check(cudaMemcpyAsync(text.ptr + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
                "text tail");

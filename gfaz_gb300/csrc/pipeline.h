@@ -141,7 +141,7 @@ class Context {
 // streams loaded from a container for decompression.
 struct Grammar {
   explicit Grammar(cudaStream_t st)
-      : enc(st), off(st), rules(st), first(st), second(st), rlen(st), roff(st), rpre(st) {}
+      : enc(st), off(st), rules(st), first(st), second(st), rlen(st), roff(st), rpre(st), rstat(st) {}
   DevVec<int32_t> enc;         // encoded traversals back to back
   DevVec<uint64_t> off;        // ntrav + 1 offsets into enc
   std::vector<uint64_t> h_off; // host copy of off
@@ -151,6 +151,7 @@ struct Grammar {
   DevVec<uint32_t> rlen;       // rule expansion lengths (decode side)
   DevVec<uint64_t> roff;       // rule prefix buffer: offsets (nrules + 1)
   DevVec<int32_t> rpre;        // inclusive prefix sums of every rule's expansion
+  DevVec<int4> rstat;          // per-rule value ranges (text lengths)
   uint64_t nrules = 0;
   uint32_t layer_start = 0, next_id = 0;
   int delta_round = 1;

@@ -68,4 +68,81 @@ __device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, c
 
 constexpr uint32_t kTextBuf = 28 * 1024;
 
+// Two decimal characters of x < 100, the first in the low byte.
+__device__ __forceinline__ uint32_t dec_pair(uint32_t x) {
+  const uint32_t t = x / 10u;
+  return ('0' + t) | (('0' + (x - 10u * t)) << 8);
+}
+
+// Writes a byte stream into a zeroed shared word buffer with 32-bit stores.
+// Bytes accumulate in a 64-bit register and leave as whole words; the
+// stream's first word (when it does not start on a word boundary) and its
+// last partial word may be shared with the neighbouring streams and are
+// OR-ed in atomically.
+struct WordWriter {
+  uint32_t *buf;
+  uint32_t w;               // next word to write
+  uint32_t n;               // bytes pending in acc (< 4 between calls)
+  uint32_t limit;           // words in buf; words beyond are dropped
+  unsigned long long acc;
+  bool shared_first;
+  bool overflow;            // a word fell outside buf
+  __device__ __forceinline__ void init(uint32_t *b, uint32_t byte_off, uint32_t words) {
+    buf = b;
+    w = byte_off >> 2;
+    n = byte_off & 3u;
+    limit = words;
+    acc = 0;
+    shared_first = n != 0;
+    overflow = false;
+  }
+  __device__ __forceinline__ void store(uint32_t word, bool shared) {
+    if (w >= limit) {
+      overflow = true;
+      return;
+    }
+    if (shared) atomicOr(&buf[w], word);
+    else buf[w] = word;
+  }
+  // Appends the low cnt (<= 4) bytes of x (bytes above cnt must be zero).
+  __device__ __forceinline__ void put(uint32_t x, uint32_t cnt) {
+    acc |= (unsigned long long)x << (8u * n);
+    n += cnt;
+    if (n >= 4) {
+      store((uint32_t)acc, shared_first);
+      shared_first = false;
+      ++w;
+      acc >>= 32;
+      n -= 4;
+    }
+  }
+  // Appends the decimal digits of v (nd = dec_digits(v)), most significant first.
+  __device__ __forceinline__ void put_dec(uint32_t v, uint32_t nd) {
+    uint32_t lo = v;
+    if (nd > 8) {
+      const uint32_t hi = v / 100000000u;
+      lo = v - hi * 100000000u;
+      const uint32_t ph = dec_pair(hi);
+      if (nd == 9) put(ph >> 8, 1);
+      else put(ph, 2);
+    }
+    const uint32_t a = lo / 10000u, b = lo - a * 10000u;
+    const uint32_t a1 = a / 100u, b1 = b / 100u;
+    unsigned long long c8 = (unsigned long long)dec_pair(a1) | ((unsigned long long)dec_pair(a - 100u * a1) << 16) |
+                            ((unsigned long long)dec_pair(b1) << 32) |
+                            ((unsigned long long)dec_pair(b - 100u * b1) << 48);
+    const uint32_t k = nd > 8 ? 8u : nd;  // digits of lo to write
+    c8 >>= 8u * (8u - k);
+    if (k > 4) {
+      put((uint32_t)c8, 4);
+      put((uint32_t)(c8 >> 32), k - 4);
+    } else {
+      put((uint32_t)c8, k);
+    }
+  }
+  __device__ __forceinline__ void finish() {
+    if (n && acc) store((uint32_t)acc, true);
+  }
+};
+
 }  // namespace gfz
