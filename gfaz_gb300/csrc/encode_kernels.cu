@@ -348,149 +348,239 @@ __global__ void k_tile_trav(const uint64_t *__restrict__ off, uint64_t ntrav, ui
     tile_trav[k] = lower_bound_u64(off, ntrav, k * (uint64_t)tile);
 }
 
-// Greedy replacement, one tile per block.  The tile index is claimed when
-// the block starts (so every tile a look-back waits on belongs to a block
-// that is already running and publishes its aggregate as soon as its
-// lookups are done; claiming further ahead would make later tiles wait on
-// tiles whose blocks are still busy elsewhere), then the tile and its head
-// bits arrive by bulk copy.
-//
-// Thread t owns positions j0 = t * ITEMS .. j0 + ITEMS - 1.  It looks up the
-// pairs starting there (one 16-byte slot load each, all issued together),
-// keeps the candidate bits, slots and steps in registers, takes part in the
-// block scan and the decoupled look-back of the run-parity recurrence, then
-// scatters its kept symbols into a shared staging buffer aligned like the
-// output, which the block writes out as 16-byte vectors.
-template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, uint64_t n,
-                                                 const uint32_t *__restrict__ heads, uint64_t head_words,
-                                                 const uint64_t *__restrict__ off, uint64_t ntrav,
-                                                 const uint64_t *__restrict__ tile_trav, PairTable tab,
-                                                 int32_t temp_base, int32_t *__restrict__ out,
-                                                 uint64_t *__restrict__ new_off, unsigned long long *desc,
-                                                 uint32_t *tile_counter, DevStatus *status) {
-  constexpr uint32_t TILE = BLOCK * ITEMS;
-  constexpr int NW = BLOCK / 32;
-  static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
-  static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
-  __shared__ __align__(128) TilePipe<TILE> P;  // stage 0 only
-  __shared__ __align__(16) int32_t so[TILE + 4];
-  __shared__ __align__(16) uint16_t lidx[TILE];  // output index (in the tile) of each kept position
-  __shared__ ParAgg s_warp[NW];
-  __shared__ uint32_t s_in_x;
-  __shared__ unsigned long long s_in_c;
-  __shared__ uint32_t s_tile;
-  __shared__ uint64_t s_tlo;
+// Greedy replacement in three passes, so that no tile waits on another:
+//  classify: per tile, the candidate bits of its positions (one byte per
+//            thread) and the tile's run-parity aggregate;
+//  states:   exclusive scan of the tile aggregates into the carried-in state
+//            (x, replaced count) of every tile;
+//  emit:     per tile, the replay of the recurrence from its carried-in
+//            state, a second lookup of the positions it replaces, and the
+//            compacted output.
+// Thread t owns positions j0 = t * ITEMS .. j0 + ITEMS - 1 of a tile.
 
-  if (threadIdx.x == 0) {
-    mbar_init(&P.bar[0], 1);
-    mbar_init_fence();
-    s_tile = atomicAdd(tile_counter, 1u);
-  }
-  __syncthreads();
-  const uint64_t tile = s_tile;
-  uint32_t phases = 0;
-  const bool bulk = pipe_issue<BLOCK, TILE>(P, 0, tile, s, n, heads, head_words);
-  if (threadIdx.x == 0) s_tlo = tile_trav[tile];
+// Lookup of the pairs at positions j0 + k (k < ITEMS) with bit k of `want`
+// set: canonical key, slot (table index) and flag word; misses flag
+// kErrLookupMiss.  All first probes are issued before any is resolved.
+template <int ITEMS>
+__device__ __forceinline__ void lookup_pairs(const int32_t (&v)[ITEMS + 1], uint32_t want, const PairTable &tab,
+                                             uint32_t (&slot)[ITEMS], uint32_t (&fl)[ITEMS], uint32_t &fwdb,
+                                             DevStatus *status) {
   const uint32_t mask = (uint32_t)(tab.cap - 1);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t j0 = threadIdx.x * ITEMS;
-  {
-    const int b = 0;
-    if (!pipe_wait<TILE>(P, b, bulk, phases)) {
-      if (threadIdx.x == 0) atomicOr(&status->err, kErrTimeout);
-      return;
-    }
-    const int32_t *sv = P.sv[b];
-    const uint32_t *hb = P.hb[b];
-    const uint64_t base = tile * TILE;
-    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
-
-    // ---- lookups: candidate (repeated) and already-used bits per position
-    int32_t v[ITEMS + 1];
-    thread_steps<ITEMS>(sv, j0, v);
-    const uint32_t hd = bits_from(hb, j0);
-    unsigned long long key[ITEMS];
-    uint32_t slot[ITEMS];
-    uint32_t fwdb = 0, validb = 0;
+  unsigned long long key[ITEMS], cur[ITEMS];
+  fwdb = 0;
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const bool valid = j0 + k < len && !((hd >> (k + 1)) & 1u);
+  for (int k = 0; k < ITEMS; ++k) {
+    key[k] = 0;
+    cur[k] = 0;
+    slot[k] = 0;
+    fl[k] = 0;
+    if ((want >> k) & 1u) {
       const unsigned long long f = pack2(v[k], v[k + 1]);
       const unsigned long long r = pack2(neg32(v[k + 1]), neg32(v[k]));
       const bool fw = key_le(f, r);
       key[k] = fw ? f : r;
       fwdb |= (uint32_t)fw << k;
-      validb |= (uint32_t)valid << k;
       slot[k] = hash_pair(key[k]) & mask;
+      load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
     }
-    uint32_t cbits = 0, ubits = 0;
-    {
-      unsigned long long cur[ITEMS];
-      uint32_t fl[ITEMS];
+  }
 #pragma unroll
-      for (int k = 0; k < ITEMS; ++k) {
-        cur[k] = key[k];
+  for (int k = 0; k < ITEMS; ++k) {
+    uint32_t p = 0;
+    while (cur[k] != key[k]) {
+      if (cur[k] == kEmptyKey || ++p >= kMaxProbe) {
+        atomicOr(&status->err, kErrLookupMiss);
         fl[k] = 0;
-        if ((validb >> k) & 1u) load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
+        break;
       }
-#pragma unroll
-      for (int k = 0; k < ITEMS; ++k) {
-        uint32_t p = 0;
-        while (cur[k] != key[k]) {
-          if (cur[k] == kEmptyKey || ++p >= kMaxProbe) {
-            atomicOr(&status->err, kErrLookupMiss);
-            fl[k] = 0;
-            break;
-          }
-          slot[k] = (slot[k] + 1) & mask;
-          load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
-        }
-        cbits |= (uint32_t)((fl[k] & kFlagRepeated) != 0) << k;
-        ubits |= (uint32_t)((fl[k] & kFlagUsed) != 0) << k;
-      }
+      slot[k] = (slot[k] + 1) & mask;
+      load_slot(&tab.slots[slot[k]], cur[k], fl[k]);
     }
+  }
+}
 
-    // ---- run-parity recurrence: thread aggregate, block scan, look-back
-    ParAgg a;
-    {
-      uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
+__device__ __forceinline__ ParAgg par_of_bits(uint32_t cbits, int items) {
+  uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
+  for (int k = 0; k < items; ++k) {
+    const uint32_t c = (cbits >> k) & 1u;
+    x0 = c & (x0 ^ 1u);
+    x1 = c & (x1 ^ 1u);
+    c0 += x0;
+    c1 += x1;
+  }
+  return ParAgg{x0 | (x1 << 1), c0, c1};
+}
+
+// Block-wide exclusive composition of the per-thread aggregates: returns
+// this thread's exclusive prefix and, in total, the whole tile's aggregate.
+template <int BLOCK>
+__device__ __forceinline__ ParAgg block_par_scan(const ParAgg &a, ParAgg &total, ParAgg *s_warp) {
+  constexpr int NW = BLOCK / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ParAgg inc = a;
 #pragma unroll
-      for (int k = 0; k < ITEMS; ++k) {
-        const uint32_t c = (cbits >> k) & 1u;
-        x0 = c & (x0 ^ 1u);
-        x1 = c & (x1 ^ 1u);
-        c0 += x0;
-        c1 += x1;
-      }
-      a = ParAgg{x0 | (x1 << 1), c0, c1};
-    }
-    ParAgg inc = a;
+  for (int d = 1; d < 32; d <<= 1) {
+    const ParAgg o = par_shfl_up(inc, d);
+    if (lane >= d) inc = par_compose(o, inc);
+  }
+  ParAgg excl = par_shfl_up(inc, 1);
+  if (lane == 0) excl = par_identity();
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  ParAgg wpre = par_identity(), tot = par_identity();
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      ParAgg o = par_shfl_up(inc, d);
-      if (lane >= d) inc = par_compose(o, inc);
+  for (int w = 0; w < NW; ++w) {
+    if (w == warp) wpre = tot;
+    tot = par_compose(tot, s_warp[w]);
+  }
+  total = tot;
+  return par_compose(wpre, excl);
+}
+
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK, 4) k_apply_classify(const int32_t *__restrict__ s, uint64_t n,
+                                                             const uint32_t *__restrict__ heads, uint64_t head_words,
+                                                             PairTable tab, uint32_t *__restrict__ tword,
+                                                             unsigned long long *__restrict__ tile_agg,
+                                                             DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(ITEMS == 8 && TILE <= 2048, "a thread word holds 8 candidate bits and 11-bit counts");
+  __shared__ __align__(128) TilePipe<TILE> P;
+  __shared__ ParAgg s_warp[BLOCK / 32];
+  const uint64_t ntiles = (n + TILE - 1) / TILE;
+  uint64_t tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&P.bar[0], 1);
+    mbar_init(&P.bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  uint32_t phases = 0;
+  bool bulk_cur = pipe_issue<BLOCK, TILE>(P, 0, tile, s, n, heads, head_words);
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  for (int b = 0;; b ^= 1) {
+    const uint64_t next = tile + gridDim.x;
+    const bool has_next = next < ntiles;
+    const bool bulk_next = has_next && pipe_issue<BLOCK, TILE>(P, b ^ 1, next, s, n, heads, head_words);
+    if (!pipe_wait<TILE>(P, b, bulk_cur, phases)) {
+      if (threadIdx.x == 0) atomicOr(&status->err, kErrTimeout);
+      if (bulk_next) mbar_wait(&P.bar[b ^ 1], (phases >> (b ^ 1)) & 1u);
+      return;
     }
-    ParAgg excl = par_shfl_up(inc, 1);
-    if (lane == 0) excl = par_identity();
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    ParAgg wpre = par_identity(), total = par_identity();
-    for (int w = 0; w < NW; ++w) {
-      if (w == warp) wpre = total;
-      total = par_compose(total, s_warp[w]);
+    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - tile * TILE);
+    int32_t v[ITEMS + 1];
+    thread_steps<ITEMS>(P.sv[b], j0, v);
+    const uint32_t hd = bits_from(P.hb[b], j0);
+    uint32_t validb = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) validb |= (uint32_t)(j0 + k < len && !((hd >> (k + 1)) & 1u)) << k;
+    uint32_t slot[ITEMS], fl[ITEMS], fwdb;
+    lookup_pairs<ITEMS>(v, validb, tab, slot, fl, fwdb, status);
+    uint32_t cbits = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) cbits |= (uint32_t)(((validb >> k) & 1u) && (fl[k] & kFlagRepeated)) << k;
+    ParAgg total;
+    const ParAgg excl = block_par_scan<BLOCK>(par_of_bits(cbits, ITEMS), total, s_warp);
+    // my candidate bits and my exclusive prefix inside the tile (counts < 2048)
+    tword[tile * BLOCK + threadIdx.x] = cbits | ((excl.xo & 3u) << 8) | (excl.c0 << 10) | (excl.c1 << 21);
+    if (threadIdx.x == 0) tile_agg[tile] = par_encode(total);
+    pipe_release();
+    if (!has_next) break;
+    tile = next;
+    bulk_cur = bulk_next;
+  }
+}
+
+// state[t] = the state (x, replaced count) before tile t, encoded x | c << 1.
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_tile_states(const unsigned long long *__restrict__ tile_agg,
+                                                       uint64_t ntiles, unsigned long long *__restrict__ state,
+                                                       unsigned long long *desc, uint32_t *tile_counter,
+                                                       DevStatus *status) {
+  __shared__ ParAgg s_warp[BLOCK / 32];
+  __shared__ uint32_t s_x;
+  __shared__ unsigned long long s_c;
+  const uint32_t blk = claim_tile(tile_counter);
+  const uint64_t i0 = ((uint64_t)blk * BLOCK + threadIdx.x) * ITEMS;
+  ParAgg agg[ITEMS];
+  ParAgg mine = par_identity();
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    agg[k] = i0 + k < ntiles ? par_decode(tile_agg[i0 + k]) : par_identity();
+    mine = par_compose(mine, agg[k]);
+  }
+  ParAgg total;
+  const ParAgg excl = block_par_scan<BLOCK>(mine, total, s_warp);
+  if (threadIdx.x < 32) {
+    const ParState in = warp_lookback<ParOp>(desc, blk, total, &status->err);
+    if (threadIdx.x == 0) {
+      s_x = in.x;
+      s_c = in.c;
     }
-    excl = par_compose(wpre, excl);
-    if (warp == 0) {
-      const ParState in = warp_lookback<ParOp>(desc, tile, total, &status->err);
-      if (lane == 0) {
-        s_in_x = in.x;
-        s_in_c = in.c;
-      }
+  }
+  __syncthreads();
+  ParState st = ParOp::apply(excl, ParState{s_x, s_c});
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    if (i0 + k < ntiles) state[i0 + k] = ParOp::encode_incl(st);
+    st = ParOp::apply(agg[k], st);
+  }
+}
+
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restrict__ s, uint64_t n,
+                                                      const uint32_t *__restrict__ heads, uint64_t head_words,
+                                                      const uint32_t *__restrict__ tword,
+                                                      const unsigned long long *__restrict__ tile_agg,
+                                                      const unsigned long long *__restrict__ state,
+                                                      const uint64_t *__restrict__ off, uint64_t ntrav,
+                                                      const uint64_t *__restrict__ tile_trav, PairTable tab,
+                                                      int32_t temp_base, int32_t *__restrict__ out,
+                                                      uint64_t *__restrict__ new_off, DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
+  static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
+  __shared__ __align__(128) TilePipe<TILE> P;
+  __shared__ __align__(16) int32_t so[TILE + 4];
+  __shared__ __align__(16) uint16_t lidx[TILE];  // output index (in the tile) of each kept position
+  __shared__ uint64_t s_tlo;
+  const uint64_t ntiles = (n + TILE - 1) / TILE;
+  uint64_t tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&P.bar[0], 1);
+    mbar_init(&P.bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  uint32_t phases = 0;
+  bool bulk_cur = pipe_issue<BLOCK, TILE>(P, 0, tile, s, n, heads, head_words);
+  uint32_t tw_cur = tword[tile * BLOCK + threadIdx.x];
+  unsigned long long st_cur = state[tile], ag_cur = tile_agg[tile];
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  for (int b = 0;; b ^= 1) {
+    const uint64_t next = tile + gridDim.x;
+    const bool has_next = next < ntiles;
+    const bool bulk_next = has_next && pipe_issue<BLOCK, TILE>(P, b ^ 1, next, s, n, heads, head_words);
+    // the next tile's thread words, aggregate and carried-in state, in flight meanwhile
+    const uint32_t tw_next = has_next ? tword[next * BLOCK + threadIdx.x] : 0u;
+    const unsigned long long st_next = has_next ? state[next] : 0ull;
+    const unsigned long long ag_next = has_next ? tile_agg[next] : 0ull;
+    if (threadIdx.x == 0) s_tlo = tile_trav[tile];
+    if (!pipe_wait<TILE>(P, b, bulk_cur, phases)) {
+      if (threadIdx.x == 0) atomicOr(&status->err, kErrTimeout);
+      if (bulk_next) mbar_wait(&P.bar[b ^ 1], (phases >> (b ^ 1)) & 1u);
+      return;
     }
-    __syncthreads();
-    const uint32_t in_x = s_in_x;
-    const unsigned long long in_c = s_in_c;
+    const int32_t *sv = P.sv[b];
+    const uint64_t base = tile * TILE;
+    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
+    const uint32_t cbits = tw_cur & 0xFFu;
+    const ParAgg excl{(tw_cur >> 8) & 3u, (tw_cur >> 10) & 0x7FFu, tw_cur >> 21};
+    const ParAgg total = par_decode(ag_cur);
+    const uint32_t in_x = (uint32_t)(st_cur & 1u);
+    const unsigned long long in_c = st_cur >> 1;
     // replay from the carried-in state: kept (not consumed) and replaced bits
     const uint32_t x_init = par_x(excl, in_x);
     const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
@@ -507,15 +597,19 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
         }
       }
     }
+    // the rules of the replaced positions
+    int32_t v[ITEMS + 1];
+    thread_steps<ITEMS>(sv, j0, v);
+    uint32_t slot[ITEMS], fl[ITEMS], fwdb;
+    lookup_pairs<ITEMS>(v, xbits, tab, slot, fl, fwdb, status);
     // kept positions of the tile before j0: j0 minus the consumed ones (the
     // carried-in position and the partner of every replaced position before
     // j0, except a replaced j0 - 1 whose partner is j0 itself)
     const uint32_t kept_base = j0 - in_x - c_init + x_init;
     const uint64_t out_base = base - in_c + in_x;
     const uint32_t shift = (uint32_t)(((reinterpret_cast<uintptr_t>(out) >> 2) + out_base) & 3u);
-
-    // ---- scatter kept symbols; record output indices
     uint32_t lpk[ITEMS / 2];
+    uint32_t need = 0;
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
       const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
@@ -524,6 +618,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
         if ((xbits >> k) & 1u) {
           const int32_t sym = temp_base + (int32_t)slot[k];
           val = ((fwdb >> k) & 1u) ? sym : neg32(sym);
+          if (!(fl[k] & kFlagUsed)) need |= 1u << k;
         }
         so[shift + lo] = val;
       }
@@ -533,22 +628,21 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
     *reinterpret_cast<uint4 *>(&lidx[j0]) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
     // rules chosen here whose slot was not yet flagged used: one flag update
     // per distinct slot per warp (frequent pairs hit one slot from every lane)
-    const uint32_t need = xbits & ~ubits;
+    if (__any_sync(0xffffffffu, need != 0)) {
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const bool nk = (need >> k) & 1u;
-      if (__any_sync(0xffffffffu, nk)) {
-        const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
-        if (nk && (peers & lanemask_lt()) == 0) atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+      for (int k = 0; k < ITEMS; ++k) {
+        const bool nk = (need >> k) & 1u;
+        if (__any_sync(0xffffffffu, nk)) {
+          const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
+          if (nk && (peers & lanemask_lt()) == 0) atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+        }
       }
     }
     __syncthreads();
-
-    // ---- write out: positions consumed inside the tile are the carried-in
-    // one (in_x) plus the partner of every replaced position except a
-    // replaced last position, whose partner opens the next tile (x_out)
-    const uint32_t tile_rep = par_c(total, in_x);
-    const uint32_t kept = len - in_x - tile_rep + par_x(total, in_x);
+    // positions consumed inside the tile: the carried-in one (in_x) plus the
+    // partner of every replaced position except a replaced last position,
+    // whose partner opens the next tile (x_out)
+    const uint32_t kept = len - in_x - par_c(total, in_x) + par_x(total, in_x);
     stage_out_phased<BLOCK>(out + out_base, so, shift, kept);
     const bool last_tile = base + len == n;
     for (uint64_t t = s_tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
@@ -558,6 +652,13 @@ __global__ void __launch_bounds__(BLOCK) k_apply(const int32_t *__restrict__ s, 
       else break;
     }
     if (last_tile && threadIdx.x == 0) status->u64[2] = out_base + kept;
+    pipe_release();
+    if (!has_next) break;
+    tile = next;
+    bulk_cur = bulk_next;
+    tw_cur = tw_next;
+    st_cur = st_next;
+    ag_cur = ag_next;
   }
 }
 
@@ -887,14 +988,35 @@ void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t 
   k_tile_trav<<<grid_for(tiles, kBlock), kBlock, 0, st>>>(off, ntrav, tiles, kBlock * kApplyItems, tile_trav);
 }
 
-void launch_apply(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
-                  const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                  unsigned long long *desc, uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
-  if (!n) return;
+constexpr int kStateItems = 16;
+uint64_t apply_state_blocks(uint64_t n) {
   const uint64_t tiles = apply_num_tiles(n);
-  k_apply<kBlock, kApplyItems><<<(unsigned)tiles, kBlock, 0, st>>>(s, n, heads, head_words(n), off, ntrav, tile_trav,
-                                                                   tab, temp_base, out, new_off, desc, tile_counter,
-                                                                   status);
+  constexpr uint64_t PER = kBlock * kStateItems;
+  return (tiles + PER - 1) / PER;
+}
+
+void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
+                           DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  auto k = k_apply_classify<kBlock, kApplyItems>;
+  k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), tab, w.tword,
+                                                                       w.tile_agg, status);
+}
+
+void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  k_tile_states<kBlock, kStateItems><<<(unsigned)apply_state_blocks(n), kBlock, 0, st>>>(
+      w.tile_agg, apply_num_tiles(n), w.state, w.desc, w.counter, status);
+}
+
+void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
+                       const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
+                       const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+  if (!n) return;
+  auto k = k_apply_emit<kBlock, kApplyItems>;
+  k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), w.tword,
+                                                                       w.tile_agg, w.state, off, ntrav, tile_trav,
+                                                                       tab, temp_base, out, new_off, status);
 }
 
 void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,

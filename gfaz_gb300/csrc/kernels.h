@@ -51,12 +51,25 @@ void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, Pai
 // Greedy left-to-right replacement of candidate pairs; writes the compacted
 // stream with temporary symbols +-(temp_base + slot), the new traversal
 // offsets (ntrav + 1 entries) and status->u64[2] = output length.
-// heads: the stream's head bitmap; tile_trav: launch_tile_trav's table;
-// desc: one u64 per tile (apply_num_tiles), zeroed; tile_counter zeroed.
-void launch_apply(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
-                  const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                  unsigned long long *desc, uint32_t *tile_counter, DevStatus *status, cudaStream_t st);
+// heads: the stream's head bitmap; tile_trav: launch_tile_trav's table.
+// Scratch: tword (apply_num_tiles(n) * 256 thread words: candidate bits and
+// in-tile prefix), tile_agg and state (one u64 per tile), desc (one u64 per
+// apply_state_blocks(n) block, zeroed) and a zeroed counter.
+struct ApplyScratch {
+  uint32_t *tword;
+  unsigned long long *tile_agg, *state, *desc;
+  uint32_t *counter;
+};
+// The three passes: candidate bits and tile aggregates; carried-in state
+// of every tile; replay and compacted output.
+void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
+                           DevStatus *status, cudaStream_t st);
+void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
+                       const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
+                       const ApplyScratch &w, DevStatus *status, cudaStream_t st);
 uint64_t apply_num_tiles(uint64_t n);
+uint64_t apply_state_blocks(uint64_t n);
 // tile_trav[k] = first traversal t with off[t] >= k * (apply tile), for the
 // apply_num_tiles(n) tiles.
 void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st);

@@ -268,6 +268,8 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
   DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st);
   DevVec<uint64_t> tile_trav(st);
+  DevVec<uint32_t> tword(st);
+  DevVec<unsigned long long> tile_agg(st), tile_state(st);
 
   uint64_t n = N;
   uint64_t prev_distinct = 0;
@@ -307,13 +309,21 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
       throw std::overflow_error("Compression workflow error: rule id space exhausted");
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
+    const uint64_t tiles = apply_num_tiles(n);
     uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(apply_num_tiles(n), &counter);
-    tile_trav.resize(std::max<uint64_t>(apply_num_tiles(n), 1));
+    unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
+    tile_trav.resize(std::max<uint64_t>(tiles, 1));
+    tword.resize(std::max<uint64_t>(tiles * 256, 1));
+    tile_agg.resize(std::max<uint64_t>(tiles, 1));
+    tile_state.resize(std::max<uint64_t>(tiles, 1));
     GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, tile_trav.ptr, st));
-    GFZ_TIMED_B(ctx, "apply", 4.0 * n,
-              launch_apply(A.ptr, n, heads.ptr, offA.ptr, ntrav, tile_trav.ptr, tab.view(cap), temp_base, B.ptr,
-                           offB.ptr, desc, counter, ds, st));
+    const ApplyScratch w{tword.ptr, tile_agg.ptr, tile_state.ptr, desc, counter};
+    GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n,
+                launch_apply_classify(A.ptr, n, heads.ptr, tab.view(cap), w, ds, st));
+    GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, w, ds, st));
+    GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
+                launch_apply_emit(A.ptr, n, heads.ptr, offA.ptr, ntrav, tile_trav.ptr, tab.view(cap), temp_base,
+                                  B.ptr, offB.ptr, w, ds, st));
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
     GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, std::max<uint64_t>(repeated, 1), ds, st));
@@ -321,7 +331,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     ctx.check_status("apply");
     const uint64_t n_out = s1.u64[2];
     const uint64_t U = s1.u64[3];
-    ctx.add_bytes("apply", 4.0 * n_out);
+    ctx.add_bytes("apply_emit", 4.0 * n_out);
     ctx.add_bytes("collect_used", 12.0 * U);
     if (U == 0) break;  // no rule used: stop all rounds
     ukeys_tmp.resize(U);

@@ -68,6 +68,18 @@ __device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, c
 
 constexpr uint32_t kTextBuf = 28 * 1024;
 
+// The four decimal characters of every x < 10000 ("0000" .. "9999"), the
+// first in the low byte; 40 KB that stays in L1 while text is written.
+struct Dec4Table {
+  uint32_t v[10000];
+  constexpr Dec4Table() : v() {
+    for (uint32_t x = 0; x < 10000; ++x)
+      v[x] = (uint32_t)('0' + x / 1000) | ((uint32_t)('0' + x / 100 % 10) << 8) |
+             ((uint32_t)('0' + x / 10 % 10) << 16) | ((uint32_t)('0' + x % 10) << 24);
+  }
+};
+__device__ const Dec4Table g_dec4 = Dec4Table();
+
 // Two decimal characters of x < 100, the first in the low byte.
 __device__ __forceinline__ uint32_t dec_pair(uint32_t x) {
   const uint32_t t = x / 10u;
@@ -84,7 +96,7 @@ struct WordWriter {
   uint32_t w;               // next word to write
   uint32_t n;               // bytes pending in acc (< 4 between calls)
   uint32_t limit;           // words in buf; words beyond are dropped
-  unsigned long long acc;
+  uint32_t acc;
   bool shared_first;
   bool overflow;            // a word fell outside buf
   __device__ __forceinline__ void init(uint32_t *b, uint32_t byte_off, uint32_t words) {
@@ -106,14 +118,18 @@ struct WordWriter {
   }
   // Appends the low cnt (<= 4) bytes of x (bytes above cnt must be zero).
   __device__ __forceinline__ void put(uint32_t x, uint32_t cnt) {
-    acc |= (unsigned long long)x << (8u * n);
+    const uint32_t sh = 8u * n;
+    const uint32_t lo = acc | (x << sh);
+    const uint32_t spill = __funnelshift_l(x, 0u, sh);  // the bytes of x beyond this word
     n += cnt;
     if (n >= 4) {
-      store((uint32_t)acc, shared_first);
+      store(lo, shared_first);
       shared_first = false;
       ++w;
-      acc >>= 32;
+      acc = spill;
       n -= 4;
+    } else {
+      acc = lo;
     }
   }
   // Appends the decimal digits of v (nd = dec_digits(v)), most significant first.
@@ -126,11 +142,8 @@ struct WordWriter {
       if (nd == 9) put(ph >> 8, 1);
       else put(ph, 2);
     }
-    const uint32_t a = lo / 10000u, b = lo - a * 10000u;
-    const uint32_t a1 = a / 100u, b1 = b / 100u;
-    unsigned long long c8 = (unsigned long long)dec_pair(a1) | ((unsigned long long)dec_pair(a - 100u * a1) << 16) |
-                            ((unsigned long long)dec_pair(b1) << 32) |
-                            ((unsigned long long)dec_pair(b - 100u * b1) << 48);
+    const uint32_t a = lo / 10000u;
+    unsigned long long c8 = (unsigned long long)g_dec4.v[a] | ((unsigned long long)g_dec4.v[lo - a * 10000u] << 32);
     const uint32_t k = nd > 8 ? 8u : nd;  // digits of lo to write
     c8 >>= 8u * (8u - k);
     if (k > 4) {
@@ -141,7 +154,7 @@ struct WordWriter {
     }
   }
   __device__ __forceinline__ void finish() {
-    if (n && acc) store((uint32_t)acc, true);
+    if (n && acc) store(acc, true);
   }
 };
 
