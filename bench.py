@@ -54,6 +54,9 @@ def parse_args():
     ap.add_argument("--cpu-sample-paths", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=5000.0, help="extract requests per second")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     return ap.parse_args()
 
 
@@ -145,6 +148,107 @@ def run_cpu_port(steps, off, sample_paths, threads):
     nbytes, _, _ = oracle.roundtrip_p(s, o, 8, 1, threads)
     dt = time.perf_counter() - t0
     return nbytes / dt / 1e9, dt, nbytes, f"{k} of {len(off) - 1} P-lines ({int(o[-1])} steps)"
+
+
+def serving_bench(ctx, rate: float, duration: float, cpu: bool, seed: int = 5):
+    """Serving on the config-1 bubble graph resident in HBM: Poisson-arriving
+    extract-path requests at `rate` req/s for `duration` s against
+    gfaz_gb300.Server, with an append of 1-8 new P-lines interleaved every
+    1000 requests.  Config-1 paths are ~22k steps, so the graph is the
+    config-1 generator on a 600k-segment backbone whose 64 P-lines are
+    lognormal windows (median 200k steps) of its traversals: the requests
+    keep the serving config's lengths.  Beside it: the same requests one per
+    launch through the non-resident extraction API (whole-container decode,
+    like the reference's extract-path), and the oracle's CPU expansion +
+    formatting of one path."""
+    import queue
+    import tempfile
+    import gfaz_gb300 as gz
+    from gfaz_gb300 import synthetic
+    steps, off, names, nseg, links = synthetic.serve_paths(seed=seed)
+    nt = len(off) - 1
+    g = gz.encode(steps, off, rounds=8, delta_round=1, ctx=ctx)
+    ptext = g.text(0, nt, names=names, overlaps=["*"] * nt)
+    del g
+    lines = ptext.split(b"\n")[:-1]
+    body = [b"H\tVN:Z:1.1\n", b"".join(b"S\t%d\t*\n" % i for i in range(1, nseg + 1)),
+            b"".join(b"L\t%d\t+\t%d\t+\t0M\n" % (a, b) for a, b in links.tolist()), ptext]
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "serve.gfa")
+        with open(path, "wb") as fh:
+            fh.write(b"".join(body))
+        data = gz.compress_file(path)
+    rng = np.random.default_rng(seed)
+    n_req = max(1, int(rate * duration))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    picks = rng.integers(0, nt, n_req)
+    lat, nbytes = [], [0]
+    with gz.Server(data, hbm_budget=40 << 30, workers=4) as srv:
+        for n in names:
+            srv.wait(srv.submit_path(n))
+        q = queue.Queue()
+
+        def waiter():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                kind, t = item
+                size, ms = srv.wait_size(t)
+                if kind == "x":
+                    lat.append(ms)
+                    nbytes[0] += size
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        appended = 0
+        t0 = time.perf_counter()
+        for k in range(n_req):
+            target = t0 + arrivals[k]
+            while time.perf_counter() < target:
+                pass
+            if k % 1000 == 500:
+                m = int(rng.integers(1, 9))
+                new = []
+                for j in range(m):
+                    src = lines[int(rng.integers(0, len(lines)))].split(b"\t")
+                    new.append(b"\t".join([src[0], b"app%d_%d" % (appended, j)] + src[2:]) + b"\n")
+                appended += 1
+                q.put(("a", srv.submit_append(b"".join(new))))
+            q.put(("x", srv.submit_path(names[int(picks[k])])))
+        q.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    plain = []
+    for i in rng.integers(0, nt, 10).tolist():
+        a = time.perf_counter()
+        gz.extract_path_line(data, names[i], ctx=ctx)
+        plain.append((time.perf_counter() - a) * 1e3)
+    out = {"rate_req_s": rate, "requests": len(lat), "appends": appended, "seconds": wall,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "gbps": nbytes[0] / wall / 1e9, "batches": st["batches"], "max_batch": st["max_batch"],
+           "workers": 4, "hbm_budget_gb": 40,
+           "graph": "config-1 bubble graph, 600k-segment backbone, 64 P-lines of lognormal length "
+                    "(median 200k steps), %d steps" % len(steps),
+           "plain_gpu": {"p50_ms": float(np.percentile(plain, 50)), "requests": len(plain),
+                         "form": "one request per launch, whole-container decode (non-resident extract API)"}}
+    if cpu:
+        from oracle import oracle
+        enc = oracle.compress(steps, off, 8, 1)
+        oo = off.astype(np.uint64)
+        cpu_ms = []
+        for i in rng.integers(0, nt, 5).tolist():
+            a = time.perf_counter()
+            e0, e1 = int(enc["enc_offsets"][i]), int(enc["enc_offsets"][i + 1])
+            x = oracle.expand(enc["encoded"][e0:e1], np.array([0, e1 - e0], np.uint64), enc["rules_first"],
+                              enc["rules_second"], enc["layer_start"], 1,
+                              np.array([0, int(oo[i + 1] - oo[i])], np.uint64))
+            oracle.format_p(x, np.array([0, len(x)], np.uint64), [names[i]], ["*"])
+            cpu_ms.append((time.perf_counter() - a) * 1e3)
+        out["cpu"] = {"p50_ms": float(np.percentile(cpu_ms, 50)), "requests": len(cpu_ms), "kind": "port",
+                      "form": "oracle expansion + P-line formatting of one path from a preloaded grammar"}
+    return out
 
 
 def reference_arm(args):
@@ -337,6 +441,10 @@ def main():
                "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s "
                          "(oracle/gfaz_oracle.c, OpenMP)"}
 
+    extract = None
+    if not args.no_serving and rank == 0:
+        extract = serving_bench(ctx, args.serve_rate, args.serve_seconds, not args.no_cpu_baseline)
+
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
@@ -358,6 +466,7 @@ def main():
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "extract": extract,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

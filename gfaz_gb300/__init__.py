@@ -32,6 +32,7 @@ __all__ = [
     "write_gfa_from_compressed_data", "write_gfa_from_compressed_data_gpu", "gfa_text",
     "extract_path_line", "extract_path_lines", "extract_walk_line", "extract_walk_lines",
     "extract_walk_line_by_name", "extract_walk_lines_by_name", "add_haplotypes", "encode", "load_grammar",
+    "Server",
 ]
 
 
@@ -340,6 +341,82 @@ def extract_walk_lines_by_name(data: CompressedData, walk_names: Sequence[str],
 def extract_walk_line_by_name(data: CompressedData, walk_name: str, num_threads: int = DEFAULT_NUM_THREADS,
                               ctx: Optional[Context] = None) -> str:
     return extract_walk_lines_by_name(data, [walk_name], num_threads, ctx)[0]
+
+
+class Server:
+    """Resident extraction server with continuous batching.
+
+    The rules, their prefix buffers and every encoded traversal of `data`
+    stay on the GPU.  submit_path / submit_walk / submit_append queue a
+    request and return a ticket; wait(ticket) returns (line, latency_ms).
+    Extractions that arrive while others run on the GPU join the next batch
+    of a free worker (one CUDA stream per worker) while their expanded output
+    fits `hbm_budget` bytes; an append is applied once no batch is in flight
+    and is visible to every later request.  Lines equal extract_path_line /
+    extract_walk_line on the same container (the reference has no server:
+    each extraction decodes the whole file, extraction_workflow.cpp:207-357).
+    """
+
+    def __init__(self, data: CompressedData, hbm_budget: int = 40 << 30, workers: int = 2, device: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().gfz_server_create(int(device), data.handle, int(hbm_budget), int(workers), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gfz_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit_path(self, name: str) -> int:
+        t = ctypes.c_uint64()
+        check(lib().gfz_server_submit_path(self._h, _cstr(name), ctypes.byref(t)))
+        return t.value
+
+    def submit_walk(self, key: WalkLookupKey) -> int:
+        s, q = _cstr(key.sample_id), _cstr(key.seq_id)
+        k = WalkKeyC(s, int(key.hap_index), q, int(key.seq_start), int(key.seq_end))
+        t = ctypes.c_uint64()
+        check(lib().gfz_server_submit_walk(self._h, ctypes.byref(k), ctypes.byref(t)))
+        return t.value
+
+    def submit_append(self, gfa_text) -> int:
+        b = _cstr(gfa_text)
+        t = ctypes.c_uint64()
+        check(lib().gfz_server_submit_append(self._h, b, len(b), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, as_bytes: bool = False):
+        p, n, ms = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
+        check(lib().gfz_server_wait(self._h, int(ticket), ctypes.byref(p), ctypes.byref(n), ctypes.byref(ms)))
+        try:
+            line = ctypes.string_at(p, n.value) if n.value else b""
+        finally:
+            check(lib().gfz_server_release(self._h, int(ticket)))
+        return (line if as_bytes else line.decode()), ms.value
+
+    def wait_size(self, ticket: int):
+        """Like wait, but releases the line without copying it: (bytes, latency_ms)."""
+        p, n, ms = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
+        check(lib().gfz_server_wait(self._h, int(ticket), ctypes.byref(p), ctypes.byref(n), ctypes.byref(ms)))
+        check(lib().gfz_server_release(self._h, int(ticket)))
+        return n.value, ms.value
+
+    def stats(self) -> dict:
+        b, r, m = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().gfz_server_stats(self._h, ctypes.byref(b), ctypes.byref(r), ctypes.byref(m)))
+        return {"batches": b.value, "requests": r.value, "max_batch": m.value}
 
 
 def add_haplotypes(data: CompressedData, haplotypes_path, threads: int = DEFAULT_NUM_THREADS,

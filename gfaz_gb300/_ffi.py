@@ -94,6 +94,14 @@ SIGNATURES = {
     "gfz_decode": (I, [P, P, U64, U64, P, U64, PU64, P, I]),
     "gfz_decode_text": (I, [P, P, U64, U64, ctypes.POINTER(LineMeta), P, U64, PU64, I]),
     "gfz_grammar_text": (I, [P, PP, PU64]),
+    "gfz_server_create": (I, [I, P, U64, I, PP]),
+    "gfz_server_submit_path": (I, [P, CP, PU64]),
+    "gfz_server_submit_walk": (I, [P, ctypes.POINTER(WalkKeyC), PU64]),
+    "gfz_server_submit_append": (I, [P, CP, SZ, PU64]),
+    "gfz_server_wait": (I, [P, U64, PP, PSZ, ctypes.POINTER(ctypes.c_double)]),
+    "gfz_server_release": (I, [P, U64]),
+    "gfz_server_stats": (I, [P, PU64, PU64, PU64]),
+    "gfz_server_destroy": (None, [P]),
     "gfz_inverse_delta_noalloc": (I, [P, P, U64, P, U64, I, P]),
 }
 NOALLOC_MAX_STEPS = 1 << 26

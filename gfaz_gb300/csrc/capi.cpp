@@ -11,6 +11,7 @@
 #include <string>
 
 #include "host/model.h"
+#include "host/server.h"
 #include "host/workflows.h"
 #include "noalloc.h"
 #include "pipeline.h"
@@ -615,6 +616,76 @@ gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint
     *size = g->text_size;
   });
 }
+
+struct gfz_server {
+  std::unique_ptr<gfz::Server> s;
+};
+
+gfz_status gfz_server_create(int device, const gfz_compressed *c, uint64_t hbm_budget, int workers,
+                             gfz_server **out) {
+  return guard([&] {
+    require(c && out, "NULL argument");
+    require(workers >= 1 && workers <= 64, "workers must be in 1..64");
+    auto srv = std::make_unique<gfz_server>();
+    srv->s = std::make_unique<gfz::Server>(device, c->c, hbm_budget, workers);
+    *out = srv.release();
+  });
+}
+
+gfz_status gfz_server_submit_path(gfz_server *s, const char *name, uint64_t *ticket) {
+  return guard([&] {
+    require(s && name && ticket, "NULL argument");
+    *ticket = s->s->submit_path(name);
+  });
+}
+
+gfz_status gfz_server_submit_walk(gfz_server *s, const gfz_walk_key *key, uint64_t *ticket) {
+  return guard([&] {
+    require(s && key && key->sample_id && key->seq_id && ticket, "NULL argument");
+    gfz::WalkKey k;
+    k.sample_id = key->sample_id;
+    k.hap_index = key->hap_index;
+    k.seq_id = key->seq_id;
+    k.seq_start = key->seq_start;
+    k.seq_end = key->seq_end;
+    *ticket = s->s->submit_walk(k);
+  });
+}
+
+gfz_status gfz_server_submit_append(gfz_server *s, const char *gfa_text, size_t len, uint64_t *ticket) {
+  return guard([&] {
+    require(s && (gfa_text || !len) && ticket, "NULL argument");
+    *ticket = s->s->submit_append(std::string(gfa_text ? gfa_text : "", len));
+  });
+}
+
+gfz_status gfz_server_wait(gfz_server *s, uint64_t ticket, const char **line, size_t *len, double *latency_ms) {
+  return guard([&] {
+    require(s && line && len, "NULL argument");
+    size_t n = 0;
+    *line = s->s->wait(ticket, &n, latency_ms);
+    *len = n;
+  });
+}
+
+gfz_status gfz_server_release(gfz_server *s, uint64_t ticket) {
+  return guard([&] {
+    require(s, "NULL argument");
+    s->s->release(ticket);
+  });
+}
+
+gfz_status gfz_server_stats(gfz_server *s, uint64_t *batches, uint64_t *requests, uint64_t *max_batch) {
+  return guard([&] {
+    require(s, "NULL argument");
+    const gfz::Server::Stats st = s->s->stats();
+    if (batches) *batches = st.batches;
+    if (requests) *requests = st.requests;
+    if (max_batch) *max_batch = st.max_batch;
+  });
+}
+
+void gfz_server_destroy(gfz_server *s) { delete s; }
 
 gfz_status gfz_inverse_delta_noalloc(const int32_t *steps_in, int32_t *steps_out, uint64_t n, const uint64_t *offsets,
                                      uint64_t ntrav, int delta_round, void *cuda_stream) {

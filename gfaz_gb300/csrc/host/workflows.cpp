@@ -293,8 +293,8 @@ std::string static_text(const Compressed &d, const StaticFields &s) {
 // blob[pre_off[t] .. pre_off[t+1]) and its suffix blob[suf_off[t] ..
 // suf_off[t+1]); prefixes and suffixes live in two halves of one blob.
 // Lines of empty traversals after the last non-empty one form the tail.
-static TextPieces make_pieces(const std::vector<std::string> &pre, const std::vector<std::string> &suf,
-                              const std::vector<uint64_t> &off) {
+TextPieces make_pieces(const std::vector<std::string> &pre, const std::vector<std::string> &suf,
+                       const std::vector<uint64_t> &off) {
   const size_t n = pre.size();
   TextPieces r;
   r.pre_off.assign(n + 1, 0);
@@ -561,6 +561,16 @@ LoadedStreams load_all(Context &ctx, const Compressed &c, Grammar &g, const char
   return ls;
 }
 
+}  // namespace
+
+void load_traversals(Context &ctx, const Compressed &c, Grammar &g, uint64_t &np, uint64_t &nw) {
+  const LoadedStreams ls = load_all(ctx, c, g, "Extraction workflow error: ");
+  np = ls.np;
+  nw = ls.nw;
+}
+
+namespace {
+
 void download_text(Context &ctx, const DevVec<char> &text, uint64_t n, std::string &out) {
   const size_t o = out.size();
   out.resize(o + n);
@@ -821,14 +831,6 @@ std::vector<std::string> extract_walk_lines_by_name(Context &ctx, const Compress
 // ---------------------------------------------------------------------------
 namespace {
 
-struct AppendInput {
-  Traversals paths, walks;
-  std::vector<std::string> names, overlaps, samples, seqids;
-  std::vector<uint32_t> haps;
-  std::vector<int64_t> starts, ends;
-  bool has_paths = false, has_walks = false;
-};
-
 std::string_view field(std::string_view line, size_t &pos) {
   while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
   const size_t b = pos;
@@ -884,9 +886,7 @@ int32_t strict_node(std::string_view v, char o, const char *what) {
   return (o == '-' || o == '<') ? -(int32_t)id : (int32_t)id;
 }
 
-AppendInput parse_append(const std::string &path) {
-  std::ifstream in(path);
-  if (!in.is_open()) throw std::runtime_error(std::string(kAddErr) + "failed to open input file '" + path + "'");
+AppendInput parse_append_stream(std::istream &in) {
   AppendInput a;
   a.paths.offsets.push_back(0);
   a.walks.offsets.push_back(0);
@@ -968,6 +968,12 @@ AppendInput parse_append(const std::string &path) {
   return a;
 }
 
+AppendInput parse_append(const std::string &path) {
+  std::ifstream in(path);
+  if (!in.is_open()) throw std::runtime_error(std::string(kAddErr) + "failed to open input file '" + path + "'");
+  return parse_append_stream(in);
+}
+
 std::string walk_identity(const std::string &s, uint32_t h, const std::string &q, int64_t a, int64_t b) {
   return s + '\x1f' + std::to_string(h) + '\x1f' + q + '\x1f' + std::to_string(a) + '\x1f' + std::to_string(b);
 }
@@ -1004,9 +1010,25 @@ void encode_append(Context &ctx, const Compressed &c, const Traversals &tv, std:
 
 }  // namespace
 
+AppendInput parse_append_text(const std::string &gfa_text) {
+  std::istringstream in(gfa_text);
+  return parse_append_stream(in);
+}
+
+static void add_haplotypes_input(Context &ctx, Compressed &c, const AppendInput &in);
+
 void add_haplotypes(Context &ctx, Compressed &c, const std::string &path, int threads) {
   set_zstd_threads(resolve_threads(threads));
-  const AppendInput in = parse_append(path);
+  add_haplotypes_input(ctx, c, parse_append(path));
+}
+
+void add_haplotypes_text(Context &ctx, Compressed &c, const std::string &gfa_text, int threads) {
+  set_zstd_threads(resolve_threads(threads));
+  std::istringstream in(gfa_text);
+  add_haplotypes_input(ctx, c, parse_append_stream(in));
+}
+
+static void add_haplotypes_input(Context &ctx, Compressed &c, const AppendInput &in) {
   if (in.has_paths) {
     std::vector<std::string> names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kAddErr);
     std::unordered_set<std::string> seen(names.begin(), names.end());

@@ -44,6 +44,27 @@ std::vector<std::string> extract_walk_lines_by_name(Context &ctx, const Compress
 
 // src/workflows/add_haplotypes_workflow.cpp:579 add_haplotypes
 void add_haplotypes(Context &ctx, Compressed &c, const std::string &path, int threads);
+// Parsed add-haplotypes input: P-lines or W-lines (never both), with the
+// checks of add_haplotypes_workflow.cpp's parser.
+struct AppendInput {
+  Traversals paths, walks;
+  std::vector<std::string> names, overlaps, samples, seqids;
+  std::vector<uint32_t> haps;
+  std::vector<int64_t> starts, ends;
+  bool has_paths = false, has_walks = false;
+};
+AppendInput parse_append_text(const std::string &gfa_text);
+
+// The same with the appended P or W lines given as GFA text.
+void add_haplotypes_text(Context &ctx, Compressed &c, const std::string &gfa_text, int threads);
+
+// Rules and every encoded traversal of c (paths, then walks) into g.
+void load_traversals(Context &ctx, const Compressed &c, Grammar &g, uint64_t &np, uint64_t &nw);
+
+// Text pieces of traversal lines: prefix pre[t] before the steps of t and
+// suffix suf[t] after them (empty traversals folded in; see TextPieces).
+TextPieces make_pieces(const std::vector<std::string> &pre, const std::vector<std::string> &suf,
+                       const std::vector<uint64_t> &off);
 
 // Decoded rule columns (zstd + delta decode on the device) and text pieces.
 void decode_rule_columns(Context &ctx, const Compressed &c, Grammar &g);

@@ -596,6 +596,11 @@ static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, E
   GFZ_TIMED(ctx, "tile_symbols", launch_tile_symbols(P.pos.ptr, m, P.total, P.tile_sym.ptr, st));
 }
 
+void prepare_decode(Context &ctx, Grammar &g) {
+  ensure_rule_lengths(ctx, g);
+  if (g.delta_round <= 1) ensure_rule_prefix(ctx, g);
+}
+
 void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVec<int32_t> &out,
                        std::vector<uint64_t> &out_off) {
   cudaStream_t st = ctx.stream();

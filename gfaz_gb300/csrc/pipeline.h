@@ -28,6 +28,7 @@ struct DevVec {
   T *ptr = nullptr;
   uint64_t size = 0, cap = 0;
   cudaStream_t st = nullptr;
+  bool owned = true;  // false: a view of another vector's memory (borrow)
   DevVec() = default;
   explicit DevVec(cudaStream_t s) : st(s) {}
   DevVec(const DevVec &) = delete;
@@ -46,11 +47,20 @@ struct DevVec {
     std::swap(size, o.size);
     std::swap(cap, o.cap);
     std::swap(st, o.st);
+    std::swap(owned, o.owned);
   }
   void release() {
-    if (ptr) cudaFreeAsync(ptr, st);
+    if (ptr && owned) cudaFreeAsync(ptr, st);
     ptr = nullptr;
     size = cap = 0;
+    owned = true;
+  }
+  // Views n elements at p without owning them; the owner must outlive the view.
+  void borrow(T *p, uint64_t n) {
+    release();
+    ptr = p;
+    size = cap = n;
+    owned = false;
   }
   // Ensures capacity >= n (contents are kept when keep = true).
   void reserve(uint64_t n, bool keep = false) {
@@ -59,9 +69,10 @@ struct DevVec {
     cuda_check(cudaMallocAsync((void **)&np, (n ? n : 1) * sizeof(T), st), "device allocation");
     if (keep && ptr && size)
       cuda_check(cudaMemcpyAsync(np, ptr, size * sizeof(T), cudaMemcpyDeviceToDevice, st), "device copy");
-    if (ptr) cudaFreeAsync(ptr, st);
+    if (ptr && owned) cudaFreeAsync(ptr, st);
     ptr = np;
     cap = n;
+    owned = true;
   }
   void resize(uint64_t n, bool keep = false) {
     reserve(n, keep);
@@ -197,6 +208,10 @@ struct TextPieces {
 // data, host offsets) into a device text buffer; returns the size.
 uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uint64_t> &off,
                    const TextPieces &pieces, int mode, DevVec<char> &text);
+
+// Builds g's decode-side tables (rule lengths, rule prefix buffers) now
+// instead of on first use.
+void prepare_decode(Context &ctx, Grammar &g);
 
 // Decode + text for traversals [t0, t1) of g.  `pieces` builds the text
 // pieces from the decoded traversal offsets (t1 - t0 + 1 entries, from 0).

@@ -284,6 +284,50 @@ def cfg3_stream(seed: int = 3, n_backbone: int = 1_666_667, n_walks: int = 2000,
     return np.concatenate(walks), off, nblk * blk, meta
 
 
+def serve_paths(seed: int = 5, n_backbone: int = 600_000, n_paths: int = 64, median: float = 2e5,
+                sigma: float = 0.5, lo: int = 1000, rev_num: int = 2, rev_den: int = 100):
+    """Serving graph: the config-1 bubble graph on a longer backbone, whose
+    P-lines are windows of lognormal length (median `median` steps) of a
+    config-1 traversal starting at a random block, so that extract requests
+    have the serving config's lengths.  Returns (steps int32, offsets
+    uint64, names, num_segments, links (L, 2))."""
+    bubble_every = 10
+    nblk = n_backbone // bubble_every
+    blk = bubble_every + 2
+    base = np.arange(nblk, dtype=np.int64) * blk + 1
+    per_blk = bubble_every + 1
+    hi = (nblk - 3) * per_blk  # a window of nb = n // per_blk + 2 blocks fits the backbone
+    u = rng_u64(seed, 1, 2 * n_paths)
+    q = ((u[:n_paths] >> np.uint64(32)).astype(np.float64) + 0.5) / float(1 << 32)
+    z = np.array([_inv_norm(x) for x in q.tolist()])
+    steps_n = np.clip(np.round(median * np.exp(sigma * z)), lo, hi).astype(np.int64)
+    paths = []
+    for p in range(n_paths):
+        n = int(steps_n[p])
+        nb = n // per_blk + 2
+        first = int(u[n_paths + p] % np.uint64(max(1, nblk - nb)))
+        bidx = first + np.arange(nb)
+        r = rng_u64(seed, 100 + p, 2 * nb)
+        choice = (r[:nb] & np.uint64(1)).astype(np.int64)
+        rev = _bernoulli(r[nb:] >> np.uint64(1), rev_num, rev_den)
+        starts = np.empty(2 * nb, np.int64)
+        lengths = np.empty(2 * nb, np.int64)
+        revs = np.zeros(2 * nb, bool)
+        starts[0::2], lengths[0::2] = base[bidx], bubble_every
+        starts[1::2], lengths[1::2], revs[1::2] = base[bidx] + bubble_every + choice, 1, rev
+        paths.append(_expand_runs(starts, lengths, revs)[:n])
+    lens = np.array([len(x) for x in paths], dtype=np.uint64)
+    off = np.zeros(n_paths + 1, np.uint64)
+    np.cumsum(lens, out=off[1:])
+    last = base + bubble_every - 1
+    links = [np.stack([(base[:, None] + np.arange(bubble_every - 1)[None, :]).ravel(),
+                       (base[:, None] + np.arange(1, bubble_every)[None, :]).ravel()], 1),
+             np.stack([last, last + 1], 1), np.stack([last, last + 2], 1),
+             np.stack([last[:-1] + 1, base[1:]], 1), np.stack([last[:-1] + 2, base[1:]], 1)]
+    return (np.concatenate(paths).astype(np.int32), off, [f"hap{p}" for p in range(n_paths)], nblk * blk,
+            np.concatenate(links).astype(np.int64))
+
+
 def _inv_norm(p: float) -> float:
     """Acklam's rational approximation of the standard normal quantile."""
     a = [-3.969683028665376e+01, 2.209460984245205e+02, -2.759285104469687e+02,

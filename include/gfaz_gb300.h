@@ -201,6 +201,34 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
                            char *out, uint64_t cap, uint64_t *size, int where);
 gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size);
 
+/* ---- resident extraction server ------------------------------------------ */
+/* No counterpart in the reference, which decodes the whole file for each
+ * extraction (src/workflows/extraction_workflow.cpp:207-357) and rewrites
+ * the container for each append (add_haplotypes_workflow.cpp:579).  The
+ * server keeps the rules, their prefix buffers and all encoded traversals
+ * of `c` in HBM and serves extract-path / extract-walk / append requests
+ * with continuous batching: `workers` threads, one CUDA stream each, take
+ * the queued extractions whose expanded output fits the free part of
+ * `hbm_budget` bytes and decode them in one launch; requests arriving
+ * meanwhile join the next batch.  An append waits for the batches in flight
+ * and is seen by every later request.  Returned lines are byte-identical to
+ * gfz_extract_path_lines / gfz_extract_walk_lines on the same container. */
+typedef struct gfz_server gfz_server;
+gfz_status gfz_server_create(int device, const gfz_compressed *c, uint64_t hbm_budget, int workers,
+                             gfz_server **out);
+gfz_status gfz_server_submit_path(gfz_server *s, const char *name, uint64_t *ticket);
+gfz_status gfz_server_submit_walk(gfz_server *s, const gfz_walk_key *key, uint64_t *ticket);
+/* P or W lines to append, as GFA text (the add-haplotypes input format). */
+gfz_status gfz_server_submit_append(gfz_server *s, const char *gfa_text, size_t len, uint64_t *ticket);
+/* Blocks until request `ticket` is done: its line (empty for an append)
+ * and the time from submission to completion.  The line lives in the
+ * server's pinned host memory, valid until gfz_server_release(s, ticket);
+ * a request that failed returns its error and is released already. */
+gfz_status gfz_server_wait(gfz_server *s, uint64_t ticket, const char **line, size_t *len, double *latency_ms);
+gfz_status gfz_server_release(gfz_server *s, uint64_t ticket);
+gfz_status gfz_server_stats(gfz_server *s, uint64_t *batches, uint64_t *requests, uint64_t *max_batch);
+void gfz_server_destroy(gfz_server *s);
+
 /* Allocation-free inverse delta.  This entry point has no counterpart in the
  * reference.  It is for callers that may not allocate device memory: hosts
  * whose own pool allocator holds nearly all of HBM, plug-ins that such a host
