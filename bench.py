@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-traversal-per-launch GPU baseline")
     ap.add_argument("--serve-rate", type=float, default=5000.0, help="extract requests per second")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     return ap.parse_args()
@@ -441,6 +442,37 @@ def main():
                "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s "
                          "(oracle/gfaz_oracle.c, OpenMP)"}
 
+    # plain GPU form: the same kernels with one traversal per launch sequence
+    # (compression encodes each P-line as its own stream, so its rulebooks
+    # are per path: a throughput baseline; decompression decodes the shared
+    # grammar one path at a time and gives identical text)
+    plain = None
+    if not args.no_plain:
+        with torch.cuda.stream(stream):
+            torch.cuda.synchronize()
+            c0 = time.perf_counter()
+            grams = []
+            for t in range(ntrav):
+                o = np.array([0, int(off[t + 1] - off[t])], np.uint64)
+                grams.append(gz.encode(None, o, rounds=8, delta_round=1, ctx=ctx,
+                                       device_ptr=d_steps.data_ptr() + 4 * int(off[t])))
+            torch.cuda.synchronize()
+            pc = time.perf_counter() - c0
+            del grams
+            g = gz.encode(None, off, rounds=8, delta_round=1, ctx=ctx, device_ptr=d_steps.data_ptr())
+            torch.cuda.synchronize()
+            d0 = time.perf_counter()
+            pbytes = 0
+            for t in range(ntrav):
+                pbytes += g.decode_text(t, t + 1, names=names[t:t + 1], overlaps=overlaps[t:t + 1])
+            torch.cuda.synchronize()
+            pd = time.perf_counter() - d0
+            del g
+        plain = {"value": ws * text_bytes / (pc + pd) / 1e9, "compress_gbps": ws * text_bytes / pc / 1e9,
+                 "decompress_gbps": ws * pbytes / pd / 1e9, "compress_ms": pc * 1e3, "decompress_ms": pd * 1e3,
+                 "text_identical_size": pbytes == text_bytes,
+                 "form": "one traversal per launch sequence (%d sequences), wall clock" % ntrav}
+
     extract = None
     if not args.no_serving and rank == 0:
         extract = serving_bench(ctx, args.serve_rate, args.serve_seconds, not args.no_cpu_baseline)
@@ -466,6 +498,7 @@ def main():
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "plain_gpu": plain,
         "extract": extract,
     }
     if rank == 0:

@@ -162,3 +162,35 @@ def test_warp_dedup_switch_gives_same_result(gpu_ctx):
     b = gz.encode(steps, off, ctx=ctx2).arrays()
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
+
+
+def test_cfg3_walk_text(gpu_ctx):
+    # config-3 shape: uneven walks (lognormal lengths, sigma 2) as W lines
+    steps, off, _, meta = synthetic.cfg3_stream(seed=3, n_backbone=200_000, n_walks=300, median=5e3, sigma=2.0,
+                                                hi=1_000_000, max_total=4_000_000)
+    for dr in (1, 0):
+        g, _ = check_encode(steps, off, gpu_ctx, delta_round=dr)
+        n = len(off) - 1
+        samples, haps, seqids, starts, ends = (list(x) for x in zip(*meta))
+        got = g.text(0, n, mode=gz.W_LINES, names=samples, hap_indices=haps, seq_ids=seqids, seq_starts=starts,
+                     seq_ends=ends)
+        assert got == oracle.format_w(steps, off, samples, haps, seqids, starts, ends)
+
+
+@pytest.mark.parametrize("delta_round", [0, 1])
+def test_text_incompressible_and_long_pieces(delta_round, gpu_ctx):
+    # random steps barely compress: output tiles cover more symbols than the
+    # shared-memory stage holds; ids span every digit count and both signs
+    rng = np.random.default_rng(31 + delta_round)
+    lens = [0, 1, 5000, 0, 12_000, 3, 9000]
+    steps = rng.integers(-2_000_000_000, 2_000_000_000, size=sum(lens)).astype(np.int32)
+    steps[rng.integers(0, len(steps), 200)] = rng.integers(-9, 10, 200)
+    off = offsets_of(lens)
+    g, _ = check_encode(steps, off, gpu_ctx, delta_round=delta_round)
+    n = len(lens)
+    names = [f"p{i}" for i in range(n)]
+    ovs = ["*"] * n
+    assert g.text(0, n, names=names, overlaps=ovs) == oracle.format_p(steps, off, names, ovs)
+    # a name longer than a tile's text staging: that tile writes straight to HBM
+    names[2] = "n" * 40_000
+    assert g.text(0, n, names=names, overlaps=ovs) == oracle.format_p(steps, off, names, ovs)
