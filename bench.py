@@ -58,6 +58,8 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true", help="skip the one-traversal-per-launch GPU baseline")
     ap.add_argument("--serve-rate", type=float, default=5000.0, help="extract requests per second")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-sweep", default="100,1000,10000,20000",
+                    help="further request rates to report (comma separated; empty for none)")
     return ap.parse_args()
 
 
@@ -151,18 +153,11 @@ def run_cpu_port(steps, off, sample_paths, threads):
     return nbytes / dt / 1e9, dt, nbytes, f"{k} of {len(off) - 1} P-lines ({int(o[-1])} steps)"
 
 
-def serving_bench(ctx, rate: float, duration: float, cpu: bool, seed: int = 5):
-    """Serving on the config-1 bubble graph resident in HBM: Poisson-arriving
-    extract-path requests at `rate` req/s for `duration` s against
-    gfaz_gb300.Server, with an append of 1-8 new P-lines interleaved every
-    1000 requests.  Config-1 paths are ~22k steps, so the graph is the
-    config-1 generator on a 600k-segment backbone whose 64 P-lines are
-    lognormal windows (median 200k steps) of its traversals: the requests
-    keep the serving config's lengths.  Beside it: the same requests one per
-    launch through the non-resident extraction API (whole-container decode,
-    like the reference's extract-path), and the oracle's CPU expansion +
-    formatting of one path."""
-    import queue
+def serving_setup(ctx, seed: int = 5):
+    """The serving graph: the config-1 generator on a 600k-segment backbone
+    whose 64 P-lines are lognormal windows (median 200k steps) of its
+    traversals, compressed into a container.  Config-1 paths are ~22k
+    steps, so the longer windows keep the serving config's lengths."""
     import tempfile
     import gfaz_gb300 as gz
     from gfaz_gb300 import synthetic
@@ -179,12 +174,24 @@ def serving_bench(ctx, rate: float, duration: float, cpu: bool, seed: int = 5):
         with open(path, "wb") as fh:
             fh.write(b"".join(body))
         data = gz.compress_file(path)
+    return {"data": data, "steps": steps, "off": off, "names": names, "lines": lines}
+
+
+def serving_run(S, rate: float, duration: float, seed: int = 5, append_every: int = 1000, workers: int = 4,
+                trace: list = None) -> dict:
+    """Poisson-arriving extract-path requests at `rate` req/s for `duration`
+    s against gfaz_gb300.Server holding the serving graph, with an append of
+    1-8 new P-lines every `append_every` requests."""
+    import queue
+    import gfaz_gb300 as gz
+    data, names, lines = S["data"], S["names"], S["lines"]
+    nt = len(names)
     rng = np.random.default_rng(seed)
     n_req = max(1, int(rate * duration))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
     picks = rng.integers(0, nt, n_req)
-    lat, nbytes = [], [0]
-    with gz.Server(data, hbm_budget=40 << 30, workers=4) as srv:
+    lat, qms, sms, bsz, nbytes = [], [], [], [], [0]
+    with gz.Server(data, hbm_budget=40 << 30, workers=workers) as srv:
         for n in names:
             srv.wait(srv.submit_path(n))
         q = queue.Queue()
@@ -194,11 +201,16 @@ def serving_bench(ctx, rate: float, duration: float, cpu: bool, seed: int = 5):
                 item = q.get()
                 if item is None:
                     return
-                kind, t = item
-                size, ms = srv.wait_size(t)
+                kind, k, t = item
+                size, ms, q_ms, s_ms, b = srv.wait_detail(t)
                 if kind == "x":
                     lat.append(ms)
+                    qms.append(q_ms)
+                    sms.append(s_ms)
+                    bsz.append(b)
                     nbytes[0] += size
+                if trace is not None:
+                    trace.append((kind, k, float(arrivals[k]), ms, q_ms, s_ms, b))
 
         th = threading.Thread(target=waiter)
         th.start()
@@ -206,37 +218,59 @@ def serving_bench(ctx, rate: float, duration: float, cpu: bool, seed: int = 5):
         t0 = time.perf_counter()
         for k in range(n_req):
             target = t0 + arrivals[k]
-            while time.perf_counter() < target:
-                pass
-            if k % 1000 == 500:
+            while True:
+                d = target - time.perf_counter()
+                if d <= 0:
+                    break
+                if d > 4e-4:
+                    time.sleep(d - 3e-4)  # leave the interpreter to the waiter thread
+            if append_every and k % append_every == append_every // 2:
                 m = int(rng.integers(1, 9))
                 new = []
                 for j in range(m):
                     src = lines[int(rng.integers(0, len(lines)))].split(b"\t")
                     new.append(b"\t".join([src[0], b"app%d_%d" % (appended, j)] + src[2:]) + b"\n")
                 appended += 1
-                q.put(("a", srv.submit_append(b"".join(new))))
-            q.put(("x", srv.submit_path(names[int(picks[k])])))
+                q.put(("a", k, srv.submit_append(b"".join(new))))
+            q.put(("x", k, srv.submit_path(names[int(picks[k])])))
         q.put(None)
         th.join()
         wall = time.perf_counter() - t0
         st = srv.stats()
+    return {"rate_req_s": rate, "requests": len(lat), "appends": appended, "seconds": wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "queue_p50_ms": float(np.percentile(qms, 50)), "queue_p99_ms": float(np.percentile(qms, 99)),
+            "service_p50_ms": float(np.percentile(sms, 50)), "service_p99_ms": float(np.percentile(sms, 99)),
+            "mean_batch": float(np.mean(bsz)), "gbps": nbytes[0] / wall / 1e9, "batches": st["batches"],
+            "max_batch": st["max_batch"], "workers": workers}
+
+
+def serving_bench(ctx, rate: float, duration: float, cpu: bool, sweep=(), seed: int = 5) -> dict:
+    """Serving (config 5): the headline rate, a sweep of other rates, and
+    beside them the same requests one per launch through the non-resident
+    extraction API (whole-container decode, like the reference's
+    extract-path) and the oracle's CPU expansion + formatting of one path."""
+    import gfaz_gb300 as gz
+    S = serving_setup(ctx, seed)
+    out = serving_run(S, rate, duration, seed)
+    out.update({"hbm_budget_gb": 40,
+                "graph": "config-1 bubble graph, 600k-segment backbone, 64 P-lines of lognormal length "
+                         "(median 200k steps), %d steps" % len(S["steps"])})
+    keep = ("rate_req_s", "p50_ms", "p99_ms", "queue_p99_ms", "service_p99_ms", "mean_batch", "gbps")
+    out["sweep"] = [{k: v for k, v in serving_run(S, r, duration, seed).items() if k in keep} for r in sweep]
+    data, names, off = S["data"], S["names"], S["off"]
+    nt = len(names)
+    rng = np.random.default_rng(seed + 1)
     plain = []
     for i in rng.integers(0, nt, 10).tolist():
         a = time.perf_counter()
         gz.extract_path_line(data, names[i], ctx=ctx)
         plain.append((time.perf_counter() - a) * 1e3)
-    out = {"rate_req_s": rate, "requests": len(lat), "appends": appended, "seconds": wall,
-           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-           "gbps": nbytes[0] / wall / 1e9, "batches": st["batches"], "max_batch": st["max_batch"],
-           "workers": 4, "hbm_budget_gb": 40,
-           "graph": "config-1 bubble graph, 600k-segment backbone, 64 P-lines of lognormal length "
-                    "(median 200k steps), %d steps" % len(steps),
-           "plain_gpu": {"p50_ms": float(np.percentile(plain, 50)), "requests": len(plain),
-                         "form": "one request per launch, whole-container decode (non-resident extract API)"}}
+    out["plain_gpu"] = {"p50_ms": float(np.percentile(plain, 50)), "requests": len(plain),
+                        "form": "one request per launch, whole-container decode (non-resident extract API)"}
     if cpu:
         from oracle import oracle
-        enc = oracle.compress(steps, off, 8, 1)
+        enc = oracle.compress(S["steps"], off, 8, 1)
         oo = off.astype(np.uint64)
         cpu_ms = []
         for i in rng.integers(0, nt, 5).tolist():
@@ -475,7 +509,8 @@ def main():
 
     extract = None
     if not args.no_serving and rank == 0:
-        extract = serving_bench(ctx, args.serve_rate, args.serve_seconds, not args.no_cpu_baseline)
+        sweep = [float(x) for x in args.serve_sweep.split(",") if x]
+        extract = serving_bench(ctx, args.serve_rate, args.serve_seconds, not args.no_cpu_baseline, sweep)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

@@ -408,10 +408,16 @@ class Server:
 
     def wait_size(self, ticket: int):
         """Like wait, but releases the line without copying it: (bytes, latency_ms)."""
-        p, n, ms = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
-        check(lib().gfz_server_wait(self._h, int(ticket), ctypes.byref(p), ctypes.byref(n), ctypes.byref(ms)))
-        check(lib().gfz_server_release(self._h, int(ticket)))
-        return n.value, ms.value
+        n, ms, _, _, _ = self.wait_detail(ticket)
+        return n, ms
+
+    def wait_detail(self, ticket: int):
+        """Waits for the request and releases its line without copying it:
+        (bytes, latency_ms, queue_ms, service_ms, batch_size)."""
+        n, ms, q, sv, b = ctypes.c_size_t(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint32()
+        check(lib().gfz_server_collect(self._h, int(ticket), ctypes.byref(n), ctypes.byref(ms), ctypes.byref(q),
+                                       ctypes.byref(sv), ctypes.byref(b)))
+        return n.value, ms.value, q.value, sv.value, b.value
 
     def stats(self) -> dict:
         b, r, m = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

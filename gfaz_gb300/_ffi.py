@@ -99,7 +99,11 @@ SIGNATURES = {
     "gfz_server_submit_walk": (I, [P, ctypes.POINTER(WalkKeyC), PU64]),
     "gfz_server_submit_append": (I, [P, CP, SZ, PU64]),
     "gfz_server_wait": (I, [P, U64, PP, PSZ, ctypes.POINTER(ctypes.c_double)]),
+    "gfz_server_request_times": (I, [P, U64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_uint32)]),
     "gfz_server_release": (I, [P, U64]),
+    "gfz_server_collect": (I, [P, U64, PSZ, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint32)]),
     "gfz_server_stats": (I, [P, PU64, PU64, PU64]),
     "gfz_server_destroy": (None, [P]),
     "gfz_inverse_delta_noalloc": (I, [P, P, U64, P, U64, I, P]),

@@ -215,8 +215,10 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     else if (std::string(name) == "first_table_cap") {
       require(value >= 0 && (value & (value - 1)) == 0, "first_table_cap must be 0 or a power of two");
       c.first_table_cap = (uint64_t)value;
-    }
-    else throw std::invalid_argument(std::string("unknown option: ") + name);
+    } else if (std::string(name) == "append_chunk") {
+      require(value >= 0, "append_chunk must be >= 0");
+      c.append_chunk = (uint64_t)value;
+    } else throw std::invalid_argument(std::string("unknown option: ") + name);
   });
 }
 
@@ -664,6 +666,26 @@ gfz_status gfz_server_wait(gfz_server *s, uint64_t ticket, const char **line, si
     require(s && line && len, "NULL argument");
     size_t n = 0;
     *line = s->s->wait(ticket, &n, latency_ms);
+    *len = n;
+  });
+}
+
+gfz_status gfz_server_request_times(gfz_server *s, uint64_t ticket, double *queue_ms, double *service_ms,
+                                    uint32_t *batch_size) {
+  return guard([&] {
+    require(s, "NULL argument");
+    s->s->times(ticket, queue_ms, service_ms, batch_size);
+  });
+}
+
+gfz_status gfz_server_collect(gfz_server *s, uint64_t ticket, size_t *len, double *latency_ms, double *queue_ms,
+                              double *service_ms, uint32_t *batch_size) {
+  return guard([&] {
+    require(s && len, "NULL argument");
+    size_t n = 0;
+    s->s->wait(ticket, &n, latency_ms);
+    s->s->times(ticket, queue_ms, service_ms, batch_size);
+    s->s->release(ticket);
     *len = n;
   });
 }

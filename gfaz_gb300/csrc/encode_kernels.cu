@@ -833,6 +833,8 @@ __global__ void k_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlo
 // ---------------------------------------------------------------------------
 // Append encoder
 // ---------------------------------------------------------------------------
+// Rule i of [lo, hi) gets id start + i - lo under its key pack(first,
+// second).
 __global__ void k_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi,
                                    uint32_t start, PairTable tab, DevStatus *status) {
   const uint32_t mask = (uint32_t)(tab.cap - 1);
@@ -904,6 +906,97 @@ __global__ void k_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, u
     len[t] = top;
   }
   (void)status;
+}
+
+// One push of the stack pass with stack top t and pushed symbol x: the
+// forward key first, then the reversed key (path_encoder.cpp:40-75).
+__device__ __forceinline__ bool stack_match(const PairTable &tab, int32_t t, int32_t x, int32_t &r) {
+  const unsigned long long k = pack2(t, x);
+  uint32_t id;
+  if (table_find(tab, k, id)) {
+    r = (int32_t)id;
+    return true;
+  }
+  if (table_find(tab, rev2(k), id)) {
+    r = neg32((int32_t)id);
+    return true;
+  }
+  return false;
+}
+
+// Chunked stack pass.  The pass only ever looks at the stack top and the
+// pushed symbol, so its state is the top alone: after symbol p it is either
+// p's own value (p did not pair, and the previous top went to the output)
+// or the rule the pair made.  Each chunk runs from its first symbol as if
+// the incoming top did not pair with it; top[p] is the top after p and bit 0
+// of fl[p] says that p did not pair (it emitted the previous top).  Bit 1
+// of fl[p] marks the last symbol of a traversal.  Chunk bounds carry flags
+// in bit 63 (kChunkEdge): cs = first chunk of a traversal, ce = last chunk.
+
+__global__ void k_stack_spec(const int32_t *s, const uint64_t *cs, const uint64_t *ce, uint64_t nchunks,
+                             PairTable tab, int32_t *top, uint8_t *fl) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < nchunks;
+       c += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t a = cs[c] & ~kChunkEdge, b = ce[c] & ~kChunkEdge;
+    const bool first = cs[c] & kChunkEdge, last = ce[c] & kChunkEdge;
+    if (b <= a) continue;
+    int32_t cur = s[a];
+    top[a] = cur;
+    fl[a] = (first ? 0 : 1) | (last && b == a + 1 ? 2 : 0);
+    for (uint64_t p = a + 1; p < b; ++p) {
+      const int32_t x = s[p];
+      int32_t r;
+      const bool m = stack_match(tab, cur, x, r);
+      cur = m ? r : x;
+      top[p] = cur;
+      fl[p] = (m ? 0 : 1) | (last && p + 1 == b ? 2 : 0);
+    }
+  }
+}
+
+// A chunk whose first symbol does pair with the true incoming top (the
+// previous chunk's last top, final once that chunk converged) runs the pass
+// again until its top equals the speculative top; from there on the chunk
+// is already right.  A chunk that reaches its end first counts in *nonconv
+// and the whole pass must be redone another way.
+__global__ void k_stack_fix(const int32_t *s, const uint64_t *cs, const uint64_t *ce, uint64_t nchunks,
+                            PairTable tab, int32_t *top, uint8_t *fl, unsigned long long *nonconv) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < nchunks;
+       c += (uint64_t)gridDim.x * blockDim.x) {
+    if (cs[c] & kChunkEdge) continue;
+    const uint64_t a = cs[c], b = ce[c] & ~kChunkEdge;
+    if (b <= a) continue;
+    int32_t cur;
+    if (!stack_match(tab, top[a - 1], s[a], cur)) continue;
+    fl[a] &= 2;
+    if (cur == top[a]) continue;
+    top[a] = cur;
+    uint64_t p = a + 1;
+    for (; p < b; ++p) {
+      const int32_t x = s[p];
+      int32_t r;
+      const bool m = stack_match(tab, cur, x, r);
+      const int32_t nxt = m ? r : x;
+      fl[p] = (fl[p] & 2) | (m ? 0 : 1);
+      if (nxt == top[p]) break;
+      top[p] = nxt;
+      cur = nxt;
+    }
+    if (p == b) atomicAdd(nonconv, 1ull);
+  }
+}
+
+// keep[p] = 1 when top[p] goes to the output: p is the last symbol of its
+// traversal, or the next symbol did not pair.
+__global__ void k_stack_keep(const uint8_t *fl, uint64_t n, uint32_t *keep) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x)
+    keep[p] = ((fl[p] & 2) || (p + 1 < n && (fl[p + 1] & 1))) ? 1u : 0u;
+}
+
+__global__ void k_stack_scatter(const int32_t *top, const uint32_t *keep, const uint64_t *pos, uint64_t n,
+                                int32_t *out) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x)
+    if (keep[p]) out[pos[p]] = top[p];
 }
 
 __global__ void k_gather_ranges(const int32_t *src, const uint64_t *starts, const uint64_t *dst_off, uint64_t nr,
@@ -1078,6 +1171,24 @@ void launch_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, uint64_
                          DevStatus *status, cudaStream_t st) {
   if (!ntrav) return;
   k_stack_encode<<<grid_for(ntrav, 32), 32, 0, st>>>(s, off, len, ntrav, tab, status);
+}
+
+void launch_stack_chunks(const int32_t *s, const uint64_t *cs, const uint64_t *ce, uint64_t nchunks, PairTable tab,
+                         int32_t *top, uint8_t *fl, unsigned long long *nonconv, cudaStream_t st) {
+  if (!nchunks) return;
+  k_stack_spec<<<grid_for(nchunks, 64), 64, 0, st>>>(s, cs, ce, nchunks, tab, top, fl);
+  k_stack_fix<<<grid_for(nchunks, 64), 64, 0, st>>>(s, cs, ce, nchunks, tab, top, fl, nonconv);
+}
+
+void launch_stack_keep(const uint8_t *fl, uint64_t n, uint32_t *keep, cudaStream_t st) {
+  if (!n) return;
+  k_stack_keep<<<grid_for(n, kBlock), kBlock, 0, st>>>(fl, n, keep);
+}
+
+void launch_stack_scatter(const int32_t *top, const uint32_t *keep, const uint64_t *pos, uint64_t n, int32_t *out,
+                          cudaStream_t st) {
+  if (!n) return;
+  k_stack_scatter<<<grid_for(n, kBlock), kBlock, 0, st>>>(top, keep, pos, n, out);
 }
 
 void launch_gather_ranges(const int32_t *src, const uint64_t *starts, const uint64_t *dst_off, uint64_t nr,

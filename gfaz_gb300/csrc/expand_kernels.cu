@@ -411,89 +411,90 @@ __device__ __forceinline__ unsigned long long step_offset(const ExpandSource &E,
   return o + steps_text<DELTA>(r, rtot, sdig[i], 0, (uint32_t)(p - start), pmode, E.rules.rpre);
 }
 
+// Text offset of the first step of every output tile: where the tile's
+// text begins (before the line prefix when that step opens a traversal).
+template <int DELTA>
+__global__ void k_tile_text_off(ExpandSource E, TextSource T, const uint64_t *__restrict__ soff,
+                                const uint8_t *__restrict__ sdig, uint64_t ntiles, uint32_t tile_steps,
+                                uint64_t *__restrict__ toff) {
+  const bool pmode = T.meta.mode == 0;
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < ntiles;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = E.tile_sym[k];
+    const int4 r = E.rec[i];
+    toff[k] = step_offset<DELTA>(E, T, soff, sdig, i, r, E.pos[i], k * tile_steps, pmode);
+  }
+}
+
+// One output tile per block: the steps' values from the rule prefix buffer,
+// each thread's text length from its values, a block scan for the thread
+// offsets, the text packed into 32-bit words in shared memory and written
+// out with 16-byte stores.  toff[tile] (k_tile_text_off) places the tile;
+// its end must meet the next tile's start (or the body end), else the
+// per-symbol lengths and the text disagree and kErrLength is raised.
 template <int BLOCK, int ITEMS, int DELTA>
-__global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ soff,
-                                                      const uint8_t *__restrict__ sdig, char *__restrict__ text) {
+__global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ toff,
+                                                      char *__restrict__ text) {
+  static_assert(ITEMS <= 8, "digit counts are packed 4 bits per step");
   constexpr uint32_t TILE = BLOCK * ITEMS;
   constexpr uint32_t kWords = kTextBuf / 4 + 8;
   __shared__ __align__(16) uint32_t sbuf[kWords];
   __shared__ SymStage S;
-  __shared__ unsigned long long s_t0, s_t1;
   const uint64_t tile = blockIdx.x;
   const bool pmode = T.meta.mode == 0;
+  const uint32_t per = pmode ? 2u : 1u;
   stage_symbols<BLOCK>(E, tile, S);
   const uint64_t P0 = tile * TILE;
-  if (threadIdx.x == 0) {
-    // text range of the tile: [offset of its first step, offset of the next tile's)
-    const uint64_t i0 = E.tile_sym[tile];
-    const int4 r0 = E.rec[i0];
-    s_t0 = step_offset<DELTA>(E, T, soff, sdig, i0, r0, E.pos[i0], P0, pmode);
-    const uint64_t P1 = P0 + TILE;
-    if (P1 >= E.total) {
-      s_t1 = soff[E.m];
-    } else {
-      const uint64_t i1 = E.tile_sym[tile + 1];
-      const int4 r1 = E.rec[i1];
-      s_t1 = step_offset<DELTA>(E, T, soff, sdig, i1, r1, E.pos[i1], P1, pmode);
-    }
-  }
   const uint64_t p0 = P0 + (uint64_t)threadIdx.x * ITEMS;
   int32_t val[ITEMS];
   const uint32_t cnt = thread_values<ITEMS, DELTA>(E, S, tile, p0, val);
-  // my first symbol again, for my text offset and the shared digit counts
-  uint64_t i = 0, start = 0, end = 0;
-  int4 r = make_int4(0, 0, 0, 0);
-  unsigned long long my = 0;
-  if (cnt) {
-    if (S.staged) {
-      uint32_t lo = 0, hi = S.cnt - 1;
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (S.pos[mid] <= p0) lo = mid; else hi = mid - 1;
-      }
-      i = S.lo + lo;
-      start = S.pos[lo];
-      end = S.pos[lo + 1];
-      r = S.rec[lo];
-    } else {
-      uint64_t lo = E.tile_sym[tile], hi = E.tile_sym[tile + 1];
-      while (lo < hi) {
-        const uint64_t mid = (lo + hi + 1) >> 1;
-        if (E.pos[mid] <= p0) lo = mid; else hi = mid - 1;
-      }
-      i = lo;
-      start = E.pos[lo];
-      end = E.pos[lo + 1];
-      r = E.rec[lo];
-    }
-    my = step_offset<DELTA>(E, T, soff, sdig, i, r, start, p0, pmode);
-  }
-  __syncthreads();
-  const unsigned long long t0 = s_t0, total = s_t1 - s_t0;
   const uint32_t hd = cnt ? (uint32_t)((((unsigned long long)T.heads[(p0 >> 5) + 1] << 32) | T.heads[p0 >> 5]) >> (p0 & 31)) : 0u;
+  // text bytes of my steps, line pieces included
+  uint32_t ndp = 0;  // digit counts, 4 bits per step
+  unsigned long long len = 0;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    if ((uint32_t)k < cnt) {
+      const uint32_t nd = dec_digits(abs32(val[k]));
+      ndp |= nd << (4 * k);
+      len += nd + per;
+    }
+  }
+  const uint32_t edges = cnt ? (hd & ((2u << cnt) - 1u)) : 0u;
+  if (edges) {
+    for (int k = 0; k < ITEMS; ++k) {
+      if ((uint32_t)k >= cnt) break;
+      const bool fst = (hd >> k) & 1u, lst = (hd >> (k + 1)) & 1u;
+      if (fst | lst) {
+        const uint64_t t = trav_of(T.off, T.ntrav, p0 + k);
+        if (fst) len += pre_len(T, t);
+        if (lst) len += suf_len(T, t) - (pmode ? 1ull : 0ull);
+      }
+    }
+  }
+  unsigned long long total;
+  const unsigned long long my = block_excl_sum<BLOCK>(len, total);
+  const unsigned long long t0 = toff[tile];
+  if (threadIdx.x == 0) {
+    const unsigned long long want = tile + 1 < gridDim.x ? toff[tile + 1] : T.cap;
+    if (t0 + total != want) atomicOr(T.err, kErrLength);
+  }
   if (total <= kTextBuf) {
     const uint32_t nw = (uint32_t)(total / 4) + 2;
     for (uint32_t k = threadIdx.x; k < nw; k += BLOCK) sbuf[k] = 0;
     __syncthreads();
     WordWriter wr;
-    wr.init(sbuf, cnt ? (uint32_t)(my - t0) : 0u, nw);
-    uint32_t dig = sdig[i];
+    wr.init(sbuf, (uint32_t)my, nw);
 #pragma unroll 1  // a rolled loop keeps the kernel inside the instruction cache
     for (int k = 0; k < ITEMS; ++k) {
       if ((uint32_t)k < cnt) {
-        const uint64_t p = p0 + k;
-        if (p >= end) {  // next symbol
-          ++i;
-          end = E.pos[i + 1];
-          dig = sdig[i];
-        }
         const bool fst = (hd >> k) & 1u, lst = (hd >> (k + 1)) & 1u;
         uint64_t t = 0;
-        if (fst | lst) t = trav_of(T.off, T.ntrav, p);
+        if (fst | lst) t = trav_of(T.off, T.ntrav, p0 + k);
         if (fst)
           for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) wr.put((uint8_t)T.meta.blob[q], 1);
         const int32_t v = val[k];
-        const uint32_t av = abs32(v), nd = dig ? dig : dec_digits(av);
+        const uint32_t av = abs32(v), nd = (ndp >> (4 * k)) & 15u;
         if (pmode) {
           wr.put_dec(av, nd);
           const uint32_t mark = v < 0 ? '-' : '+';
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource
   }
   // a tile with very long line pieces: bytes straight to global memory
   // (each thread's bytes end where the next thread's begin)
-  unsigned long long o = my;
+  unsigned long long o = t0 + my;
   char dec[10];
   auto put = [&](char c) {
     if (o < T.cap) text[o] = c;
@@ -532,7 +533,7 @@ __global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource
       if (fst)
         for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) put(T.meta.blob[q]);
       const int32_t v = val[k];
-      const uint32_t av = abs32(v), nd = dec_digits(av);
+      const uint32_t av = abs32(v), nd = (ndp >> (4 * k)) & 15u;
       put_dec(dec, av, nd);
       if (!pmode) put(v < 0 ? '<' : '>');
       for (uint32_t q = 0; q < nd; ++q) put(dec[q]);
@@ -547,6 +548,38 @@ __global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Line ends
+// ---------------------------------------------------------------------------
+// Positions of the '\n' bytes of text[0, n), unordered: out[0] counts them
+// all, out[1 .. cap] holds the first cap found.  16 bytes per thread and
+// step; the text buffer starts 16-byte aligned.
+__global__ void k_find_newlines(const char *__restrict__ text, uint64_t n, unsigned long long *out, uint64_t cap) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * 16;
+  for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * 16; i < n; i += stride) {
+    if (i + 16 <= n) {
+      const uint4 v = *reinterpret_cast<const uint4 *>(text + i);
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t eq = __vcmpeq4(w[k], 0x0A0A0A0Au);
+        while (eq) {
+          const int b = (__ffs(eq) - 1) >> 3;
+          eq &= ~(0xFFu << (8 * b));
+          const unsigned long long at = atomicAdd(&out[0], 1ull);
+          if (at < cap) out[1 + at] = i + 4 * k + b;
+        }
+      }
+    } else {
+      for (uint64_t j = i; j < n; ++j)
+        if (text[j] == '\n') {
+          const unsigned long long at = atomicAdd(&out[0], 1ull);
+          if (at < cap) out[1 + at] = j;
+        }
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Launchers
@@ -616,14 +649,29 @@ void launch_symbol_text(const ExpandSource &E, const TextSource &T, int delta, u
     k_symbol_text<0><<<grid_for(E.m, kBlock), kBlock, 0, st>>>(E, T, slen, sdig);
 }
 
-void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
-                       const uint8_t *sdig, char *text, cudaStream_t st) {
+void launch_find_newlines(const char *text, uint64_t n, unsigned long long *out, uint64_t cap, cudaStream_t st) {
+  if (!n) return;
+  k_find_newlines<<<grid_for((n + 15) / 16, kBlock), kBlock, 0, st>>>(text, n, out, cap);
+}
+
+void launch_tile_text_off(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
+                          const uint8_t *sdig, uint64_t *toff, cudaStream_t st) {
   const uint64_t nt = expand_num_tiles(E.total);
   if (!nt) return;
   if (delta)
-    k_text_write<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, soff, sdig, text);
+    k_tile_text_off<1><<<grid_for(nt, kBlock), kBlock, 0, st>>>(E, T, soff, sdig, nt, kExpandTile, toff);
   else
-    k_text_write<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, soff, sdig, text);
+    k_tile_text_off<0><<<grid_for(nt, kBlock), kBlock, 0, st>>>(E, T, soff, sdig, nt, kExpandTile, toff);
+}
+
+void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *toff, char *text,
+                       cudaStream_t st) {
+  const uint64_t nt = expand_num_tiles(E.total);
+  if (!nt) return;
+  if (delta)
+    k_text_write<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, toff, text);
+  else
+    k_text_write<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, toff, text);
 }
 
 }  // namespace gfz

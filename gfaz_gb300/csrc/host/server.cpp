@@ -1,6 +1,7 @@
 // Resident extraction server (see server.h).
 #include "server.h"
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
@@ -38,6 +39,12 @@ Server::~Server() {
   }
   cv_work_.notify_all();
   for (auto &t : threads_) t.join();
+  if (debug_enabled())
+    fprintf(stderr, "[gfaz gb300] server: %llu batches, %llu requests, %llu appends, %llu pageable; host ms: decode %.1f, "
+            "copy %.1f, split %.1f\n",
+            (unsigned long long)stats_.batches, (unsigned long long)stats_.requests,
+            (unsigned long long)stats_.appends, (unsigned long long)stats_.pageable, stats_.decode_ms, stats_.copy_ms,
+            stats_.split_ms);
   for (auto &b : pinned_) {
     if (!b.p) continue;
     if (b.pooled) cudaFreeHost(b.p);
@@ -45,31 +52,53 @@ Server::~Server() {
   }
 }
 
-// A pinned chunk from the pool; when none is free (or n exceeds a chunk),
-// ordinary pageable memory: pinning memory on the request path would stall
-// the worker far longer than a pageable copy.
-int Server::take_pinned(size_t n) {
-  if (n <= kChunk && !free_pinned_.empty()) {
-    const int i = free_pinned_.back();
-    free_pinned_.pop_back();
-    return i;
+// A range of the open pinned chunk; when it is full, the next free chunk
+// opens.  With no free chunk (or n above a chunk), ordinary pageable memory:
+// pinning memory on the request path would stall the worker far longer than
+// a pageable copy.
+int Server::take_pinned(size_t n, char **dst) {
+  const size_t need = (n + 63) & ~size_t(63);
+  if (need <= kChunk) {
+    if (open_pinned_ < 0 || pinned_[open_pinned_].cap - pinned_[open_pinned_].used < need) {
+      if (!free_pinned_.empty()) {
+        const int prev = open_pinned_;
+        open_pinned_ = free_pinned_.back();
+        free_pinned_.pop_back();
+        pinned_[open_pinned_].used = 0;
+        if (prev >= 0 && pinned_[prev].refs == 0) free_pinned_.push_back(prev);
+      }
+    }
+    if (open_pinned_ >= 0 && pinned_[open_pinned_].cap - pinned_[open_pinned_].used >= need) {
+      Pinned &c = pinned_[open_pinned_];
+      *dst = c.p + c.used;
+      c.used += need;
+      c.refs++;
+      return open_pinned_;
+    }
   }
+  stats_.pageable++;
   Pinned b;
-  b.cap = n;
+  b.cap = std::max<size_t>(n, 1);
   b.pooled = false;
-  b.p = static_cast<char *>(std::malloc(n));
+  b.refs = 1;
+  b.p = static_cast<char *>(std::malloc(b.cap));
   if (!b.p) throw std::bad_alloc();
   pinned_.push_back(b);
+  *dst = b.p;
   return (int)pinned_.size() - 1;
 }
 
-void Server::return_pinned(int b) {
-  if (pinned_[b].pooled) {
-    free_pinned_.push_back(b);
+void Server::drop_pinned(int b) {
+  Pinned &c = pinned_[b];
+  if (--c.refs > 0) return;
+  if (!c.pooled) {
+    std::free(c.p);
+    c.p = nullptr;
+    c.cap = 0;
+  } else if (b == open_pinned_) {
+    c.used = 0;  // nothing in it is live: refill from the start
   } else {
-    std::free(pinned_[b].p);
-    pinned_[b].p = nullptr;
-    pinned_[b].cap = 0;
+    free_pinned_.push_back(b);
   }
 }
 
@@ -85,14 +114,6 @@ void Server::load_resident() {
   auto g = std::make_unique<Grammar>(setup_->stream());
   load_traversals(*setup_, c_, *g, np_, nw_);
   prepare_decode(*setup_, *g);
-  rules_first_.resize(g->nrules);
-  rules_second_.resize(g->nrules);
-  if (g->nrules) {
-    cuda_check(cudaMemcpyAsync(rules_first_.data(), g->first.ptr, g->nrules * 4, cudaMemcpyDeviceToHost,
-                               setup_->stream()), "rules download");
-    cuda_check(cudaMemcpyAsync(rules_second_.data(), g->second.ptr, g->nrules * 4, cudaMemcpyDeviceToHost,
-                               setup_->stream()), "rules download");
-  }
   cuda_check(cudaStreamSynchronize(setup_->stream()), "stream sync");
   layers_.clear();
   for (const auto &l : c_.layers) layers_.push_back(Layer{l.k, l.start_id, l.end_id, l.flattened_offset, l.element_count});
@@ -202,13 +223,24 @@ const char *Server::wait(uint64_t ticket, size_t *len, double *latency_ms) {
   return r.result ? r.result : "";
 }
 
+void Server::times(uint64_t ticket, double *queue_ms, double *service_ms, uint32_t *batch_size) {
+  std::lock_guard<std::mutex> lk(mu_);
+  const auto it = reqs_.find(ticket);
+  if (it == reqs_.end() || !it->second.done) throw std::invalid_argument("unknown or unfinished request ticket");
+  const Request &r = it->second;
+  using ms = std::chrono::duration<double, std::milli>;
+  if (queue_ms) *queue_ms = ms(r.ts - r.t0).count();
+  if (service_ms) *service_ms = ms(r.t1 - r.ts).count();
+  if (batch_size) *batch_size = r.batch_size;
+}
+
 void Server::release(uint64_t ticket) {
   std::lock_guard<std::mutex> lk(mu_);
   const auto it = reqs_.find(ticket);
   if (it == reqs_.end() || !it->second.done) throw std::invalid_argument("unknown or unfinished request ticket");
   const int b = it->second.buf;
   reqs_.erase(it);
-  if (b >= 0 && --pinned_[b].refs == 0) return_pinned(b);
+  if (b >= 0) drop_pinned(b);
 }
 
 Server::Stats Server::stats() {
@@ -236,6 +268,8 @@ void Server::worker(int) {
     const Kind kind = reqs_.at(head).kind;
     if (kind == kAppend) {
       queue_.pop_front();
+      reqs_.at(head).ts = std::chrono::steady_clock::now();
+      reqs_.at(head).batch_size = 1;
       lk.unlock();
       std::string err;
       Prepared prep;
@@ -276,6 +310,12 @@ void Server::worker(int) {
       batch.push_back(queue_.front());
       queue_.pop_front();
     }
+    const auto started = std::chrono::steady_clock::now();
+    for (uint64_t t : batch) {
+      Request &r = reqs_.at(t);
+      r.ts = started;
+      r.batch_size = (uint32_t)batch.size();
+    }
     in_use_ += bytes;
     ++in_flight_;
     stats_.batches++;
@@ -312,6 +352,8 @@ void Server::worker(int) {
 }
 
 void Server::run_batch(Context &ctx, Kind kind, const std::vector<uint64_t> &tickets) {
+  using clock = std::chrono::steady_clock;
+  const auto t_start = clock::now();
   cudaStream_t st = ctx.stream();
   const Grammar &R = *g_;
   std::vector<uint64_t> trav;
@@ -362,34 +404,51 @@ void Server::run_batch(Context &ctx, Kind kind, const std::vector<uint64_t> &tic
   const uint64_t n = decode_text(
       ctx, gb, 0, nb, [&](const std::vector<uint64_t> &xoff) { return make_pieces(pre, suf, xoff); },
       kind == kPath ? 0 : 1, text);
+  // line ends: every line is one request and ends in its only '\n'
+  DevVec<unsigned long long> d_nl(st);
+  d_nl.resize(nb + 1);
+  cuda_check(cudaMemsetAsync(d_nl.ptr, 0, sizeof(unsigned long long), st), "line ends");
+  launch_find_newlines(text.ptr, n, d_nl.ptr, nb, st);
+  std::vector<unsigned long long> nl(nb + 1);
+  const auto t_decoded = clock::now();
   int b;
   char *dst;
   {
     std::lock_guard<std::mutex> lk(mu_);
-    b = take_pinned(n + 1);
-    dst = pinned_[b].p;
+    b = take_pinned(n + 1, &dst);
   }
   try {
     if (n) cuda_check(cudaMemcpyAsync(dst, text.ptr, n, cudaMemcpyDeviceToHost, st), "text download");
+    cuda_check(cudaMemcpyAsync(nl.data(), d_nl.ptr, (nb + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               st),
+               "line ends");
     cuda_check(cudaStreamSynchronize(st), "stream sync");
+    if (nl[0] != nb) throw std::runtime_error("extraction text does not hold one line per request");
   } catch (...) {
     std::lock_guard<std::mutex> lk(mu_);
-    return_pinned(b);
+    drop_pinned(b);
     throw;
   }
-  // one line per request, in batch order, each a view into the buffer
+  const auto t_copied = clock::now();
+  std::sort(nl.begin() + 1, nl.end());
+  std::vector<size_t> ends(nb);
+  for (uint64_t k = 0; k < nb; ++k) ends[k] = (size_t)nl[k + 1] + 1;
+  const auto t_split = clock::now();
+  // each line is a view into the buffer holding one reference to it (the
+  // batch's own reference passes to the first)
   std::lock_guard<std::mutex> lk(mu_);
-  pinned_[b].refs = (int)nb;
-  size_t pos = 0;
+  pinned_[b].refs += (int)nb - 1;
   for (uint64_t k = 0; k < nb; ++k) {
-    const char *nl = static_cast<const char *>(std::memchr(dst + pos, '\n', n - pos));
-    const size_t stop = nl ? (size_t)(nl - dst) + 1 : n;
     Request &r = reqs_.at(tickets[k]);
-    r.result = dst + pos;
-    r.result_len = stop - pos;
+    const size_t begin = k ? ends[k - 1] : 0;
+    r.result = dst + begin;
+    r.result_len = ends[k] - begin;
     r.buf = b;
-    pos = stop;
   }
+  using ms = std::chrono::duration<double, std::milli>;
+  stats_.decode_ms += ms(t_decoded - t_start).count();
+  stats_.copy_ms += ms(t_copied - t_decoded).count();
+  stats_.split_ms += ms(t_split - t_copied).count();
 }
 
 // Appends encode with the stored rulebook exactly as add_haplotypes does
@@ -432,15 +491,13 @@ Server::Prepared Server::prepare_append(Context &ctx, uint64_t ticket) {
   const Traversals &tv = p.in.has_paths ? p.in.paths : p.in.walks;
   std::vector<int32_t> steps = tv.steps;
   uint32_t max_abs = 0;
-  append_encode(ctx, rules_first_.data(), rules_second_.data(), rules_first_.size(), layers_, c_.delta_round, steps,
-                tv.offsets, p.lens, max_abs);
+  append_encode(ctx, g_->first.ptr, g_->second.ptr, g_->nrules, layers_, c_.delta_round, steps, tv.offsets, p.lens,
+                max_abs);
   if (!c_.layers.empty() && max_abs >= c_.min_rule_id())
     throw std::runtime_error(std::string(kAddErr) + "delta-encoded appended sequence reaches ID " +
                              std::to_string(max_abs) + ", which collides with the stored rule region starting at " +
                              std::to_string(c_.min_rule_id()));
-  for (uint64_t t = 0; t < tv.size(); ++t)
-    p.add.insert(p.add.end(), steps.begin() + (ptrdiff_t)tv.offsets[t],
-                 steps.begin() + (ptrdiff_t)(tv.offsets[t] + p.lens[t]));
+  p.add = std::move(steps);
   return p;
 }
 

@@ -54,10 +54,18 @@ class Server {
   // release(ticket), with its length in *len; latency_ms = submission to
   // completion.  A failed request rethrows its error and needs no release.
   const char *wait(uint64_t ticket, size_t *len, double *latency_ms);
+  // For a finished request that is not yet released: time queued (submission
+  // to the start of its batch), time in service (batch start to completion)
+  // and the number of requests in its batch.
+  void times(uint64_t ticket, double *queue_ms, double *service_ms, uint32_t *batch_size);
   void release(uint64_t ticket);
 
   struct Stats {
     uint64_t batches = 0, requests = 0, max_batch = 0, appends = 0;
+    uint64_t pageable = 0;  // batches whose text went to pageable memory (pinned pool exhausted)
+    // host wall time summed over batches: gather + expansion + text, text
+    // download, splitting into lines
+    double decode_ms = 0, copy_ms = 0, split_ms = 0;
   };
   Stats stats();
 
@@ -69,23 +77,27 @@ class Server {
     std::string pre, suf;    // line pieces
     std::string append_text;
     uint64_t need = 0;       // admission bytes
-    std::chrono::steady_clock::time_point t0, t1;
+    std::chrono::steady_clock::time_point t0, ts, t1;  // submitted, batch started, done
+    uint32_t batch_size = 0;
     const char *result = nullptr;  // the line, inside `buf`
     size_t result_len = 0;
     int buf = -1;                  // pinned buffer holding the line
     std::string error;
     bool done = false;
   };
-  // Pinned host buffers that batch text lands in; a buffer goes back to the
-  // pool once every line in it is released.
+  // Pinned host chunks that batch text lands in.  Batches take 64-byte
+  // aligned ranges of the open chunk one after another; a chunk is reused
+  // once every range in it was released, so a few slow readers pin only the
+  // chunks holding their own lines.
   struct Pinned {
     char *p = nullptr;
-    size_t cap = 0;
-    int refs = 0;
-    bool pooled = true;  // false: pageable one-off memory (pool empty, or larger than a chunk)
+    size_t cap = 0, used = 0;  // used: bump offset while the chunk is open
+    int refs = 0;              // ranges (lines, or a batch in flight) not yet released
+    bool pooled = true;        // false: pageable one-off memory (pool exhausted, or larger than a chunk)
   };
-  int take_pinned(size_t n);       // mu_ held
-  void return_pinned(int b);       // mu_ held
+  // A range of n bytes holding one reference: the buffer index and the address.
+  int take_pinned(size_t n, char **dst);  // mu_ held
+  void drop_pinned(int b);                // mu_ held: one reference fewer
   void add_pinned_chunk();
 
   void load_resident();                 // (re)build the resident grammar from c_
@@ -110,7 +122,6 @@ class Server {
   std::unique_ptr<Grammar> g_;          // resident grammar (decode side)
   uint64_t np_ = 0, nw_ = 0;
   std::vector<uint64_t> steps_;         // decoded steps per traversal
-  std::vector<int32_t> rules_first_, rules_second_;  // host copy of the rule columns (appends)
   std::vector<Layer> layers_;
   std::unordered_map<std::string, uint64_t> path_index_;
   std::vector<std::string> overlaps_;
@@ -130,7 +141,8 @@ class Server {
   bool stop_ = false;
   Stats stats_;
   std::vector<Pinned> pinned_;
-  std::vector<int> free_pinned_;
+  std::vector<int> free_pinned_;  // pooled chunks holding no range
+  int open_pinned_ = -1;          // the chunk ranges are taken from
   std::vector<std::thread> threads_;
 };
 

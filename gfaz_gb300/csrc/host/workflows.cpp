@@ -984,28 +984,19 @@ void encode_append(Context &ctx, const Compressed &c, const Traversals &tv, std:
                    std::vector<uint32_t> &lens) {
   Grammar g(ctx.stream());
   decode_rule_columns(ctx, c, g);
-  std::vector<int32_t> first(g.nrules), second(g.nrules);
-  if (g.nrules) {
-    cuda_check(cudaMemcpyAsync(first.data(), g.first.ptr, g.nrules * 4, cudaMemcpyDeviceToHost, ctx.stream()), "dl");
-    cuda_check(cudaMemcpyAsync(second.data(), g.second.ptr, g.nrules * 4, cudaMemcpyDeviceToHost, ctx.stream()), "dl");
-    cuda_check(cudaStreamSynchronize(ctx.stream()), "sync");
-  }
   std::vector<Layer> layers;
   for (const auto &l : c.layers) layers.push_back(Layer{l.k, l.start_id, l.end_id, l.flattened_offset, l.element_count});
   std::vector<int32_t> steps = tv.steps;
   std::vector<uint64_t> out_lens;
   uint32_t max_abs = 0;
-  append_encode(ctx, first.data(), second.data(), g.nrules, layers, c.delta_round, steps, tv.offsets, out_lens,
+  append_encode(ctx, g.first.ptr, g.second.ptr, g.nrules, layers, c.delta_round, steps, tv.offsets, out_lens,
                 max_abs);
   if (!c.layers.empty() && max_abs >= c.min_rule_id())
     throw std::runtime_error(std::string(kAddErr) + "delta-encoded appended sequence reaches ID " +
                              std::to_string(max_abs) + ", which collides with the stored rule region starting at " +
                              std::to_string(c.min_rule_id()));
-  for (size_t t = 0; t + 1 < tv.offsets.size(); ++t) {
-    flat.insert(flat.end(), steps.begin() + (ptrdiff_t)tv.offsets[t],
-                steps.begin() + (ptrdiff_t)(tv.offsets[t] + out_lens[t]));
-    lens.push_back((uint32_t)out_lens[t]);
-  }
+  flat.insert(flat.end(), steps.begin(), steps.end());
+  for (size_t t = 0; t + 1 < tv.offsets.size(); ++t) lens.push_back((uint32_t)out_lens[t]);
 }
 
 }  // namespace

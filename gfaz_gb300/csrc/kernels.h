@@ -102,6 +102,20 @@ void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlot *slo
 // [lo, hi) of the decoded columns get ids start .. start + hi - lo).
 void launch_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi,
                              uint32_t start, PairTable tab, DevStatus *status, cudaStream_t st);
+// Chunked stack pass (the same result as the stack encoder below): chunk c
+// covers [cs[c], ce[c]) of one traversal, bit 63 of cs / ce flags the first
+// / last chunk of a traversal.  Writes the stack top after every symbol and
+// per-symbol flags (bit 0: the symbol did not pair, bit 1: last symbol of a
+// traversal); *nonconv counts chunks whose fix-up did not settle (then the
+// result is void).
+constexpr uint64_t kChunkEdge = 1ull << 63;
+void launch_stack_chunks(const int32_t *s, const uint64_t *cs, const uint64_t *ce, uint64_t nchunks, PairTable tab,
+                         int32_t *top, uint8_t *fl, unsigned long long *nonconv, cudaStream_t st);
+// keep[p] = 1 for the stack tops that are output symbols.
+void launch_stack_keep(const uint8_t *fl, uint64_t n, uint32_t *keep, cudaStream_t st);
+// out[pos[p]] = top[p] where keep[p] (pos: exclusive scan of keep).
+void launch_stack_scatter(const int32_t *top, const uint32_t *keep, const uint64_t *pos, uint64_t n, int32_t *out,
+                          cudaStream_t st);
 // Stack encoder, one thread per traversal (sequential within a traversal).
 // Encodes s[off[t] .. off[t] + len[t]) in place and updates len[t].
 void launch_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, uint64_t ntrav, PairTable tab,
@@ -216,7 +230,16 @@ void launch_expand_steps(const ExpandSource &E, int delta, int32_t *out, cudaStr
 // then, with soff = exclusive scan of slen, the text of every output tile.
 void launch_symbol_text(const ExpandSource &E, const TextSource &T, int delta, uint64_t *slen, uint8_t *sdig,
                         cudaStream_t st);
-void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
-                       const uint8_t *sdig, char *text, cudaStream_t st);
+// toff[k]: text offset of output tile k (expand_num_tiles entries), from the
+// per-symbol text offsets soff and shared digit counts sdig.
+void launch_tile_text_off(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
+                          const uint8_t *sdig, uint64_t *toff, cudaStream_t st);
+// The text of every output tile at toff[tile]; T.cap = the body size.
+void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *toff, char *text,
+                       cudaStream_t st);
+// Adds the number of '\n' bytes in text[0, n) (16-byte aligned buffer) to
+// out[0] (zero it first); out[1 .. min(count, cap)] = their positions,
+// unordered.
+void launch_find_newlines(const char *text, uint64_t n, unsigned long long *out, uint64_t cap, cudaStream_t st);
 
 }  // namespace gfz

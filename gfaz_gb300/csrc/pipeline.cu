@@ -50,16 +50,6 @@ uint64_t next_pow2(uint64_t x) {
 
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
 
-// GFA_COMPRESSION_DEBUG=1 (the reference's debug switch) prints per-round
-// grammar statistics to stderr.
-bool debug_enabled() {
-  static int on = -1;
-  if (on < 0) {
-    const char *e = std::getenv("GFA_COMPRESSION_DEBUG");
-    on = (e && e[0] && e[0] != '0') ? 1 : 0;
-  }
-  return on == 1;
-}
 
 struct Table {
   DevVec<PairSlot> slots;
@@ -72,7 +62,27 @@ struct Table {
   }
 };
 
+// Scratch of one greedy replacement pass (per 2048-step tile).
+struct ReplaceWork {
+  explicit ReplaceWork(cudaStream_t st) : tile_trav(st), tword(st), tile_agg(st), tile_state(st) {}
+  DevVec<uint64_t> tile_trav;
+  DevVec<uint32_t> tword;
+  DevVec<unsigned long long> tile_agg, tile_state;
+};
+
 }  // namespace
+
+// GFA_COMPRESSION_DEBUG=1 (the reference's debug switch) prints per-round
+// grammar statistics to stderr.
+bool debug_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = std::getenv("GFA_COMPRESSION_DEBUG");
+    on = (e && e[0] && e[0] != '0') ? 1 : 0;
+  }
+  return on == 1;
+}
+
 
 // ---------------------------------------------------------------------------
 // Context
@@ -220,6 +230,31 @@ void Context::clear_kernel_stats() {
 // ---------------------------------------------------------------------------
 // Compression
 // ---------------------------------------------------------------------------
+// Greedy left-to-right replacement of A[0, n) (traversal offsets offA, head
+// bitmap heads): inside each traversal, a position whose canonical pair is
+// REPEATED in tab and whose predecessor was not replaced becomes
+// +-(temp_base + slot).  Writes B and offB; the output length lands in
+// status u64[2] for the caller to read.
+static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint64_t *offA, uint64_t ntrav,
+                          const uint32_t *heads, PairTable tab, int32_t temp_base, int32_t *B, uint64_t *offB,
+                          ReplaceWork &w) {
+  cudaStream_t st = ctx.stream();
+  DevStatus *ds = ctx.dstatus();
+  const uint64_t tiles = apply_num_tiles(n);
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
+  w.tile_trav.resize(std::max<uint64_t>(tiles, 1));
+  w.tword.resize(std::max<uint64_t>(tiles * 256, 1));
+  w.tile_agg.resize(std::max<uint64_t>(tiles, 1));
+  w.tile_state.resize(std::max<uint64_t>(tiles, 1));
+  GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA, ntrav, n, w.tile_trav.ptr, st));
+  const ApplyScratch sc{w.tword.ptr, w.tile_agg.ptr, w.tile_state.ptr, desc, counter};
+  GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify(A, n, heads, tab, sc, ds, st));
+  GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
+  GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
+              launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, sc, ds, st));
+}
+
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
                        const EncodeParams &p, Grammar &g) {
   cudaStream_t st = ctx.stream();
@@ -267,9 +302,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   Table tab(st);
   DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
   DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st);
-  DevVec<uint64_t> tile_trav(st);
-  DevVec<uint32_t> tword(st);
-  DevVec<unsigned long long> tile_agg(st), tile_state(st);
+  ReplaceWork rw(st);
 
   uint64_t n = N;
   uint64_t prev_distinct = 0;
@@ -309,21 +342,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
       throw std::overflow_error("Compression workflow error: rule id space exhausted");
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
-    const uint64_t tiles = apply_num_tiles(n);
-    uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
-    tile_trav.resize(std::max<uint64_t>(tiles, 1));
-    tword.resize(std::max<uint64_t>(tiles * 256, 1));
-    tile_agg.resize(std::max<uint64_t>(tiles, 1));
-    tile_state.resize(std::max<uint64_t>(tiles, 1));
-    GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, tile_trav.ptr, st));
-    const ApplyScratch w{tword.ptr, tile_agg.ptr, tile_state.ptr, desc, counter};
-    GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n,
-                launch_apply_classify(A.ptr, n, heads.ptr, tab.view(cap), w, ds, st));
-    GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, w, ds, st));
-    GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
-                launch_apply_emit(A.ptr, n, heads.ptr, offA.ptr, ntrav, tile_trav.ptr, tab.view(cap), temp_base,
-                                  B.ptr, offB.ptr, w, ds, st));
+    replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr, rw);
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
     GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, std::max<uint64_t>(repeated, 1), ds, st));
@@ -775,8 +794,11 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   text.resize(std::max<uint64_t>(size, 1));
   text.size = size;
   T.cap = body;
+  DevVec<uint64_t> toff(st);
+  toff.resize(std::max<uint64_t>(expand_num_tiles(P.total), 1));
+  GFZ_TIMED(ctx, "symbol_text", launch_tile_text_off(E, T, g.delta_round, soff.ptr, sdig.ptr, toff.ptr, st));
   GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
-              launch_text_write(E, T, g.delta_round, soff.ptr, sdig.ptr, text.ptr, st));
+              launch_text_write(E, T, g.delta_round, toff.ptr, text.ptr, st));
   if (!pieces.tail.empty())
     cuda_check(cudaMemcpyAsync(text.ptr + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
                "text tail");
@@ -788,7 +810,7 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
 // ---------------------------------------------------------------------------
 // Append encoding
 // ---------------------------------------------------------------------------
-void append_encode(Context &ctx, const int32_t *first, const int32_t *second, uint64_t nrules,
+void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second, uint64_t nrules,
                    const std::vector<Layer> &layers, int delta_round, std::vector<int32_t> &steps,
                    const std::vector<uint64_t> &off, std::vector<uint64_t> &lens, uint32_t &max_abs) {
   cudaStream_t st = ctx.stream();
@@ -797,46 +819,109 @@ void append_encode(Context &ctx, const int32_t *first, const int32_t *second, ui
   DevVec<int32_t> A(st), B(st);
   A.resize(std::max<uint64_t>(N, 1));
   B.resize(std::max<uint64_t>(N, 1));
-  DevVec<uint64_t> d_off(st), d_len(st);
-  d_off.resize(nt + 1);
-  d_len.resize(std::max<uint64_t>(nt, 1));
-  cuda_check(cudaMemcpyAsync(d_off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  DevVec<uint64_t> offA(st), offB(st), d_len(st);
+  offA.resize(nt + 1);
+  offB.resize(nt + 1);
+  cuda_check(cudaMemcpyAsync(offA.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
   if (N) cuda_check(cudaMemcpyAsync(B.ptr, steps.data(), N * 4, cudaMemcpyHostToDevice, st), "upload");
   ctx.reset_status();
   for (int r = 0; r < delta_round; ++r) {
-    GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(B.ptr, A.ptr, N, d_off.ptr, nt, &ctx.dstatus()->aux, st));
+    GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(B.ptr, A.ptr, N, offA.ptr, nt, &ctx.dstatus()->aux, st));
     A.swap(B);
   }
-  // the encoded data lives in B after the swaps
+  A.swap(B);  // the stream to encode is in A
   const DevStatus &s = ctx.read_status();
   max_abs = s.aux;
-  lens.resize(nt);
-  for (uint64_t t = 0; t < nt; ++t) lens[t] = off[t + 1] - off[t];
-  cuda_check(cudaMemcpyAsync(d_len.ptr, lens.data(), nt * 8, cudaMemcpyHostToDevice, st), "upload");
+  std::vector<uint64_t> h_off = off;  // offsets of A
+  uint64_t n = N;
   if (nrules && nt) {
-    DevVec<int32_t> df(st), dsn(st);
-    df.resize(nrules);
-    dsn.resize(nrules);
-    cuda_check(cudaMemcpyAsync(df.ptr, first, nrules * 4, cudaMemcpyHostToDevice, st), "upload");
-    cuda_check(cudaMemcpyAsync(dsn.ptr, second, nrules * 4, cudaMemcpyHostToDevice, st), "upload");
     Table tab(st);
+    DevVec<uint64_t> d_cs(st), d_ce(st), pos(st);
+    DevVec<int32_t> top(st);
+    DevVec<uint8_t> fl(st);
+    DevVec<uint32_t> keep(st);
     for (const Layer &L : layers) {
       const uint64_t count = (uint64_t)(L.end - L.start);
       const uint64_t lo = L.k == 0 ? 0 : L.flat_off / (uint64_t)L.k;
       if (lo + count > nrules) throw std::runtime_error("Add-haplotypes workflow error: rule column is truncated");
+      if (!count || !n) continue;
       const uint64_t cap = next_pow2(std::max<uint64_t>(2 * count + 1024, 1u << 12));
       tab.prepare(cap, st, 0xFFFFFFFFu);
       ctx.reset_status();
       GFZ_TIMED(ctx, "build_rule_table",
-                launch_build_rule_table(df.ptr, dsn.ptr, lo, lo + count, L.start, tab.view(cap), ctx.dstatus(), st));
-      GFZ_TIMED(ctx, "stack_encode",
-                launch_stack_encode(B.ptr, d_off.ptr, d_len.ptr, nt, tab.view(cap), ctx.dstatus(), st));
-      ctx.read_status();
-      ctx.check_status("append encoding");
+                launch_build_rule_table(d_first, d_second, lo, lo + count, L.start, tab.view(cap), ctx.dstatus(), st));
+      // chunked stack pass; a chunk whose fix-up does not settle within
+      // the chunk voids the pass, which is redone with longer chunks and
+      // finally one thread per traversal
+      bool done = false;
+      const std::vector<uint64_t> ladder =
+          ctx.append_chunk ? std::vector<uint64_t>{ctx.append_chunk} : std::vector<uint64_t>{256, 2048, 16384};
+      for (uint64_t C : ladder) {
+        std::vector<uint64_t> cs, ce;
+        for (uint64_t t = 0; t < nt; ++t)
+          for (uint64_t a = h_off[t]; a < h_off[t + 1]; a += C) {
+            const uint64_t b = std::min(a + C, h_off[t + 1]);
+            cs.push_back(a | (a == h_off[t] ? kChunkEdge : 0));
+            ce.push_back(b | (b == h_off[t + 1] ? kChunkEdge : 0));
+          }
+        const uint64_t nc = cs.size();
+        d_cs.resize(std::max<uint64_t>(nc, 1));
+        d_ce.resize(std::max<uint64_t>(nc, 1));
+        cuda_check(cudaMemcpyAsync(d_cs.ptr, cs.data(), nc * 8, cudaMemcpyHostToDevice, st), "upload");
+        cuda_check(cudaMemcpyAsync(d_ce.ptr, ce.data(), nc * 8, cudaMemcpyHostToDevice, st), "upload");
+        top.resize(n);
+        fl.resize(n);
+        ctx.reset_status();
+        GFZ_TIMED(ctx, "stack_chunks", launch_stack_chunks(A.ptr, d_cs.ptr, d_ce.ptr, nc, tab.view(cap), top.ptr,
+                                                           fl.ptr, &ctx.dstatus()->u64[7], st));
+        const DevStatus &sc = ctx.read_status();
+        ctx.check_status("append encoding");
+        if (sc.u64[7]) continue;
+        keep.resize(n);
+        pos.resize(n + 1);
+        GFZ_TIMED(ctx, "stack_pack", launch_stack_keep(fl.ptr, n, keep.ptr, st));
+        uint32_t *counter;
+        unsigned long long *desc = ctx.lookback(excl_scan_tiles(n), &counter);
+        GFZ_TIMED(ctx, "stack_pack", launch_excl_scan_u32(keep.ptr, n, pos.ptr, desc, counter, ctx.dstatus(), st));
+        GFZ_TIMED(ctx, "stack_pack", launch_stack_scatter(top.ptr, keep.ptr, pos.ptr, n, B.ptr, st));
+        GFZ_TIMED(ctx, "stack_pack", (k_gather_pos<<<grid_for(nt + 1, 256), 256, 0, st>>>(pos.ptr, offA.ptr, nt + 1,
+                                                                                            0, offB.ptr)));
+        A.swap(B);
+        offA.swap(offB);
+        cuda_check(cudaMemcpyAsync(h_off.data(), offA.ptr, (nt + 1) * 8, cudaMemcpyDeviceToHost, st), "download");
+        ctx.read_status();
+        ctx.check_status("append encoding");
+        n = h_off[nt];
+        done = true;
+        break;
+      }
+      if (!done) {
+        // the reference's stack pass, one thread per traversal, in place;
+        // then the traversals are packed back to back again
+        std::vector<uint64_t> len(nt);
+        for (uint64_t t = 0; t < nt; ++t) len[t] = h_off[t + 1] - h_off[t];
+        d_len.resize(nt);
+        cuda_check(cudaMemcpyAsync(d_len.ptr, len.data(), nt * 8, cudaMemcpyHostToDevice, st), "upload");
+        GFZ_TIMED(ctx, "stack_encode", launch_stack_encode(A.ptr, offA.ptr, d_len.ptr, nt, tab.view(cap),
+                                                           ctx.dstatus(), st));
+        cuda_check(cudaMemcpyAsync(len.data(), d_len.ptr, nt * 8, cudaMemcpyDeviceToHost, st), "download");
+        ctx.read_status();
+        ctx.check_status("append encoding");
+        std::vector<uint64_t> packed(nt + 1, 0);
+        for (uint64_t t = 0; t < nt; ++t) packed[t + 1] = packed[t] + len[t];
+        cuda_check(cudaMemcpyAsync(offB.ptr, packed.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+        launch_gather_ranges(A.ptr, offA.ptr, offB.ptr, nt, B.ptr, st);
+        A.swap(B);
+        offA.swap(offB);
+        h_off = packed;
+        n = packed[nt];
+      }
     }
   }
-  cuda_check(cudaMemcpyAsync(lens.data(), d_len.ptr, nt * 8, cudaMemcpyDeviceToHost, st), "download");
-  if (N) cuda_check(cudaMemcpyAsync(steps.data(), B.ptr, N * 4, cudaMemcpyDeviceToHost, st), "download");
+  lens.resize(nt);
+  for (uint64_t t = 0; t < nt; ++t) lens[t] = h_off[t + 1] - h_off[t];
+  steps.resize(n);
+  if (n) cuda_check(cudaMemcpyAsync(steps.data(), A.ptr, n * 4, cudaMemcpyDeviceToHost, st), "download");
   cuda_check(cudaStreamSynchronize(st), "stream sync");
 }
 

@@ -17,6 +17,9 @@
 
 namespace gfz {
 
+// GFA_COMPRESSION_DEBUG set (and not "0"): diagnostics on stderr.
+bool debug_enabled();
+
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
@@ -124,6 +127,7 @@ class Context {
   // tuning knobs
   bool warp_dedup = false;
   uint64_t first_table_cap = 0;  // pair-table slots of the first round (0 = automatic)
+  uint64_t append_chunk = 0;     // steps per chunk of the chunked stack pass (0 = the automatic ladder)
 
  private:
   int device_ = 0, sms_ = 152;
@@ -225,9 +229,12 @@ struct Layer {
   uint32_t start, end;
   uint64_t flat_off, count;
 };
-// steps: raw appended traversals (host), encoded in place; lens updated.
-// Returns max |delta| seen (for the collision check).
-void append_encode(Context &ctx, const int32_t *first, const int32_t *second, uint64_t nrules,
+// Encodes appended traversals with a stored rulebook, layer by layer
+// (add_haplotypes_workflow.cpp:336-465 with path_encoder.cpp:31-79).
+// d_first/d_second: the decoded rule columns on the device.  steps: the raw
+// traversals (host, offsets `off`); on return the encoded traversals back
+// to back, lens[t] steps each.  max_abs: max |delta| (collision check).
+void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second, uint64_t nrules,
                    const std::vector<Layer> &layers, int delta_round, std::vector<int32_t> &steps,
                    const std::vector<uint64_t> &off, std::vector<uint64_t> &lens, uint32_t &max_abs);
 

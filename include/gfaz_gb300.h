@@ -70,7 +70,10 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
 /* Tuning switches: "warp_dedup" = warp-level de-duplication of pair inserts
  * (default 0); "first_table_cap" = pair-table slots of the first grammar
  * round, a power of two (default 0 = sized automatically; the table grows
- * when it fills either way). */
+ * when it fills either way); "append_chunk" = steps per chunk of the
+ * chunked append encoder (default 0 = 256, then 2048 and 16384 where a
+ * chunk's fix-up does not settle, then one thread per traversal; any other
+ * value tries that size, then one thread per traversal). */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
@@ -225,7 +228,16 @@ gfz_status gfz_server_submit_append(gfz_server *s, const char *gfa_text, size_t 
  * server's pinned host memory, valid until gfz_server_release(s, ticket);
  * a request that failed returns its error and is released already. */
 gfz_status gfz_server_wait(gfz_server *s, uint64_t ticket, const char **line, size_t *len, double *latency_ms);
+/* For a finished request before its release: the time it waited in the
+ * queue (submission to the start of its batch), the time in service (batch
+ * start to completion) and the number of requests in its batch. */
+gfz_status gfz_server_request_times(gfz_server *s, uint64_t ticket, double *queue_ms, double *service_ms,
+                                    uint32_t *batch_size);
 gfz_status gfz_server_release(gfz_server *s, uint64_t ticket);
+/* Wait, request times and release in one call, for clients that consume
+ * only the size of the line (load generators, health checks). */
+gfz_status gfz_server_collect(gfz_server *s, uint64_t ticket, size_t *len, double *latency_ms, double *queue_ms,
+                              double *service_ms, uint32_t *batch_size);
 gfz_status gfz_server_stats(gfz_server *s, uint64_t *batches, uint64_t *requests, uint64_t *max_batch);
 void gfz_server_destroy(gfz_server *s);
 
