@@ -495,7 +495,24 @@ __global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource
           for (uint64_t q = T.meta.pre_off[t]; q < T.meta.pre_off[t + 1]; ++q) wr.put((uint8_t)T.meta.blob[q], 1);
         const int32_t v = val[k];
         const uint32_t av = abs32(v), nd = (ndp >> (4 * k)) & 15u;
-        if (pmode) {
+        if (nd <= 8) {
+          // the whole step in one append: digits, mark, comma (P) or mark, digits (W)
+          const unsigned long long D = ascii_digits(av, nd);
+          unsigned long long s0;
+          uint32_t s1, len;
+          if (pmode) {
+            const uint32_t tail = (v < 0 ? '-' : '+') | (lst ? 0u : ((uint32_t)',' << 8));
+            const uint32_t sh = 8u * nd;
+            s0 = sh < 64 ? D | ((unsigned long long)tail << sh) : D;
+            s1 = sh > 48 ? (uint32_t)((unsigned long long)tail >> (64u - sh)) : 0u;
+            len = nd + (lst ? 1u : 2u);
+          } else {
+            s0 = (unsigned long long)(v < 0 ? '<' : '>') | (D << 8);
+            s1 = (uint32_t)(D >> 56);
+            len = nd + 1u;
+          }
+          wr.put12(s0, s1, len);
+        } else if (pmode) {
           wr.put_dec(av, nd);
           const uint32_t mark = v < 0 ? '-' : '+';
           if (lst) wr.put(mark, 1);

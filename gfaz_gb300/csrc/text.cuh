@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "digits.h"
+
 namespace gfz {
 
 __device__ __forceinline__ uint32_t dec_digits(uint32_t v) {
@@ -108,13 +110,34 @@ struct WordWriter {
     shared_first = n != 0;
     overflow = false;
   }
-  __device__ __forceinline__ void store(uint32_t word, bool shared) {
-    if (w >= limit) {
+  __device__ __forceinline__ void store(uint32_t word, bool shared) { store_at(w, word, shared); }
+  __device__ __forceinline__ void store_at(uint32_t at, uint32_t word, bool shared) {
+    if (at >= limit) {
       overflow = true;
       return;
     }
-    if (shared) atomicOr(&buf[w], word);
-    else buf[w] = word;
+    if (shared) atomicOr(&buf[at], word);
+    else buf[at] = word;
+  }
+  // Appends len (<= 12) bytes: the low bytes of b0 then of b1 (bytes above
+  // len zero).  Whole words leave with up to three stores.
+  __device__ __forceinline__ void put12(unsigned long long b0, uint32_t b1, uint32_t len) {
+    const uint32_t x0 = (uint32_t)b0, x1 = (uint32_t)(b0 >> 32);
+    const uint32_t sh = 8u * n;
+    const uint32_t w0 = acc | (x0 << sh);
+    const uint32_t w1 = __funnelshift_l(x0, x1, sh);
+    const uint32_t w2 = __funnelshift_l(x1, b1, sh);
+    const uint32_t w3 = __funnelshift_l(b1, 0u, sh);
+    const uint32_t t = n + len, k = t >> 2;
+    if (k >= 1) {
+      store_at(w, w0, shared_first);
+      shared_first = false;
+    }
+    if (k >= 2) store_at(w + 1, w1, false);
+    if (k >= 3) store_at(w + 2, w2, false);
+    w += k;
+    n = t & 3u;
+    acc = k == 0 ? w0 : k == 1 ? w1 : k == 2 ? w2 : w3;
   }
   // Appends the low cnt (<= 4) bytes of x (bytes above cnt must be zero).
   __device__ __forceinline__ void put(uint32_t x, uint32_t cnt) {
