@@ -94,6 +94,8 @@ __global__ void __launch_bounds__(BLOCK) k_max_abs(const int32_t *__restrict__ i
 // Open-addressed pair table (linear probing over 16-byte slots)
 // ---------------------------------------------------------------------------
 constexpr uint32_t kMaxProbe = 4096;
+// Flipping the sign bit makes unsigned order of packed keys their signed order.
+constexpr unsigned long long kSignFlip = 0x8000000000000000ULL;
 
 __device__ __forceinline__ void load_slot(const PairSlot *p, unsigned long long &key, uint32_t &flags) {
   const ulonglong2 w = *reinterpret_cast<const ulonglong2 *>(p);
@@ -537,7 +539,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
                                                       const uint64_t *__restrict__ off, uint64_t ntrav,
                                                       const uint64_t *__restrict__ tile_trav, PairTable tab,
                                                       int32_t temp_base, int32_t *__restrict__ out,
-                                                      uint64_t *__restrict__ new_off, DevStatus *status) {
+                                                      uint64_t *__restrict__ new_off, uint32_t *used_bits,
+                                                      DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
   static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
@@ -627,14 +630,18 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
     }
     *reinterpret_cast<uint4 *>(&lidx[j0]) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
     // rules chosen here whose slot was not yet flagged used: one flag update
-    // per distinct slot per warp (frequent pairs hit one slot from every lane)
+    // per distinct slot per warp (frequent pairs hit one slot from every
+    // lane), mirrored into the bitmap of used slots
     if (__any_sync(0xffffffffu, need != 0)) {
 #pragma unroll
       for (int k = 0; k < ITEMS; ++k) {
         const bool nk = (need >> k) & 1u;
         if (__any_sync(0xffffffffu, nk)) {
           const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
-          if (nk && (peers & lanemask_lt()) == 0) atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+          if (nk && (peers & lanemask_lt()) == 0) {
+            atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+            atomicOr(&used_bits[slot[k] >> 5], 1u << (slot[k] & 31));
+          }
         }
       }
     }
@@ -663,37 +670,50 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
 }
 
 // ---------------------------------------------------------------------------
-// Used-rule collection, radix sort, id assignment, remap
+// Used-rule collection
 // ---------------------------------------------------------------------------
-constexpr unsigned long long kSignFlip = 0x8000000000000000ULL;
-
-__global__ void k_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
+// (key with the sign bit flipped, slot) of every slot set in the used
+// bitmap, in no particular order; the count lands in status->u64[3] and
+// entries beyond cap_out are dropped with kErrLength.
+__global__ void k_collect_used(const uint32_t *__restrict__ bits, uint64_t words, PairTable tab,
+                               unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
                                DevStatus *status) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tab.cap;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    unsigned long long key;
-    uint32_t fl;
-    load_slot(&tab.slots[i], key, fl);
-    const bool used = (fl & kFlagUsed) != 0;
+  for (uint64_t wi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wi < words;
+       wi += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t b = bits[wi];
     const uint32_t act = __activemask();
-    const uint32_t m = __ballot_sync(act, used);
-    if (!m) continue;
-    const int leader = __ffs(m) - 1;
-    unsigned long long basepos = 0;
-    if ((int)(threadIdx.x & 31) == leader) basepos = atomicAdd(&status->u64[3], (unsigned long long)__popc(m));
-    basepos = __shfl_sync(act, basepos, leader);
-    if (used) {
-      const uint64_t p = basepos + __popc(m & lanemask_lt());
-      if (p < cap_out) {
-        keys_out[p] = key ^ kSignFlip;
-        slots_out[p] = (uint32_t)i;
+    const uint32_t cnt = __popc(b);
+    // warp-aggregated reservation of this lane's cnt entries
+    uint32_t incl = cnt;
+    const int lane = threadIdx.x & 31;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t o = __shfl_up_sync(act, incl, d);
+      if (lane >= d && ((act >> (lane - d)) & 1u)) incl += o;
+    }
+    const int last = 31 - __clz(act);
+    const uint32_t wsum = __shfl_sync(act, incl, last);
+    if (!wsum) continue;
+    unsigned long long base = 0;
+    if (lane == last) base = atomicAdd(&status->u64[3], (unsigned long long)wsum);
+    base = __shfl_sync(act, base, last) + (incl - cnt);
+    while (b) {
+      const uint32_t j = (uint32_t)__ffs(b) - 1;
+      b &= b - 1;
+      const uint64_t slot = wi * 32 + j;
+      if (base < cap_out) {
+        keys_out[base] = tab.slots[slot].key ^ kSignFlip;
+        slots_out[base] = (uint32_t)slot;
       } else {
         atomicOr(&status->err, kErrLength);
       }
+      ++base;
     }
   }
 }
 
+// ---------------------------------------------------------------------------
+// Radix sort of the used rules, id assignment, remap
+// ---------------------------------------------------------------------------
 __global__ void k_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status) {
   unsigned long long o = 0, a = ~0ULL;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -1104,17 +1124,18 @@ void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, c
 
 void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
                        const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                       const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+                       uint32_t *used_bits, const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
   if (!n) return;
   auto k = k_apply_emit<kBlock, kApplyItems>;
   k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), w.tword,
                                                                        w.tile_agg, w.state, off, ntrav, tile_trav,
-                                                                       tab, temp_base, out, new_off, status);
+                                                                       tab, temp_base, out, new_off, used_bits, status);
 }
 
-void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
-                         DevStatus *status, cudaStream_t st) {
-  k_collect_used<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, keys_out, slots_out, cap_out, status);
+void launch_collect_used(const uint32_t *bits, uint64_t cap, PairTable tab, unsigned long long *keys_out,
+                         uint32_t *slots_out, uint64_t cap_out, DevStatus *status, cudaStream_t st) {
+  const uint64_t words = (cap + 31) / 32;
+  k_collect_used<<<grid_for(words, kBlock), kBlock, 0, st>>>(bits, words, tab, keys_out, slots_out, cap_out, status);
 }
 
 void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status, cudaStream_t st) {

@@ -65,19 +65,22 @@ struct ApplyScratch {
 void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
                            DevStatus *status, cudaStream_t st);
 void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+// Emit also sets bit `slot` of used_bits (cap bits, zeroed) for every slot
+// it flags used.
 void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
                        const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                       const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+                       uint32_t *used_bits, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
 uint64_t apply_num_tiles(uint64_t n);
+// (key with the sign bit flipped, slot) of every slot set in the used bitmap
+// (cap bits), in no particular order; count in status->u64[3], entries
+// beyond cap_out dropped with kErrLength.
+void launch_collect_used(const uint32_t *bits, uint64_t cap, PairTable tab, unsigned long long *keys_out,
+                         uint32_t *slots_out, uint64_t cap_out, DevStatus *status, cudaStream_t st);
 uint64_t apply_state_blocks(uint64_t n);
 // tile_trav[k] = first traversal t with off[t] >= k * (apply tile), for the
 // apply_num_tiles(n) tiles.
 void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st);
 
-// Appends (transformed key, slot) of every used slot; count in status->u64[3].
-// Outputs beyond cap_out entries are dropped and flag kErrLength.
-void launch_collect_used(PairTable tab, unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
-                         DevStatus *status, cudaStream_t st);
 
 // Stable LSD radix sort of (u64 key, u32 value) pairs on the given byte
 // positions (bit i of byte_mask = sort on byte i).  Ping-pongs between the

@@ -233,11 +233,12 @@ void Context::clear_kernel_stats() {
 // Greedy left-to-right replacement of A[0, n) (traversal offsets offA, head
 // bitmap heads): inside each traversal, a position whose canonical pair is
 // REPEATED in tab and whose predecessor was not replaced becomes
-// +-(temp_base + slot).  Writes B and offB; the output length lands in
+// +-(temp_base + slot).  Writes B and offB and sets the bit of every used
+// slot in used_bits (zeroed, tab.cap bits); the output length lands in
 // status u64[2] for the caller to read.
 static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint64_t *offA, uint64_t ntrav,
                           const uint32_t *heads, PairTable tab, int32_t temp_base, int32_t *B, uint64_t *offB,
-                          ReplaceWork &w) {
+                          uint32_t *used_bits, ReplaceWork &w) {
   cudaStream_t st = ctx.stream();
   DevStatus *ds = ctx.dstatus();
   const uint64_t tiles = apply_num_tiles(n);
@@ -252,7 +253,7 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
   GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify(A, n, heads, tab, sc, ds, st));
   GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
   GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
-              launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, sc, ds, st));
+              launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, used_bits, sc, ds, st));
 }
 
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
@@ -301,7 +302,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   DevVec<long long> rules(st);
   Table tab(st);
   DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
-  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st);
+  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st), used_bits(st);
   ReplaceWork rw(st);
 
   uint64_t n = N;
@@ -342,16 +343,21 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
       throw std::overflow_error("Compression workflow error: rule id space exhausted");
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
-    replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr, rw);
+    used_bits.resize((cap + 31) / 32);
+    cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
+    replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr,
+                  used_bits.ptr, rw);
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
-    GFZ_TIMED_B(ctx, "collect_used", 4.0 * cap, launch_collect_used(tab.view(cap), ukeys.ptr, uslots.ptr, std::max<uint64_t>(repeated, 1), ds, st));
+    GFZ_TIMED_B(ctx, "collect_used", cap / 8.0,
+                launch_collect_used(used_bits.ptr, cap, tab.view(cap), ukeys.ptr, uslots.ptr,
+                                    std::max<uint64_t>(repeated, 1), ds, st));
     const DevStatus &s1 = ctx.read_status();
     ctx.check_status("apply");
     const uint64_t n_out = s1.u64[2];
     const uint64_t U = s1.u64[3];
-    ctx.add_bytes("apply_emit", 4.0 * n_out);
     ctx.add_bytes("collect_used", 12.0 * U);
+    ctx.add_bytes("apply_emit", 4.0 * n_out);
     if (U == 0) break;  // no rule used: stop all rounds
     ukeys_tmp.resize(U);
     uslots_tmp.resize(U);
