@@ -673,11 +673,14 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
 // Used-rule collection
 // ---------------------------------------------------------------------------
 // (key with the sign bit flipped, slot) of every slot set in the used
-// bitmap, in no particular order; the count lands in status->u64[3] and
+// bitmap, in no particular order; the count lands in status->u64[3], the OR
+// and AND of the keys in u64[4] / u64[5] (u64[5] preset to all ones), and
 // entries beyond cap_out are dropped with kErrLength.
-__global__ void k_collect_used(const uint32_t *__restrict__ bits, uint64_t words, PairTable tab,
-                               unsigned long long *keys_out, uint32_t *slots_out, uint64_t cap_out,
-                               DevStatus *status) {
+__global__ void __launch_bounds__(kBlock) k_collect_used(const uint32_t *__restrict__ bits, uint64_t words,
+                                                         PairTable tab, unsigned long long *keys_out,
+                                                         uint32_t *slots_out, uint64_t cap_out, DevStatus *status) {
+  unsigned long long o = 0, a = ~0ull;  // this thread's OR / AND of the keys it wrote
+  const int lane = threadIdx.x & 31;
   for (uint64_t wi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wi < words;
        wi += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t b = bits[wi];
@@ -685,10 +688,9 @@ __global__ void k_collect_used(const uint32_t *__restrict__ bits, uint64_t words
     const uint32_t cnt = __popc(b);
     // warp-aggregated reservation of this lane's cnt entries
     uint32_t incl = cnt;
-    const int lane = threadIdx.x & 31;
     for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t o = __shfl_up_sync(act, incl, d);
-      if (lane >= d && ((act >> (lane - d)) & 1u)) incl += o;
+      const uint32_t v = __shfl_up_sync(act, incl, d);
+      if (lane >= d && ((act >> (lane - d)) & 1u)) incl += v;
     }
     const int last = 31 - __clz(act);
     const uint32_t wsum = __shfl_sync(act, incl, last);
@@ -700,8 +702,11 @@ __global__ void k_collect_used(const uint32_t *__restrict__ bits, uint64_t words
       const uint32_t j = (uint32_t)__ffs(b) - 1;
       b &= b - 1;
       const uint64_t slot = wi * 32 + j;
+      const unsigned long long key = tab.slots[slot].key ^ kSignFlip;
+      o |= key;
+      a &= key;
       if (base < cap_out) {
-        keys_out[base] = tab.slots[slot].key ^ kSignFlip;
+        keys_out[base] = key;
         slots_out[base] = (uint32_t)slot;
       } else {
         atomicOr(&status->err, kErrLength);
@@ -709,108 +714,136 @@ __global__ void k_collect_used(const uint32_t *__restrict__ bits, uint64_t words
       ++base;
     }
   }
+  // one OR / AND per block
+  __shared__ unsigned long long s_o[kBlock / 32], s_a[kBlock / 32];
+  for (int d = 16; d > 0; d >>= 1) {
+    o |= __shfl_xor_sync(0xffffffffu, o, d);
+    a &= __shfl_xor_sync(0xffffffffu, a, d);
+  }
+  if (lane == 0) {
+    s_o[threadIdx.x >> 5] = o;
+    s_a[threadIdx.x >> 5] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kBlock / 32; ++w) {
+      o |= s_o[w];
+      a &= s_a[w];
+    }
+    if (o) atomicOr(&status->u64[4], o);
+    if (~a) atomicAnd(&status->u64[5], a);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Radix sort of the used rules, id assignment, remap
 // ---------------------------------------------------------------------------
-__global__ void k_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status) {
-  unsigned long long o = 0, a = ~0ULL;
+// One-sweep LSD radix sort of (u64 key, u32 value) pairs, one kernel per
+// byte pass.  Every tile of kSortTile keys ranks its keys stably in shared
+// memory, publishes its 256 digit counts, looks back over the earlier tiles
+// digit by digit (thread d follows digit d) and scatters; the digit bases
+// come from one histogram of all sorted bytes taken before the first pass.
+constexpr int kSortItems = 8;
+constexpr uint32_t kSortTile = kBlock * kSortItems;
+
+// hist[b * 256 + d] += number of keys whose byte b is d, for the bytes in
+// byte_mask (hist zeroed beforehand).
+__global__ void __launch_bounds__(kBlock) k_sort_hist(const unsigned long long *__restrict__ keys, uint64_t n,
+                                                      uint32_t byte_mask, uint32_t *hist) {
+  __shared__ uint32_t cnt[8 * 256];
+  for (uint32_t i = threadIdx.x; i < 8 * 256; i += kBlock) cnt[i] = 0;
+  __syncthreads();
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    o |= keys[i];
-    a &= keys[i];
-  }
-  for (int d = 16; d > 0; d >>= 1) {
-    o |= __shfl_xor_sync(0xffffffffu, o, d);
-    a &= __shfl_xor_sync(0xffffffffu, a, d);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicOr(&status->u64[4], o);
-    atomicAnd(&status->u64[5], a);
-  }
-}
-
-constexpr int kRadixItems = 8;
-constexpr uint32_t kRadixChunk = kBlock * kRadixItems;
-
-__global__ void __launch_bounds__(kBlock) k_radix_hist(const unsigned long long *keys, uint64_t n, int shift,
-                                                       uint32_t *hist, uint32_t nb) {
-  __shared__ uint32_t cnt[256];
-  cnt[threadIdx.x] = 0;
-  __syncthreads();
-  const uint64_t b0 = (uint64_t)blockIdx.x * kRadixChunk;
-  for (int it = 0; it < kRadixItems; ++it) {
-    const uint64_t i = b0 + it * kBlock + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xFF], 1u);
+    const unsigned long long k = keys[i];
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if ((byte_mask >> b) & 1u) atomicAdd(&cnt[b * 256 + (uint32_t)((k >> (8 * b)) & 0xFF)], 1u);
   }
   __syncthreads();
-  hist[(uint64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+  for (uint32_t i = threadIdx.x; i < 8 * 256; i += kBlock)
+    if (cnt[i]) atomicAdd(&hist[i], cnt[i]);
 }
 
-// Exclusive scan of hist[0..e) in place by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_hist(uint32_t *hist, uint64_t e) {
-  __shared__ uint32_t part[1024];
-  const uint64_t per = (e + 1023) / 1024;
-  const uint64_t lo = threadIdx.x * per, hi = min(e, lo + per);
-  uint32_t sum = 0;
-  for (uint64_t i = lo; i < hi; ++i) sum += hist[i];
-  part[threadIdx.x] = sum;
-  __syncthreads();
-  for (int d = 1; d < 1024; d <<= 1) {
-    uint32_t v = threadIdx.x >= (unsigned)d ? part[threadIdx.x - d] : 0;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
-  }
-  uint32_t run = part[threadIdx.x] - sum;
-  for (uint64_t i = lo; i < hi; ++i) {
-    const uint32_t v = hist[i];
-    hist[i] = run;
-    run += v;
-  }
-}
-
-__global__ void __launch_bounds__(kBlock) k_radix_scatter(const unsigned long long *keys, const uint32_t *vals,
-                                                          unsigned long long *keys_out, uint32_t *vals_out,
-                                                          uint64_t n, int shift, const uint32_t *hist,
-                                                          uint32_t nb) {
+// One pass on the byte at `shift`; hist_b = that byte's 256 digit counts,
+// desc = tiles * 256 zeroed descriptors, counter = zeroed tile counter.
+__global__ void __launch_bounds__(kBlock) k_sort_pass(const unsigned long long *__restrict__ keys,
+                                                      const uint32_t *__restrict__ vals,
+                                                      unsigned long long *__restrict__ keys_out,
+                                                      uint32_t *__restrict__ vals_out, uint64_t n, int shift,
+                                                      const uint32_t *__restrict__ hist_b, unsigned long long *desc,
+                                                      uint32_t *counter, uint32_t *err) {
+  static_assert(kBlock == 256, "one thread per digit");
   constexpr int NW = kBlock / 32;
-  __shared__ uint32_t base_off[256];
-  __shared__ uint32_t running[256];
+  __shared__ uint32_t s_tile;
   __shared__ uint32_t wcnt[NW][256];
-  base_off[threadIdx.x] = hist[(uint64_t)threadIdx.x * nb + blockIdx.x];
+  __shared__ uint32_t running[256];
+  __shared__ unsigned long long base[256];
+  if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
   running[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t tile = s_tile;
+  const uint64_t b0 = tile * kSortTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t b0 = (uint64_t)blockIdx.x * kRadixChunk;
-  for (int it = 0; it < kRadixItems; ++it) {
+  unsigned long long key[kSortItems];
+  uint32_t val[kSortItems], rank[kSortItems], dig[kSortItems];
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+#pragma unroll
     for (int w = 0; w < NW; ++w) wcnt[w][threadIdx.x] = 0;
     __syncthreads();
-    const uint64_t i = b0 + it * kBlock + threadIdx.x;
+    const uint64_t i = b0 + (uint64_t)it * kBlock + threadIdx.x;
     const bool valid = i < n;
-    unsigned long long key = 0;
-    uint32_t val = 0, d = 256;
+    key[it] = 0;
+    val[it] = 0;
+    dig[it] = 256;
     if (valid) {
-      key = keys[i];
-      val = vals[i];
-      d = (uint32_t)((key >> shift) & 0xFF);
+      key[it] = keys[i];
+      val[it] = vals[i];
+      dig[it] = (uint32_t)((key[it] >> shift) & 0xFF);
     }
-    const uint32_t m = __match_any_sync(0xffffffffu, d);
+    const uint32_t m = __match_any_sync(0xffffffffu, dig[it]);
     const uint32_t lrank = __popc(m & lanemask_lt());
-    if (valid && lrank == 0) wcnt[warp][d] = __popc(m);
+    if (valid && lrank == 0) wcnt[warp][dig[it]] = __popc(m);
     __syncthreads();
     if (valid) {
       uint32_t pre = 0;
-      for (int w = 0; w < warp; ++w) pre += wcnt[w][d];
-      const uint32_t dst = base_off[d] + running[d] + pre + lrank;
-      keys_out[dst] = key;
-      vals_out[dst] = val;
+      for (int w = 0; w < warp; ++w) pre += wcnt[w][dig[it]];
+      rank[it] = running[dig[it]] + pre + lrank;
     }
     __syncthreads();
     uint32_t add = 0;
+#pragma unroll
     for (int w = 0; w < NW; ++w) add += wcnt[w][threadIdx.x];
     running[threadIdx.x] += add;
-    __syncthreads();
-    (void)lane;
+  }
+  (void)lane;
+  // digit d: count in this tile, keys of digit d in earlier tiles, base
+  const uint32_t d = threadIdx.x;
+  const unsigned long long cnt_d = running[d];
+  unsigned long long excl = 0;
+  if (tile == 0) {
+    st_desc(&desc[d], kDescIncl | cnt_d);
+  } else {
+    st_desc(&desc[tile * 256 + d], kDescAgg | cnt_d);
+    for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
+      unsigned long long v = ld_desc(&desc[(uint64_t)j * 256 + d]);
+      if ((v & kDescMask) == 0) v = wait_desc(desc + d, (uint64_t)j * 256, err);
+      excl += v & kDescPayload;
+      if ((v & kDescMask) == kDescIncl) break;
+    }
+    st_desc(&desc[tile * 256 + d], kDescIncl | (excl + cnt_d));
+  }
+  unsigned long long total;
+  const unsigned long long dbase = block_excl_sum<kBlock>(hist_b[d], total);
+  base[d] = dbase + excl;
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    if (dig[it] < 256) {
+      const unsigned long long dst = base[dig[it]] + rank[it];
+      keys_out[dst] = key[it];
+      vals_out[dst] = val[it];
+    }
   }
 }
 
@@ -1138,30 +1171,20 @@ void launch_collect_used(const uint32_t *bits, uint64_t cap, PairTable tab, unsi
   k_collect_used<<<grid_for(words, kBlock), kBlock, 0, st>>>(bits, words, tab, keys_out, slots_out, cap_out, status);
 }
 
-void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status, cudaStream_t st) {
+uint64_t sort_tiles(uint64_t n) { return (n + kSortTile - 1) / kSortTile; }
+
+void launch_sort_hist(const unsigned long long *keys, uint64_t n, uint32_t byte_mask, uint32_t *hist,
+                      cudaStream_t st) {
   if (!n) return;
-  k_key_or_and<<<grid_for(n, kBlock, 304), kBlock, 0, st>>>(keys, n, status);
+  k_sort_hist<<<grid_for(n, kBlock, 152u * 4u), kBlock, 0, st>>>(keys, n, byte_mask, hist);
 }
 
-uint64_t radix_blocks(uint64_t n) { return (n + kRadixChunk - 1) / kRadixChunk; }
-
-bool radix_sort_pairs(unsigned long long *keys, uint32_t *vals, unsigned long long *keys_tmp, uint32_t *vals_tmp,
-                      uint64_t n, uint32_t byte_mask, uint32_t *hist, cudaStream_t st) {
-  if (n <= 1) return false;
-  const uint32_t nb = (uint32_t)radix_blocks(n);
-  bool in_tmp = false;
-  for (int b = 0; b < 8; ++b) {
-    if (!((byte_mask >> b) & 1u)) continue;
-    const unsigned long long *ki = in_tmp ? keys_tmp : keys;
-    const uint32_t *vi = in_tmp ? vals_tmp : vals;
-    unsigned long long *ko = in_tmp ? keys : keys_tmp;
-    uint32_t *vo = in_tmp ? vals : vals_tmp;
-    k_radix_hist<<<nb, kBlock, 0, st>>>(ki, n, 8 * b, hist, nb);
-    k_scan_hist<<<1, 1024, 0, st>>>(hist, (uint64_t)nb * 256);
-    k_radix_scatter<<<nb, kBlock, 0, st>>>(ki, vi, ko, vo, n, 8 * b, hist, nb);
-    in_tmp = !in_tmp;
-  }
-  return in_tmp;
+void launch_sort_pass(const unsigned long long *keys, const uint32_t *vals, unsigned long long *keys_out,
+                      uint32_t *vals_out, uint64_t n, int byte, const uint32_t *hist, unsigned long long *desc,
+                      uint32_t *counter, uint32_t *err, cudaStream_t st) {
+  if (!n) return;
+  k_sort_pass<<<(unsigned)sort_tiles(n), kBlock, 0, st>>>(keys, vals, keys_out, vals_out, n, 8 * byte,
+                                                           hist + 256 * byte, desc, counter, err);
 }
 
 void launch_assign_ids(const unsigned long long *sorted_keys, const uint32_t *sorted_slots, uint64_t u,

@@ -82,16 +82,17 @@ uint64_t apply_state_blocks(uint64_t n);
 void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st);
 
 
-// Stable LSD radix sort of (u64 key, u32 value) pairs on the given byte
-// positions (bit i of byte_mask = sort on byte i).  Ping-pongs between the
-// in/tmp buffers; returns true when the result ended in the tmp buffers.
-// hist must hold 256 * radix_blocks(n) + 1 u32 entries.
-uint64_t radix_blocks(uint64_t n);
-bool radix_sort_pairs(unsigned long long *keys, uint32_t *vals, unsigned long long *keys_tmp,
-                      uint32_t *vals_tmp, uint64_t n, uint32_t byte_mask, uint32_t *hist,
+// Stable LSD radix sort of (u64 key, u32 value) pairs, one launch per byte.
+// launch_sort_hist: hist[b * 256 + d] (8 * 256 entries, zeroed) += keys whose
+// byte b is d, for the bytes in byte_mask.  launch_sort_pass: one pass on
+// byte `byte` from (keys, vals) into (keys_out, vals_out); desc holds
+// sort_tiles(n) * 256 zeroed descriptors and counter one zeroed u32.
+uint64_t sort_tiles(uint64_t n);
+void launch_sort_hist(const unsigned long long *keys, uint64_t n, uint32_t byte_mask, uint32_t *hist,
                       cudaStream_t st);
-// OR / AND reduction of keys into status->u64[4] / u64[5] (pre-set u64[5] to ~0).
-void launch_key_or_and(const unsigned long long *keys, uint64_t n, DevStatus *status, cudaStream_t st);
+void launch_sort_pass(const unsigned long long *keys, const uint32_t *vals, unsigned long long *keys_out,
+                      uint32_t *vals_out, uint64_t n, int byte, const uint32_t *hist, unsigned long long *desc,
+                      uint32_t *counter, uint32_t *err, cudaStream_t st);
 
 // keys sorted (transformed, ascending signed order): vals[slot] = next_id + rank,
 // rulebook[rank] = original key.

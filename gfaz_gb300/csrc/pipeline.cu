@@ -343,6 +343,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
       throw std::overflow_error("Compression workflow error: rule id space exhausted");
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
+    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
     used_bits.resize((cap + 31) / 32);
     cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
     replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr,
@@ -356,31 +357,39 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     ctx.check_status("apply");
     const uint64_t n_out = s1.u64[2];
     const uint64_t U = s1.u64[3];
+    // key bytes that differ between the used keys: the only radix passes
+    const unsigned long long diff = s1.u64[4] ^ s1.u64[5];
     ctx.add_bytes("collect_used", 12.0 * U);
     ctx.add_bytes("apply_emit", 4.0 * n_out);
     if (U == 0) break;  // no rule used: stop all rounds
-    ukeys_tmp.resize(U);
-    uslots_tmp.resize(U);
-    // OR/AND of the used keys tell which radix passes can be skipped
-    ctx.reset_status();
-    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
-    GFZ_TIMED(ctx, "key_or_and", launch_key_or_and(ukeys.ptr, U, ds, st));
-    const DevStatus &s2 = ctx.read_status();
-    const unsigned long long diff = s2.u64[4] ^ s2.u64[5];
     uint32_t byte_mask = 0;
     for (int b = 0; b < 8; ++b)
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
-    hist.resize(256 * radix_blocks(U) + 1);
-    bool in_tmp;
-    GFZ_TIMED(ctx, "radix_sort",
-              in_tmp = radix_sort_pairs(ukeys.ptr, uslots.ptr, ukeys_tmp.ptr, uslots_tmp.ptr, U, byte_mask, hist.ptr,
-                                        st));
+    ukeys_tmp.resize(U);
+    uslots_tmp.resize(U);
+    hist.resize(8 * 256);
+    cuda_check(cudaMemsetAsync(hist.ptr, 0, 8 * 256 * sizeof(uint32_t), st), "histogram clear");
+    ctx.reset_status();
+    bool in_tmp = false;
+    GFZ_TIMED(ctx, "radix_sort", launch_sort_hist(ukeys.ptr, U, byte_mask, hist.ptr, st));
+    for (int b = 0; b < 8; ++b) {
+      if (!((byte_mask >> b) & 1u)) continue;
+      uint32_t *counter;
+      unsigned long long *desc = ctx.lookback(sort_tiles(U) * 256, &counter);
+      GFZ_TIMED(ctx, "radix_sort",
+                launch_sort_pass(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr,
+                                 in_tmp ? ukeys.ptr : ukeys_tmp.ptr, in_tmp ? uslots.ptr : uslots_tmp.ptr, U, b,
+                                 hist.ptr, desc, counter, &ds->err, st));
+      in_tmp = !in_tmp;
+    }
     rules.reserve(g.nrules + U, true);
     rules.size = g.nrules + U;
     GFZ_TIMED(ctx, "assign_ids",
               launch_assign_ids(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr, U, next_id,
                                 tab.view(cap), rules.ptr + g.nrules, st));
     GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
+    ctx.read_status();
+    ctx.check_status("rule sort");
     if (debug_enabled())
       fprintf(stderr, "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu\n",
               round + 1, (unsigned long long)n, (unsigned long long)cap, (unsigned long long)distinct,
