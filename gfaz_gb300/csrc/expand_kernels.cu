@@ -52,60 +52,113 @@ __device__ __forceinline__ uint32_t child_prefix(int32_t c, uint32_t o, const Ru
 // pass (built[c] in [1, pass)) writes pre_R = pre_first ++ (total_first +
 // pre_second) and records built[R] = pass.  Rules still waiting are counted
 // in status->u64[6].
+// Prefix value at offset o of rule i = first ++ second (lf steps of first).
+__device__ __forceinline__ uint32_t rule_prefix_at(int32_t f, int32_t g, uint32_t lf, uint32_t tf, uint32_t o,
+                                                   const RulePrefixView &rv) {
+  return o < lf ? child_prefix(f, o, rv) : tf + child_prefix(g, o - lf, rv);
+}
+
+// Value ranges of the text length shortcut, folded over offsets: delta 1:
+// prefix values (all, and {0} plus all but the last); delta 0: expansion
+// values.
+struct RangeAcc {
+  int32_t mnA = INT32_MAX, mxA = INT32_MIN, mnB = 0, mxB = 0;
+  __device__ __forceinline__ void add(int32_t y, bool not_last) {
+    mnA = min(mnA, y);
+    mxA = max(mxA, y);
+    if (not_last) {
+      mnB = min(mnB, y);
+      mxB = max(mxB, y);
+    }
+  }
+};
+
+constexpr uint32_t kWarpRule = 16;  // rules longer than this are written by a whole warp
+
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
                                    RulePrefixView rv, int32_t *rpre, int4 *rstat, int delta, uint32_t *built,
                                    uint32_t pass, DevStatus *status) {
   __shared__ uint32_t s_open;
   if (threadIdx.x == 0) s_open = 0;
   __syncthreads();
+  const int lane = threadIdx.x & 31;
   uint32_t open = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < rv.nrules;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    if (built[i]) continue;
-    const int32_t f = first[i], g = second[i];
-    const uint32_t af = abs32(f), ag = abs32(g);
-    const bool rf = is_rule(af, rv.min_id, rv.nrules), rg = is_rule(ag, rv.min_id, rv.nrules);
-    const uint32_t bf = rf ? built[af - rv.min_id] : 1u, bg = rg ? built[ag - rv.min_id] : 1u;
-    const bool ready = (!rf || (bf != 0 && bf < pass)) && (!rg || (bg != 0 && bg < pass));
-    if (!ready) {
-      open++;
-      continue;
-    }
-    const uint32_t lf = rf ? rv.rlen[af - rv.min_id] : 1u, lg = rg ? rv.rlen[ag - rv.min_id] : 1u;
-    if ((uint64_t)lf + lg != rv.rlen[i]) {
-      atomicOr(&status->err, kErrLength);
-      built[i] = pass;
-      continue;
-    }
-    const uint64_t b = rv.roff[i];
-    const uint32_t L = lf + lg;
-    // value ranges for the text length shortcut: delta 1: prefix values
-    // (all, and {0} plus all but the last); delta 0: expansion values
-    int32_t mnA = INT32_MAX, mxA = INT32_MIN, mnB = 0, mxB = 0;
-    uint32_t prev = 0, tf = 0;
-    for (uint32_t o = 0; o < L; ++o) {
-      uint32_t x;
-      if (o < lf) {
-        x = child_prefix(f, o, rv);
-        tf = x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // whole warps walk the rules together so that long rules can be shared
+  const uint64_t span = (rv.nrules + 31) & ~31ull;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < span; i += stride) {
+    bool ready = false;
+    int32_t f = 0, g = 0;
+    uint32_t lf = 0, lg = 0;
+    if (i < rv.nrules && !built[i]) {
+      f = first[i];
+      g = second[i];
+      const uint32_t af = abs32(f), ag = abs32(g);
+      const bool rf = is_rule(af, rv.min_id, rv.nrules), rg = is_rule(ag, rv.min_id, rv.nrules);
+      const uint32_t bf = rf ? built[af - rv.min_id] : 1u, bg = rg ? built[ag - rv.min_id] : 1u;
+      ready = (!rf || (bf != 0 && bf < pass)) && (!rg || (bg != 0 && bg < pass));
+      if (!ready) {
+        open++;
       } else {
-        x = tf + child_prefix(g, o - lf, rv);
-      }
-      rpre[b + o] = (int32_t)x;
-      const int32_t y = delta ? (int32_t)x : (int32_t)(x - prev);
-      prev = x;
-      mnA = min(mnA, y);
-      mxA = max(mxA, y);
-      if (delta && o + 1 < L) {
-        mnB = min(mnB, y);
-        mxB = max(mxB, y);
+        lf = rf ? rv.rlen[af - rv.min_id] : 1u;
+        lg = rg ? rv.rlen[ag - rv.min_id] : 1u;
+        if ((uint64_t)lf + lg != rv.rlen[i]) {
+          atomicOr(&status->err, kErrLength);
+          built[i] = pass;
+          ready = false;
+        }
       }
     }
-    rstat[i] = make_int4(mnA, mxA, mnB, mxB);
-    built[i] = pass;
+    const uint32_t L = lf + lg;
+    if (ready && L <= kWarpRule) {
+      const uint64_t b = rv.roff[i];
+      const uint32_t tf = child_prefix(f, lf - 1, rv);
+      RangeAcc r;
+      uint32_t prev = 0;
+      for (uint32_t o = 0; o < L; ++o) {
+        const uint32_t x = rule_prefix_at(f, g, lf, tf, o, rv);
+        rpre[b + o] = (int32_t)x;
+        r.add(delta ? (int32_t)x : (int32_t)(x - prev), delta && o + 1 < L);
+        prev = x;
+      }
+      rstat[i] = make_int4(r.mnA, r.mxA, r.mnB, r.mxB);
+      built[i] = pass;
+    }
+    // long rules: one at a time, the warp's lanes on consecutive offsets
+    uint32_t longs = __ballot_sync(0xffffffffu, ready && L > kWarpRule);
+    while (longs) {
+      const int src = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const uint64_t ri = __shfl_sync(0xffffffffu, i, src);
+      const int32_t rf_ = __shfl_sync(0xffffffffu, f, src), rg_ = __shfl_sync(0xffffffffu, g, src);
+      const uint32_t rlf = __shfl_sync(0xffffffffu, lf, src), rL = __shfl_sync(0xffffffffu, L, src);
+      const uint64_t b = rv.roff[ri];
+      const uint32_t tf = child_prefix(rf_, rlf - 1, rv);
+      RangeAcc r;
+      for (uint32_t o0 = 0; o0 < rL; o0 += 32) {
+        const uint32_t o = o0 + lane;
+        if (o < rL) {
+          const uint32_t x = rule_prefix_at(rf_, rg_, rlf, tf, o, rv);
+          rpre[b + o] = (int32_t)x;
+          int32_t y = (int32_t)x;
+          if (!delta) y = (int32_t)(x - (o ? rule_prefix_at(rf_, rg_, rlf, tf, o - 1, rv) : 0u));
+          r.add(y, delta && o + 1 < rL);
+        }
+      }
+      for (int d = 16; d > 0; d >>= 1) {
+        r.mnA = min(r.mnA, __shfl_xor_sync(0xffffffffu, r.mnA, d));
+        r.mxA = max(r.mxA, __shfl_xor_sync(0xffffffffu, r.mxA, d));
+        r.mnB = min(r.mnB, __shfl_xor_sync(0xffffffffu, r.mnB, d));
+        r.mxB = max(r.mxB, __shfl_xor_sync(0xffffffffu, r.mxB, d));
+      }
+      if (lane == src) {
+        rstat[ri] = make_int4(r.mnA, r.mxA, r.mnB, r.mxB);
+        built[ri] = pass;
+      }
+    }
   }
   open = __reduce_add_sync(0xffffffffu, open);
-  if ((threadIdx.x & 31) == 0 && open) atomicAdd(&s_open, open);
+  if (lane == 0 && open) atomicAdd(&s_open, open);
   __syncthreads();
   if (threadIdx.x == 0 && s_open) atomicAdd(&status->u64[6], (unsigned long long)s_open);
 }
