@@ -27,6 +27,7 @@ struct gfz_grammar {
   explicit gfz_grammar(cudaStream_t st) : g(st), text(st) {}
   gfz::Grammar g;
   gfz::DevVec<char> text;
+  bool text_external = false;  // the last decode_text wrote to the caller's buffer
   uint64_t text_size = 0;
 };
 struct gfz_graph {
@@ -599,21 +600,41 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
     require(g && meta && size, "NULL argument");
     require(t0 <= t1 && t1 <= g->g.ntrav, "traversal range out of bounds");
     gfz::Context &c = ctx_of(ctx);
-    g->text_size = gfz::decode_text(
-        c, g->g, t0, t1, [&](const std::vector<uint64_t> &off) { return pieces_from_meta(meta, off); }, meta->mode,
-        g->text);
-    *size = g->text_size;
+    auto pieces = [&](const std::vector<uint64_t> &off) { return pieces_from_meta(meta, off); };
+    // device memory or page-locked host memory: the kernels write the text
+    // there directly (over the chip-to-chip link for host memory)
+    char *direct = nullptr;
     if (out) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, out) == cudaSuccess &&
+          ((at.type == cudaMemoryTypeDevice && at.device == c.device()) || at.type == cudaMemoryTypeHost) &&
+          at.devicePointer)
+        direct = static_cast<char *>(at.devicePointer);
+      else
+        cudaGetLastError();  // not a CUDA allocation
+    }
+    if (direct) {
+      g->text_size = gfz::decode_text(c, g->g, t0, t1, pieces, meta->mode, g->text, direct, cap);
+      gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+      g->text_external = true;
+    } else {
+      g->text_size = gfz::decode_text(c, g->g, t0, t1, pieces, meta->mode, g->text);
+      g->text_external = false;
+    }
+    *size = g->text_size;
+    if (out && !direct) {
       if (cap < g->text_size) throw std::length_error("output buffer too small");
       copy_out(c, out, g->text.ptr, g->text_size, where);
       gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
     }
+    (void)where;
   });
 }
 
 gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size) {
   return guard([&] {
     require(g && device_text && size, "NULL argument");
+    require(!g->text_external, "the last gfz_decode_text wrote its text to the caller's buffer");
     *device_text = g->text.ptr;
     *size = g->text_size;
   });

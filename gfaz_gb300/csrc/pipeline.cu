@@ -766,7 +766,7 @@ struct DevPieces {
 
 uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
                      const std::function<TextPieces(const std::vector<uint64_t> &)> &make_pieces, int mode,
-                     DevVec<char> &text) {
+                     DevVec<char> &text, char *direct, uint64_t direct_cap) {
   cudaStream_t st = ctx.stream();
   if (t1 < t0 || t1 > g.ntrav) throw std::out_of_range("traversal range out of bounds");
   ensure_rule_lengths(ctx, g);
@@ -774,7 +774,13 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
     DevVec<int32_t> x(st);
     std::vector<uint64_t> off;
     decode_traversals(ctx, g, t0, t1, x, off);
-    return emit_text(ctx, x, off, make_pieces(off), mode, text);
+    const uint64_t n = emit_text(ctx, x, off, make_pieces(off), mode, text);
+    if (direct) {
+      if (direct_cap < n) throw std::length_error("output buffer too small");
+      if (n) cuda_check(cudaMemcpyAsync(direct, text.ptr, n, cudaMemcpyDefault, st), "text copy");
+      cuda_check(cudaStreamSynchronize(st), "stream sync");
+    }
+    return n;
   }
   ExpandPlan P(st);
   plan_expansion(ctx, g, t0, t1, P);
@@ -806,16 +812,23 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   ctx.read_status();
   ctx.check_status("text lengths");
   const uint64_t size = body + pieces.tail.size();
-  text.resize(std::max<uint64_t>(size, 1));
-  text.size = size;
+  char *dst;
+  if (direct) {
+    if (direct_cap < size) throw std::length_error("output buffer too small");
+    dst = direct;
+  } else {
+    text.resize(std::max<uint64_t>(size, 1));
+    text.size = size;
+    dst = text.ptr;
+  }
   T.cap = body;
   DevVec<uint64_t> toff(st);
   toff.resize(std::max<uint64_t>(expand_num_tiles(P.total), 1));
   GFZ_TIMED(ctx, "symbol_text", launch_tile_text_off(E, T, g.delta_round, soff.ptr, sdig.ptr, toff.ptr, st));
   GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
-              launch_text_write(E, T, g.delta_round, toff.ptr, text.ptr, st));
+              launch_text_write(E, T, g.delta_round, toff.ptr, dst, st));
   if (!pieces.tail.empty())
-    cuda_check(cudaMemcpyAsync(text.ptr + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
+    cuda_check(cudaMemcpyAsync(dst + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyDefault, st),
                "text tail");
   ctx.read_status();
   ctx.check_status("text emission");

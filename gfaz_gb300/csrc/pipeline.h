@@ -219,9 +219,11 @@ void prepare_decode(Context &ctx, Grammar &g);
 
 // Decode + text for traversals [t0, t1) of g.  `pieces` builds the text
 // pieces from the decoded traversal offsets (t1 - t0 + 1 entries, from 0).
+// direct (optional, direct_cap bytes): device memory or page-locked host
+// memory the kernels write the text into, in place of `text`.
 uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
                      const std::function<TextPieces(const std::vector<uint64_t> &)> &pieces, int mode,
-                     DevVec<char> &text);
+                     DevVec<char> &text, char *direct = nullptr, uint64_t direct_cap = 0);
 
 // Append encoding with a stored rulebook (one stack-encoder pass per layer).
 struct Layer {

@@ -198,8 +198,11 @@ typedef struct {
  * writer's path, src/gpu/decompression/path_decompression_gpu_rolling.cpp:215-370
  * and format_*_line_numeric, src/io/gfa_write_utils.cpp:238-290).  With
  * out == NULL the text stays in a device buffer owned by `g`
- * (gfz_grammar_text gives its address); otherwise it is copied to out
- * (capacity cap bytes, host or device per `where`). */
+ * (gfz_grammar_text gives its address); otherwise it goes to out (capacity
+ * cap bytes, host or device per `where`).  When out is device memory or
+ * page-locked host memory the kernels write the text there directly (no
+ * staging copy; host memory over the chip-to-chip link) and `g` keeps no
+ * copy: gfz_grammar_text then fails until the next decode without out. */
 gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64_t t1, const gfz_line_meta *meta,
                            char *out, uint64_t cap, uint64_t *size, int where);
 gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size);
