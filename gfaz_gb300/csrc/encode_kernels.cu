@@ -271,6 +271,48 @@ __global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restr
   }
 }
 
+// The count for streams whose pairs are mostly new (late rounds): one pair
+// per thread, read straight from global memory, with no staging and no
+// block barrier, so every insert is an independent chain and the memory
+// system sees as many of them at once as threads are resident.
+__global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict__ s, uint64_t n,
+                                                       const uint32_t *__restrict__ heads, PairTable tab,
+                                                       DevStatus *status) {
+  __shared__ uint32_t s_fresh, s_rep;
+  if (threadIdx.x == 0) {
+    s_fresh = 0;
+    s_rep = 0;
+  }
+  __syncthreads();
+  InsertCounts c;
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p + 1 < n;
+       p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = p + 1;
+    if ((heads[q >> 5] >> (q & 31)) & 1u) continue;  // q opens a traversal
+    const unsigned long long key = canon2(pack2(s[p], s[q]));
+    const uint32_t h = hash_pair(key) & mask;
+    unsigned long long cur;
+    uint32_t fl;
+    load_slot(&tab.slots[h], cur, fl);
+    if (!insert_at(tab, key, false, h, cur, fl, c)) {
+      atomicOr(&status->err, kErrTableFull);
+      break;
+    }
+  }
+  const uint32_t f = __reduce_add_sync(0xffffffffu, c.fresh);
+  const uint32_t r = __reduce_add_sync(0xffffffffu, c.repeated);
+  if ((threadIdx.x & 31) == 0) {
+    if (f) atomicAdd(&s_fresh, f);
+    if (r) atomicAdd(&s_rep, r);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_fresh) atomicAdd(&status->u64[0], (unsigned long long)s_fresh);
+    if (s_rep) atomicAdd(&status->u64[1], (unsigned long long)s_rep);
+  }
+}
+
 // Traversal-head bitmap: bit off[t] for every t <= ntrav (bits cleared).
 __global__ void k_head_bits(const uint64_t *__restrict__ off, uint64_t ntrav, uint32_t *bits) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntrav; t += (uint64_t)gridDim.x * blockDim.x) {
@@ -1109,12 +1151,16 @@ void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaS
 }
 
 void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
-                        bool warp_dedup, cudaStream_t st) {
+                        CountKernel kind, cudaStream_t st) {
   if (!n) return;
+  if (kind == CountKernel::kFlat) {
+    k_count_flat<<<grid_for(n, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status);
+    return;
+  }
   constexpr uint64_t TILE = kBlock * kCountItems;
   const uint64_t tiles = (n + TILE - 1) / TILE;
   const uint64_t hw = head_words(n);
-  if (warp_dedup) {
+  if (kind == CountKernel::kTiledWarpDedup) {
     auto k = k_count_pairs<kBlock, kCountItems, true>;
     k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status);
   } else {

@@ -44,9 +44,14 @@ void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaS
 
 // Inserts every canonical adjacent pair inside a traversal (heads: the
 // stream's head bitmap).  Results: status->u64[0] += new distinct keys,
-// u64[1] += keys that became repeated.
+// u64[1] += keys that became repeated.  The kernels give the same table
+// contents (slot placement aside): kTiled stages tiles in shared memory and
+// folds runs of equal keys (streams with many repeats); kTiledWarpDedup
+// also folds equal keys across a warp; kFlat takes one pair per thread
+// without staging or barriers (streams of mostly new pairs).
+enum class CountKernel { kTiled = 0, kTiledWarpDedup = 1, kFlat = 2 };
 void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
-                        bool warp_dedup, cudaStream_t st);
+                        CountKernel kind, cudaStream_t st);
 
 // Greedy left-to-right replacement of candidate pairs; writes the compacted
 // stream with temporary symbols +-(temp_base + slot), the new traversal

@@ -48,6 +48,12 @@ uint64_t next_pow2(uint64_t x) {
   return c;
 }
 
+uint64_t ceil_log2(uint64_t x) {
+  uint64_t r = 0;
+  while ((1ull << r) < x) ++r;
+  return r;
+}
+
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
 
 
@@ -161,6 +167,19 @@ unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) {
   *counter = counter_.ptr;
   count_launch(0);
   return desc_.ptr;
+}
+
+float Context::time_launches(const std::function<void()> &launch) {
+  cudaEvent_t a = take_event(), b = take_event();
+  cuda_check(cudaEventRecord(a, stream_), "event record");
+  launch();
+  cuda_check(cudaEventRecord(b, stream_), "event record");
+  cuda_check(cudaEventSynchronize(b), "event sync");
+  float ms = 0;
+  cuda_check(cudaEventElapsedTime(&ms, a, b), "event time");
+  event_pool_.push_back(a);
+  event_pool_.push_back(b);
+  return ms;
 }
 
 cudaEvent_t Context::take_event() {
@@ -321,12 +340,49 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     heads.resize(head_words(n));
     cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(n) * sizeof(uint32_t), st), "head bitmap clear");
     GFZ_TIMED(ctx, "head_bits", launch_head_bits(offA.ptr, ntrav, heads.ptr, st));
+    // Count kernel: forced by option, else the faster of the tiled and the
+    // flat kernel for this stream class (first round or not, length, and the
+    // previous round's distinct pairs per step), timed on the first stream
+    // of the class and remembered by the context.  Both fill the table alike.
+    const int cls = (round == 0 ? 0 : 1) * 1000 + 4 * (int)ceil_log2(n) +
+                    (round == 0 ? 0 : (int)std::min<uint64_t>(3, prev_distinct * 4 / std::max<uint64_t>(n, 1)));
+    CountKernel kind = ctx.warp_dedup ? CountKernel::kTiledWarpDedup : CountKernel::kTiled;
+    bool tune = false;
+    if (ctx.count_kernel >= 0) {
+      kind = (CountKernel)ctx.count_kernel;
+    } else if (!ctx.warp_dedup) {
+      const auto it = ctx.count_tuned.find(cls);
+      if (it != ctx.count_tuned.end()) kind = (CountKernel)it->second;
+      else tune = true;
+    }
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
-      tab.prepare(cap, st);
-      ctx.reset_status();
-      GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
-                launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, ctx.warp_dedup, st));
+      if (tune) {
+        tab.prepare(cap, st);
+        ctx.reset_status();
+        const float t_tiled = ctx.time_launches(
+            [&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, CountKernel::kTiled, st); });
+        const DevStatus &s0 = ctx.read_status();
+        if ((s0.err & kErrTableFull) || s0.u64[0] * 10 > cap * 8) {
+          cap *= 4;
+          continue;
+        }
+        tab.prepare(cap, st);
+        ctx.reset_status();
+        const float t_flat = ctx.time_launches(
+            [&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, CountKernel::kFlat, st); });
+        kind = t_flat < t_tiled ? CountKernel::kFlat : CountKernel::kTiled;
+        ctx.count_tuned[cls] = (int)kind;
+        if (debug_enabled())
+          fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f ms, flat %.3f ms\n", cls,
+                  (unsigned long long)n, t_tiled, t_flat);
+        tune = false;
+      } else {
+        tab.prepare(cap, st);
+        ctx.reset_status();
+        GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
+                    launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
+      }
       const DevStatus &s = ctx.read_status();
       distinct = s.u64[0];
       repeated = s.u64[1];
