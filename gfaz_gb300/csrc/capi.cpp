@@ -219,6 +219,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "count_kernel") {
       require(value >= -1 && value <= 2, "count_kernel must be -1 (tuned), 0 (tiled), 1 (tiled + warp folding) or 2 (flat)");
       c.count_kernel = (int)value;
+    } else if (std::string(name) == "classify_kernel") {
+      require(value >= -1 && value <= 1, "classify_kernel must be -1 (tuned), 0 (persistent) or 1 (flat)");
+      c.classify_kernel = (int)value;
     } else if (std::string(name) == "append_chunk") {
       require(value >= 0, "append_chunk must be >= 0");
       c.append_chunk = (uint64_t)value;

@@ -536,6 +536,49 @@ __global__ void __launch_bounds__(BLOCK, 4) k_apply_classify(const int32_t *__re
   }
 }
 
+// The same classification with one tile per block and the steps read
+// straight from global memory: no staging pipeline and no barrier besides
+// the block scan's, so more blocks are resident to hide the table probes.
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__restrict__ s, uint64_t n,
+                                                               const uint32_t *__restrict__ heads, PairTable tab,
+                                                               uint32_t *__restrict__ tword,
+                                                               unsigned long long *__restrict__ tile_agg,
+                                                               DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(ITEMS == 8 && TILE <= 2048, "a thread word holds 8 candidate bits and 11-bit counts");
+  __shared__ ParAgg s_warp[BLOCK / 32];
+  const uint64_t tile = blockIdx.x;
+  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  int32_t v[ITEMS + 1];
+  uint32_t validb = 0;
+  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+    const int4 a = *reinterpret_cast<const int4 *>(s + p0);
+    const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    v[8] = s[p0 + ITEMS];
+  } else {
+#pragma unroll
+    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+  }
+  if (p0 < n) {
+    const uint32_t w = (uint32_t)(p0 >> 5);
+    const uint32_t hd = (uint32_t)((((unsigned long long)heads[w + 1] << 32) | heads[w]) >> (p0 & 31));
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) validb |= (uint32_t)(p0 + k < n && !((hd >> (k + 1)) & 1u)) << k;
+  }
+  uint32_t slot[ITEMS], fl[ITEMS], fwdb;
+  lookup_pairs<ITEMS>(v, validb, tab, slot, fl, fwdb, status);
+  uint32_t cbits = 0;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) cbits |= (uint32_t)(((validb >> k) & 1u) && (fl[k] & kFlagRepeated)) << k;
+  ParAgg total;
+  const ParAgg excl = block_par_scan<BLOCK>(par_of_bits(cbits, ITEMS), total, s_warp);
+  tword[tile * BLOCK + threadIdx.x] = cbits | ((excl.xo & 3u) << 8) | (excl.c0 << 10) | (excl.c1 << 21);
+  if (threadIdx.x == 0) tile_agg[tile] = par_encode(total);
+}
+
 // state[t] = the state (x, replaced count) before tile t, encoded x | c << 1.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_tile_states(const unsigned long long *__restrict__ tile_agg,
@@ -1188,8 +1231,13 @@ uint64_t apply_state_blocks(uint64_t n) {
 }
 
 void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
-                           DevStatus *status, cudaStream_t st) {
+                           bool flat, DevStatus *status, cudaStream_t st) {
   if (!n) return;
+  if (flat) {
+    k_apply_classify_flat<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
+        s, n, heads, tab, w.tword, w.tile_agg, status);
+    return;
+  }
   auto k = k_apply_classify<kBlock, kApplyItems>;
   k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), tab, w.tword,
                                                                        w.tile_agg, status);

@@ -65,10 +65,12 @@ struct ApplyScratch {
   unsigned long long *tile_agg, *state, *desc;
   uint32_t *counter;
 };
-// The three passes: candidate bits and tile aggregates; carried-in state
-// of every tile; replay and compacted output.
+// The three passes: candidate bits and tile aggregates (flat: one tile per
+// block read straight from global memory, else persistent blocks with
+// staged tiles; the same output); carried-in state of every tile; replay
+// and compacted output.
 void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
-                           DevStatus *status, cudaStream_t st);
+                           bool flat, DevStatus *status, cudaStream_t st);
 void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
 // Emit also sets bit `slot` of used_bits (cap bits, zeroed) for every slot
 // it flags used.

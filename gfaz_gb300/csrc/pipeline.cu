@@ -257,7 +257,7 @@ void Context::clear_kernel_stats() {
 // status u64[2] for the caller to read.
 static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint64_t *offA, uint64_t ntrav,
                           const uint32_t *heads, PairTable tab, int32_t temp_base, int32_t *B, uint64_t *offB,
-                          uint32_t *used_bits, ReplaceWork &w) {
+                          uint32_t *used_bits, int cls, ReplaceWork &w) {
   cudaStream_t st = ctx.stream();
   DevStatus *ds = ctx.dstatus();
   const uint64_t tiles = apply_num_tiles(n);
@@ -269,7 +269,24 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
   w.tile_state.resize(std::max<uint64_t>(tiles, 1));
   GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA, ntrav, n, w.tile_trav.ptr, st));
   const ApplyScratch sc{w.tword.ptr, w.tile_agg.ptr, w.tile_state.ptr, desc, counter};
-  GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify(A, n, heads, tab, sc, ds, st));
+  // classify variant: forced by option, else tuned per stream class like
+  // the count kernel (both write the same words)
+  bool flat = ctx.classify_kernel == 1;
+  if (ctx.classify_kernel < 0) {
+    const auto it = ctx.tuned.find({Context::kTuneClassify, cls});
+    if (it != ctx.tuned.end()) {
+      flat = it->second == 1;
+    } else {
+      const float t_tiled = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, false, ds, st); });
+      const float t_flat = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, true, ds, st); });
+      flat = t_flat < t_tiled;
+      ctx.tuned[{Context::kTuneClassify, cls}] = flat ? 1 : 0;
+      if (debug_enabled())
+        fprintf(stderr, "[gfaz gb300] classify tuner: class %d n=%llu persistent %.3f ms, flat %.3f ms\n", cls,
+                (unsigned long long)n, t_tiled, t_flat);
+    }
+  }
+  GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify(A, n, heads, tab, sc, flat, ds, st));
   GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
   GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
               launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, used_bits, sc, ds, st));
@@ -351,8 +368,8 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     if (ctx.count_kernel >= 0) {
       kind = (CountKernel)ctx.count_kernel;
     } else if (!ctx.warp_dedup) {
-      const auto it = ctx.count_tuned.find(cls);
-      if (it != ctx.count_tuned.end()) kind = (CountKernel)it->second;
+      const auto it = ctx.tuned.find({Context::kTuneCount, cls});
+      if (it != ctx.tuned.end()) kind = (CountKernel)it->second;
       else tune = true;
     }
     for (;;) {
@@ -372,7 +389,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
         const float t_flat = ctx.time_launches(
             [&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, CountKernel::kFlat, st); });
         kind = t_flat < t_tiled ? CountKernel::kFlat : CountKernel::kTiled;
-        ctx.count_tuned[cls] = (int)kind;
+        ctx.tuned[{Context::kTuneCount, cls}] = (int)kind;
         if (debug_enabled())
           fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f ms, flat %.3f ms\n", cls,
                   (unsigned long long)n, t_tiled, t_flat);
@@ -403,7 +420,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     used_bits.resize((cap + 31) / 32);
     cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
     replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr,
-                  used_bits.ptr, rw);
+                  used_bits.ptr, cls, rw);
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
     GFZ_TIMED_B(ctx, "collect_used", cap / 8.0,

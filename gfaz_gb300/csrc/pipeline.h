@@ -129,9 +129,11 @@ class Context {
   uint64_t first_table_cap = 0;  // pair-table slots of the first round (0 = automatic)
   uint64_t append_chunk = 0;     // steps per chunk of the chunked stack pass (0 = the automatic ladder)
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
-  // Tuner: stream class -> the count kernel that was faster the first time
-  // the class came up (see encode_traversals).
-  std::map<int, int> count_tuned;
+  int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
+  // Tuner: (kernel, stream class) -> the variant that was faster the first
+  // time the class came up (see encode_traversals).
+  enum TunedKernel { kTuneCount = 0, kTuneClassify = 1 };
+  std::map<std::pair<int, int>, int> tuned;
   // Launches on this context's stream and returns their device time (ms).
   float time_launches(const std::function<void()> &launch);
 

@@ -77,7 +77,9 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * the pair-count kernel of the grammar rounds: -1 (default) = the faster of
  * the tiled and the flat kernel, timed the first time the context meets a
  * stream class (length, repeat density) and remembered, 0 = tiled, 1 =
- * tiled with warp folding, 2 = flat (one pair per thread). */
+ * tiled with warp folding, 2 = flat (one pair per thread); "classify_kernel"
+ * = the candidate classification pass, tuned alike: -1 (default), 0 =
+ * persistent with staged tiles, 1 = flat (one tile per block). */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */

@@ -156,10 +156,12 @@ def test_load_grammar_decodes_oracle_output(gpu_ctx):
 
 def test_count_kernels_give_same_result(gpu_ctx):
     """Every pair-count kernel (the tuner's pick, tiled, tiled with warp
-    folding, flat) and the warp folding switch give the same grammar."""
+    folding, flat), both classification kernels and the warp folding switch
+    give the same grammar."""
     steps, off, _ = synthetic.cfg2_stream(seed=4, n_segments=80_000, n_paths=6)
     a = gz.encode(steps, off, ctx=gpu_ctx).arrays()
-    for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("warp_dedup", 1)]:
+    for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("warp_dedup", 1),
+                     ("classify_kernel", 0), ("classify_kernel", 1)]:
         ctx2 = gz.Context(0)
         ctx2.set_option(opt, val)
         b = gz.encode(steps, off, ctx=ctx2).arrays()
