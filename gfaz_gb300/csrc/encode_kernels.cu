@@ -615,6 +615,102 @@ __global__ void __launch_bounds__(BLOCK) k_tile_states(const unsigned long long 
   }
 }
 
+// Replays one tile from its carried-in state: replaced positions become
+// their temporary rule symbols, consumed ones vanish, and the kept symbols
+// are compacted into out; traversal offsets inside the tile are moved to
+// their output positions.  v = the thread's ITEMS steps and the next one;
+// tw / st / ag = the thread's word, the tile's carried-in state and its
+// aggregate; tlo = the tile's first traversal; so / lidx = shared scratch.
+template <int BLOCK, int ITEMS>
+__device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_t tile, uint64_t n, uint32_t tw,
+                                          unsigned long long st, unsigned long long ag, const uint64_t *s_tlo,
+                                          const uint64_t *__restrict__ off, uint64_t ntrav, const PairTable &tab,
+                                          int32_t temp_base, int32_t *__restrict__ out, uint64_t *__restrict__ new_off,
+                                          uint32_t *used_bits, DevStatus *status, int32_t *so, uint16_t *lidx) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  const uint32_t j0 = threadIdx.x * ITEMS;
+  const uint64_t base = tile * TILE;
+  const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
+  const uint32_t cbits = tw & 0xFFu;
+  const ParAgg excl{(tw >> 8) & 3u, (tw >> 10) & 0x7FFu, tw >> 21};
+  const ParAgg total = par_decode(ag);
+  const uint32_t in_x = (uint32_t)(st & 1u);
+  const unsigned long long in_c = st >> 1;
+  // replay from the carried-in state: kept (not consumed) and replaced bits
+  const uint32_t x_init = par_x(excl, in_x);
+  const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
+  uint32_t keptbits = 0, xbits = 0;
+  {
+    uint32_t x = x_init;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      if (j0 + k < len) {
+        const uint32_t prev = x;
+        x = ((cbits >> k) & 1u) & (prev ^ 1u);
+        keptbits |= (prev ^ 1u) << k;
+        xbits |= x << k;
+      }
+    }
+  }
+  // the rules of the replaced positions
+  uint32_t slot[ITEMS], fl[ITEMS], fwdb;
+  lookup_pairs<ITEMS>(v, xbits, tab, slot, fl, fwdb, status);
+  // kept positions of the tile before j0: j0 minus the consumed ones (the
+  // carried-in position and the partner of every replaced position before
+  // j0, except a replaced j0 - 1 whose partner is j0 itself)
+  const uint32_t kept_base = j0 - in_x - c_init + x_init;
+  const uint64_t out_base = base - in_c + in_x;
+  const uint32_t shift = (uint32_t)(((reinterpret_cast<uintptr_t>(out) >> 2) + out_base) & 3u);
+  uint32_t lpk[ITEMS / 2];
+  uint32_t need = 0;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
+    if ((keptbits >> k) & 1u) {
+      int32_t val = v[k];
+      if ((xbits >> k) & 1u) {
+        const int32_t sym = temp_base + (int32_t)slot[k];
+        val = ((fwdb >> k) & 1u) ? sym : neg32(sym);
+        if (!(fl[k] & kFlagUsed)) need |= 1u << k;
+      }
+      so[shift + lo] = val;
+    }
+    if (k & 1) lpk[k >> 1] |= lo << 16;
+    else lpk[k >> 1] = lo & 0xFFFFu;
+  }
+  *reinterpret_cast<uint4 *>(&lidx[j0]) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
+  // rules chosen here whose slot was not yet flagged used: one flag update
+  // per distinct slot per warp (frequent pairs hit one slot from every
+  // lane), mirrored into the bitmap of used slots
+  if (__any_sync(0xffffffffu, need != 0)) {
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const bool nk = (need >> k) & 1u;
+      if (__any_sync(0xffffffffu, nk)) {
+        const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
+        if (nk && (peers & lanemask_lt()) == 0) {
+          atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+          atomicOr(&used_bits[slot[k] >> 5], 1u << (slot[k] & 31));
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // positions consumed inside the tile: the carried-in one (in_x) plus the
+  // partner of every replaced position except a replaced last position,
+  // whose partner opens the next tile (x_out)
+  const uint32_t kept = len - in_x - par_c(total, in_x) + par_x(total, in_x);
+  stage_out_phased<BLOCK>(out + out_base, so, shift, kept);
+  const bool last_tile = base + len == n;
+  for (uint64_t t = *s_tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
+    const uint64_t q = off[t];
+    if (q < base + len) new_off[t] = out_base + lidx[(uint32_t)(q - base)];
+    else if (last_tile && q == n) new_off[t] = out_base + kept;
+    else break;
+  }
+  if (last_tile && threadIdx.x == 0) status->u64[2] = out_base + kept;
+}
+
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restrict__ s, uint64_t n,
                                                       const uint32_t *__restrict__ heads, uint64_t head_words,
@@ -661,89 +757,10 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
       if (bulk_next) mbar_wait(&P.bar[b ^ 1], (phases >> (b ^ 1)) & 1u);
       return;
     }
-    const int32_t *sv = P.sv[b];
-    const uint64_t base = tile * TILE;
-    const uint32_t len = (uint32_t)min((uint64_t)TILE, n - base);
-    const uint32_t cbits = tw_cur & 0xFFu;
-    const ParAgg excl{(tw_cur >> 8) & 3u, (tw_cur >> 10) & 0x7FFu, tw_cur >> 21};
-    const ParAgg total = par_decode(ag_cur);
-    const uint32_t in_x = (uint32_t)(st_cur & 1u);
-    const unsigned long long in_c = st_cur >> 1;
-    // replay from the carried-in state: kept (not consumed) and replaced bits
-    const uint32_t x_init = par_x(excl, in_x);
-    const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
-    uint32_t keptbits = 0, xbits = 0;
-    {
-      uint32_t x = x_init;
-#pragma unroll
-      for (int k = 0; k < ITEMS; ++k) {
-        if (j0 + k < len) {
-          const uint32_t prev = x;
-          x = ((cbits >> k) & 1u) & (prev ^ 1u);
-          keptbits |= (prev ^ 1u) << k;
-          xbits |= x << k;
-        }
-      }
-    }
-    // the rules of the replaced positions
     int32_t v[ITEMS + 1];
-    thread_steps<ITEMS>(sv, j0, v);
-    uint32_t slot[ITEMS], fl[ITEMS], fwdb;
-    lookup_pairs<ITEMS>(v, xbits, tab, slot, fl, fwdb, status);
-    // kept positions of the tile before j0: j0 minus the consumed ones (the
-    // carried-in position and the partner of every replaced position before
-    // j0, except a replaced j0 - 1 whose partner is j0 itself)
-    const uint32_t kept_base = j0 - in_x - c_init + x_init;
-    const uint64_t out_base = base - in_c + in_x;
-    const uint32_t shift = (uint32_t)(((reinterpret_cast<uintptr_t>(out) >> 2) + out_base) & 3u);
-    uint32_t lpk[ITEMS / 2];
-    uint32_t need = 0;
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const uint32_t lo = kept_base + __popc(keptbits & ((1u << k) - 1u));
-      if ((keptbits >> k) & 1u) {
-        int32_t val = v[k];
-        if ((xbits >> k) & 1u) {
-          const int32_t sym = temp_base + (int32_t)slot[k];
-          val = ((fwdb >> k) & 1u) ? sym : neg32(sym);
-          if (!(fl[k] & kFlagUsed)) need |= 1u << k;
-        }
-        so[shift + lo] = val;
-      }
-      if (k & 1) lpk[k >> 1] |= lo << 16;
-      else lpk[k >> 1] = lo & 0xFFFFu;
-    }
-    *reinterpret_cast<uint4 *>(&lidx[j0]) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
-    // rules chosen here whose slot was not yet flagged used: one flag update
-    // per distinct slot per warp (frequent pairs hit one slot from every
-    // lane), mirrored into the bitmap of used slots
-    if (__any_sync(0xffffffffu, need != 0)) {
-#pragma unroll
-      for (int k = 0; k < ITEMS; ++k) {
-        const bool nk = (need >> k) & 1u;
-        if (__any_sync(0xffffffffu, nk)) {
-          const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
-          if (nk && (peers & lanemask_lt()) == 0) {
-            atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
-            atomicOr(&used_bits[slot[k] >> 5], 1u << (slot[k] & 31));
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // positions consumed inside the tile: the carried-in one (in_x) plus the
-    // partner of every replaced position except a replaced last position,
-    // whose partner opens the next tile (x_out)
-    const uint32_t kept = len - in_x - par_c(total, in_x) + par_x(total, in_x);
-    stage_out_phased<BLOCK>(out + out_base, so, shift, kept);
-    const bool last_tile = base + len == n;
-    for (uint64_t t = s_tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
-      const uint64_t q = off[t];
-      if (q < base + len) new_off[t] = out_base + lidx[(uint32_t)(q - base)];
-      else if (last_tile && q == n) new_off[t] = out_base + kept;
-      else break;
-    }
-    if (last_tile && threadIdx.x == 0) status->u64[2] = out_base + kept;
+    thread_steps<ITEMS>(P.sv[b], j0, v);
+    emit_tile<BLOCK, ITEMS>(v, tile, n, tw_cur, st_cur, ag_cur, &s_tlo, off, ntrav, tab, temp_base, out, new_off,
+                            used_bits, status, so, lidx);
     pipe_release();
     if (!has_next) break;
     tile = next;
@@ -752,6 +769,44 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
     st_cur = st_next;
     ag_cur = ag_next;
   }
+}
+
+// The same replay with one tile per block and the steps read straight from
+// global memory (no staging pipeline).
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_apply_emit_flat(const int32_t *__restrict__ s, uint64_t n,
+                                                           const uint32_t *__restrict__ tword,
+                                                           const unsigned long long *__restrict__ tile_agg,
+                                                           const unsigned long long *__restrict__ state,
+                                                           const uint64_t *__restrict__ off, uint64_t ntrav,
+                                                           const uint64_t *__restrict__ tile_trav, PairTable tab,
+                                                           int32_t temp_base, int32_t *__restrict__ out,
+                                                           uint64_t *__restrict__ new_off, uint32_t *used_bits,
+                                                           DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
+  static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
+  __shared__ __align__(16) int32_t so[TILE + 4];
+  __shared__ __align__(16) uint16_t lidx[TILE];
+  __shared__ uint64_t s_tlo;
+  const uint64_t tile = blockIdx.x;
+  if (threadIdx.x == 0) s_tlo = tile_trav[tile];
+  const uint32_t tw = tword[tile * BLOCK + threadIdx.x];
+  const unsigned long long st = state[tile], ag = tile_agg[tile];
+  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  int32_t v[ITEMS + 1];
+  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+    const int4 a = *reinterpret_cast<const int4 *>(s + p0);
+    const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    v[8] = s[p0 + ITEMS];
+  } else {
+#pragma unroll
+    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+  }
+  emit_tile<BLOCK, ITEMS>(v, tile, n, tw, st, ag, &s_tlo, off, ntrav, tab, temp_base, out, new_off, used_bits, status,
+                          so, lidx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1251,8 +1306,14 @@ void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, c
 
 void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
                        const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                       uint32_t *used_bits, const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+                       uint32_t *used_bits, const ApplyScratch &w, bool flat, DevStatus *status,
+                       cudaStream_t st) {
   if (!n) return;
+  if (flat) {
+    k_apply_emit_flat<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
+        s, n, w.tword, w.tile_agg, w.state, off, ntrav, tile_trav, tab, temp_base, out, new_off, used_bits, status);
+    return;
+  }
   auto k = k_apply_emit<kBlock, kApplyItems>;
   k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), w.tword,
                                                                        w.tile_agg, w.state, off, ntrav, tile_trav,

@@ -73,10 +73,11 @@ void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, 
                            bool flat, DevStatus *status, cudaStream_t st);
 void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
 // Emit also sets bit `slot` of used_bits (cap bits, zeroed) for every slot
-// it flags used.
+// it flags used; flat = one tile per block, read from global memory.
 void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, const uint64_t *off, uint64_t ntrav,
                        const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out, uint64_t *new_off,
-                       uint32_t *used_bits, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+                       uint32_t *used_bits, const ApplyScratch &w, bool flat, DevStatus *status,
+                       cudaStream_t st);
 uint64_t apply_num_tiles(uint64_t n);
 // (key with the sign bit flipped, slot) of every slot set in the used bitmap
 // (cap bits), in no particular order; count in status->u64[3], entries

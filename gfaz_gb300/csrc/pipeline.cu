@@ -270,7 +270,8 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
   GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA, ntrav, n, w.tile_trav.ptr, st));
   const ApplyScratch sc{w.tword.ptr, w.tile_agg.ptr, w.tile_state.ptr, desc, counter};
   // classify variant: forced by option, else tuned per stream class like
-  // the count kernel (both write the same words)
+  // the count kernel (both write the same words); emit follows the choice
+  // (it flags rules used, so a second timing run would not be alike)
   bool flat = ctx.classify_kernel == 1;
   if (ctx.classify_kernel < 0) {
     const auto it = ctx.tuned.find({Context::kTuneClassify, cls});
@@ -289,7 +290,8 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
   GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify(A, n, heads, tab, sc, flat, ds, st));
   GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
   GFZ_TIMED_B(ctx, "apply_emit", 4.0 * n,
-              launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, used_bits, sc, ds, st));
+              launch_apply_emit(A, n, heads, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, used_bits, sc, flat,
+                                ds, st));
 }
 
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
