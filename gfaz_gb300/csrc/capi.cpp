@@ -217,7 +217,8 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
       require(value >= 0 && (value & (value - 1)) == 0, "first_table_cap must be 0 or a power of two");
       c.first_table_cap = (uint64_t)value;
     } else if (std::string(name) == "count_kernel") {
-      require(value >= -1 && value <= 2, "count_kernel must be -1 (tuned), 0 (tiled), 1 (tiled + warp folding) or 2 (flat)");
+      require(value >= -1 && value <= 3,
+              "count_kernel must be -1 (tuned), 0 (tiled), 1 (tiled + warp folding), 2 (flat) or 3 (flat, 4 pairs)");
       c.count_kernel = (int)value;
     } else if (std::string(name) == "classify_kernel") {
       require(value >= -1 && value <= 1, "classify_kernel must be -1 (tuned), 0 (persistent) or 1 (flat)");

@@ -313,6 +313,78 @@ __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict
   }
 }
 
+// Four consecutive pairs per thread, read straight from global memory;
+// a run of equal keys inside the thread is inserted once (flagged repeated
+// when longer than one), as in the tiled kernel, but with no barrier.
+__global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restrict__ s, uint64_t n,
+                                                        const uint32_t *__restrict__ heads, PairTable tab,
+                                                        DevStatus *status) {
+  constexpr int K = 4;
+  __shared__ uint32_t s_fresh, s_rep;
+  if (threadIdx.x == 0) {
+    s_fresh = 0;
+    s_rep = 0;
+  }
+  __syncthreads();
+  InsertCounts c;
+  const uint32_t mask = (uint32_t)(tab.cap - 1);
+  const bool aligned = (reinterpret_cast<uintptr_t>(s) & 15u) == 0;
+  bool full = false;
+  for (uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * K; p0 + 1 < n && !full;
+       p0 += (uint64_t)gridDim.x * blockDim.x * K) {
+    int32_t v[K + 1];
+    if (aligned && p0 + K < n) {
+      const int4 a = *reinterpret_cast<const int4 *>(s + p0);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+      v[4] = s[p0 + K];
+    } else {
+#pragma unroll
+      for (int k = 0; k <= K; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+    }
+    const uint32_t w = (uint32_t)(p0 >> 5);
+    const uint32_t hd = (uint32_t)((((unsigned long long)heads[w + 1] << 32) | heads[w]) >> (p0 & 31));
+    unsigned long long key[K];
+    uint32_t validb = 0, sameb = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      key[k] = canon2(pack2(v[k], v[k + 1]));
+      validb |= (uint32_t)(p0 + k + 1 < n && !((hd >> (k + 1)) & 1u)) << k;
+      if (k > 0) sameb |= (uint32_t)(key[k] == key[k - 1]) << k;
+    }
+    const uint32_t dropped = validb & (validb << 1) & sameb;
+    const uint32_t insb = validb & ~dropped;
+    const uint32_t moreb = insb & (dropped >> 1);
+    uint32_t h[K];
+    unsigned long long cur[K];
+    uint32_t fl[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      h[k] = hash_pair(key[k]) & mask;
+      cur[k] = kEmptyKey;
+      fl[k] = 0;
+      if ((insb >> k) & 1u) load_slot(&tab.slots[h[k]], cur[k], fl[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (((insb >> k) & 1u) && !full && !insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], c)) {
+        atomicOr(&status->err, kErrTableFull);
+        full = true;
+      }
+    }
+  }
+  const uint32_t f = __reduce_add_sync(0xffffffffu, c.fresh);
+  const uint32_t r = __reduce_add_sync(0xffffffffu, c.repeated);
+  if ((threadIdx.x & 31) == 0) {
+    if (f) atomicAdd(&s_fresh, f);
+    if (r) atomicAdd(&s_rep, r);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_fresh) atomicAdd(&status->u64[0], (unsigned long long)s_fresh);
+    if (s_rep) atomicAdd(&status->u64[1], (unsigned long long)s_rep);
+  }
+}
+
 // Traversal-head bitmap: bit off[t] for every t <= ntrav (bits cleared).
 __global__ void k_head_bits(const uint64_t *__restrict__ off, uint64_t ntrav, uint32_t *bits) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntrav; t += (uint64_t)gridDim.x * blockDim.x) {
@@ -1253,6 +1325,10 @@ void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, Pai
   if (!n) return;
   if (kind == CountKernel::kFlat) {
     k_count_flat<<<grid_for(n, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status);
+    return;
+  }
+  if (kind == CountKernel::kFlat4) {
+    k_count_flat4<<<grid_for((n + 3) / 4, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status);
     return;
   }
   constexpr uint64_t TILE = kBlock * kCountItems;

@@ -48,8 +48,9 @@ void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaS
 // contents (slot placement aside): kTiled stages tiles in shared memory and
 // folds runs of equal keys (streams with many repeats); kTiledWarpDedup
 // also folds equal keys across a warp; kFlat takes one pair per thread
-// without staging or barriers (streams of mostly new pairs).
-enum class CountKernel { kTiled = 0, kTiledWarpDedup = 1, kFlat = 2 };
+// without staging or barriers (streams of mostly new pairs); kFlat4 takes
+// four and folds their runs, still without barriers.
+enum class CountKernel { kTiled = 0, kTiledWarpDedup = 1, kFlat = 2, kFlat4 = 3 };
 void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
                         CountKernel kind, cudaStream_t st);
 

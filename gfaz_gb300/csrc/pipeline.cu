@@ -377,24 +377,33 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       if (tune) {
-        tab.prepare(cap, st);
-        ctx.reset_status();
-        const float t_tiled = ctx.time_launches(
-            [&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, CountKernel::kTiled, st); });
-        const DevStatus &s0 = ctx.read_status();
-        if ((s0.err & kErrTableFull) || s0.u64[0] * 10 > cap * 8) {
+        // every candidate kernel counts into a cleared table; the last run's
+        // table is kept (all fill it alike)
+        const CountKernel cand[] = {CountKernel::kTiled, CountKernel::kFlat, CountKernel::kFlat4};
+        float best = 0, t[3] = {0, 0, 0};
+        bool refill = false;
+        for (int i = 0; i < 3; ++i) {
+          tab.prepare(cap, st);
+          ctx.reset_status();
+          t[i] = ctx.time_launches([&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, cand[i], st); });
+          const DevStatus &s0 = ctx.read_status();
+          if ((s0.err & kErrTableFull) || s0.u64[0] * 10 > cap * 8) {
+            refill = true;
+            break;
+          }
+          if (i == 0 || t[i] < best) {
+            best = t[i];
+            kind = cand[i];
+          }
+        }
+        if (refill) {
           cap *= 4;
           continue;
         }
-        tab.prepare(cap, st);
-        ctx.reset_status();
-        const float t_flat = ctx.time_launches(
-            [&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, CountKernel::kFlat, st); });
-        kind = t_flat < t_tiled ? CountKernel::kFlat : CountKernel::kTiled;
         ctx.tuned[{Context::kTuneCount, cls}] = (int)kind;
         if (debug_enabled())
-          fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f ms, flat %.3f ms\n", cls,
-                  (unsigned long long)n, t_tiled, t_flat);
+          fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f, flat %.3f, flat4 %.3f ms\n", cls,
+                  (unsigned long long)n, t[0], t[1], t[2]);
         tune = false;
       } else {
         tab.prepare(cap, st);

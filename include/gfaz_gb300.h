@@ -74,10 +74,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * chunked append encoder (default 0 = 256, then 2048 and 16384 where a
  * chunk's fix-up does not settle, then one thread per traversal; any other
  * value tries that size, then one thread per traversal); "count_kernel" =
- * the pair-count kernel of the grammar rounds: -1 (default) = the faster of
- * the tiled and the flat kernel, timed the first time the context meets a
+ * the pair-count kernel of the grammar rounds: -1 (default) = the fastest of
+ * the tiled and the flat kernels, timed the first time the context meets a
  * stream class (length, repeat density) and remembered, 0 = tiled, 1 =
- * tiled with warp folding, 2 = flat (one pair per thread); "classify_kernel"
+ * tiled with warp folding, 2 = flat (one pair per thread), 3 = flat with
+ * four pairs per thread and run folding; "classify_kernel"
  * = the candidate classification pass, tuned alike: -1 (default), 0 =
  * persistent with staged tiles, 1 = flat (one tile per block). */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);

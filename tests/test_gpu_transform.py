@@ -160,7 +160,8 @@ def test_count_kernels_give_same_result(gpu_ctx):
     give the same grammar."""
     steps, off, _ = synthetic.cfg2_stream(seed=4, n_segments=80_000, n_paths=6)
     a = gz.encode(steps, off, ctx=gpu_ctx).arrays()
-    for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("warp_dedup", 1),
+    for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("count_kernel", 3),
+                     ("warp_dedup", 1),
                      ("classify_kernel", 0), ("classify_kernel", 1)]:
         ctx2 = gz.Context(0)
         ctx2.set_option(opt, val)
