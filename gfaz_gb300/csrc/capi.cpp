@@ -223,6 +223,12 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "classify_kernel") {
       require(value >= -1 && value <= 1, "classify_kernel must be -1 (tuned), 0 (persistent) or 1 (flat)");
       c.classify_kernel = (int)value;
+    } else if (std::string(name) == "hbm_budget") {
+      require(value >= 0, "hbm_budget must be >= 0");
+      c.hbm_budget = (uint64_t)value;
+    } else if (std::string(name) == "encode_chunk") {
+      require(value >= 0, "encode_chunk must be >= 0");
+      c.encode_chunk = (uint64_t)value;
     } else if (std::string(name) == "append_chunk") {
       require(value >= 0, "append_chunk must be >= 0");
       c.append_chunk = (uint64_t)value;
@@ -499,10 +505,7 @@ gfz_status gfz_encode(gfz_context *ctx, const int32_t *steps, const uint64_t *of
     if (where == GFZ_WHERE_DEVICE) {
       gfz::encode_traversals(c, steps, off, gfz::EncodeParams{rounds, delta_round}, g->g);
     } else {
-      gfz::DevVec<int32_t> d(c.stream());
-      d.resize(std::max<uint64_t>(n, 1));
-      if (n) gfz::cuda_check(cudaMemcpyAsync(d.ptr, steps, n * 4, cudaMemcpyHostToDevice, c.stream()), "upload");
-      gfz::encode_traversals(c, d.ptr, off, gfz::EncodeParams{rounds, delta_round}, g->g);
+      gfz::encode_host(c, {gfz::HostSeg{steps, n}}, off, gfz::EncodeParams{rounds, delta_round}, g->g);
     }
     *out = g.release();
   });

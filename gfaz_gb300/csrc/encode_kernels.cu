@@ -393,6 +393,34 @@ __global__ void k_head_bits(const uint64_t *__restrict__ off, uint64_t ntrav, ui
   }
 }
 
+// Head bitmap of the positions lo .. lo + span of a longer stream: bit q - lo
+// for every traversal start q = off[t] in that range (bits cleared).
+__global__ void k_head_bits_range(const uint64_t *__restrict__ off, uint64_t ntrav, uint64_t lo, uint64_t span,
+                                  uint32_t *bits) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntrav; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = off[t];
+    if (q >= lo && q - lo <= span) atomicOr(&bits[(q - lo) >> 5], 1u << ((q - lo) & 31));
+  }
+}
+
+// One delta round over a chunk: in[j + 1] is the step at chunk position j
+// and in[0] the step before the chunk (any value when the chunk opens the
+// stream); out[j] = in[j + 1] - in[j] unless position j opens a traversal
+// (heads, chunk-relative).  Max |out| folds into *max_abs.
+__global__ void __launch_bounds__(kBlock) k_delta_chunk(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                                        uint64_t len, const uint32_t *__restrict__ heads,
+                                                        uint32_t *max_abs) {
+  uint32_t m = 0;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < len; j += (uint64_t)gridDim.x * blockDim.x) {
+    const int32_t x = in[j + 1];
+    const int32_t d = ((heads[j >> 5] >> (j & 31)) & 1u) ? x : (int32_t)((uint32_t)x - (uint32_t)in[j]);
+    out[j] = d;
+    m = max(m, abs32(d));
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(max_abs, m);
+}
+
 // ---------------------------------------------------------------------------
 // Greedy replacement (apply)
 // ---------------------------------------------------------------------------
@@ -611,10 +639,13 @@ __global__ void __launch_bounds__(BLOCK, 4) k_apply_classify(const int32_t *__re
 // The same classification with one tile per block and the steps read
 // straight from global memory: no staging pipeline and no barrier besides
 // the block scan's, so more blocks are resident to hide the table probes.
+// n_pos positions are classified (tiles of the launch), n_data >= n_pos
+// steps are readable (one more when the stream continues past the range, as
+// in a chunk of a longer stream); heads covers positions 0 .. n_pos.
 template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__restrict__ s, uint64_t n,
-                                                               const uint32_t *__restrict__ heads, PairTable tab,
-                                                               uint32_t *__restrict__ tword,
+__global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__restrict__ s, uint64_t n_pos,
+                                                               uint64_t n_data, const uint32_t *__restrict__ heads,
+                                                               PairTable tab, uint32_t *__restrict__ tword,
                                                                unsigned long long *__restrict__ tile_agg,
                                                                DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
@@ -624,7 +655,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__
   const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
   int32_t v[ITEMS + 1];
   uint32_t validb = 0;
-  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+  if (p0 + ITEMS < n_data && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
     const int4 a = *reinterpret_cast<const int4 *>(s + p0);
     const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
@@ -632,13 +663,14 @@ __global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__
     v[8] = s[p0 + ITEMS];
   } else {
 #pragma unroll
-    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n_data ? s[p0 + k] : 0;
   }
-  if (p0 < n) {
+  if (p0 < n_pos) {
     const uint32_t w = (uint32_t)(p0 >> 5);
     const uint32_t hd = (uint32_t)((((unsigned long long)heads[w + 1] << 32) | heads[w]) >> (p0 & 31));
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) validb |= (uint32_t)(p0 + k < n && !((hd >> (k + 1)) & 1u)) << k;
+    for (int k = 0; k < ITEMS; ++k)
+      validb |= (uint32_t)(p0 + k < n_pos && p0 + k + 1 < n_data && !((hd >> (k + 1)) & 1u)) << k;
   }
   uint32_t slot[ITEMS], fl[ITEMS], fwdb;
   lookup_pairs<ITEMS>(v, validb, tab, slot, fl, fwdb, status);
@@ -697,8 +729,9 @@ template <int BLOCK, int ITEMS>
 __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_t tile, uint64_t n, uint32_t tw,
                                           unsigned long long st, unsigned long long ag, const uint64_t *s_tlo,
                                           const uint64_t *__restrict__ off, uint64_t ntrav, const PairTable &tab,
-                                          int32_t temp_base, int32_t *__restrict__ out, uint64_t *__restrict__ new_off,
-                                          uint32_t *used_bits, DevStatus *status, int32_t *so, uint16_t *lidx) {
+                                          int32_t temp_base, int32_t *__restrict__ out, uint64_t out_shift,
+                                          uint64_t *__restrict__ new_off, uint32_t *used_bits, DevStatus *status,
+                                          int32_t *so, uint16_t *lidx) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   const uint32_t j0 = threadIdx.x * ITEMS;
   const uint64_t base = tile * TILE;
@@ -732,7 +765,8 @@ __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_
   // j0, except a replaced j0 - 1 whose partner is j0 itself)
   const uint32_t kept_base = j0 - in_x - c_init + x_init;
   const uint64_t out_base = base - in_c + in_x;
-  const uint32_t shift = (uint32_t)(((reinterpret_cast<uintptr_t>(out) >> 2) + out_base) & 3u);
+  int32_t *dst = out + (out_base - out_shift);  // out holds output positions from out_shift on
+  const uint32_t shift = (uint32_t)((reinterpret_cast<uintptr_t>(dst) >> 2) & 3u);
   uint32_t lpk[ITEMS / 2];
   uint32_t need = 0;
 #pragma unroll
@@ -772,7 +806,7 @@ __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_
   // partner of every replaced position except a replaced last position,
   // whose partner opens the next tile (x_out)
   const uint32_t kept = len - in_x - par_c(total, in_x) + par_x(total, in_x);
-  stage_out_phased<BLOCK>(out + out_base, so, shift, kept);
+  stage_out_phased<BLOCK>(dst, so, shift, kept);
   const bool last_tile = base + len == n;
   for (uint64_t t = *s_tlo + threadIdx.x; t <= ntrav; t += BLOCK) {
     const uint64_t q = off[t];
@@ -831,8 +865,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
     }
     int32_t v[ITEMS + 1];
     thread_steps<ITEMS>(P.sv[b], j0, v);
-    emit_tile<BLOCK, ITEMS>(v, tile, n, tw_cur, st_cur, ag_cur, &s_tlo, off, ntrav, tab, temp_base, out, new_off,
-                            used_bits, status, so, lidx);
+    emit_tile<BLOCK, ITEMS>(v, tile, n, tw_cur, st_cur, ag_cur, &s_tlo, off, ntrav, tab, temp_base, out, 0,
+                            new_off, used_bits, status, so, lidx);
     pipe_release();
     if (!has_next) break;
     tile = next;
@@ -845,40 +879,46 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
 
 // The same replay with one tile per block and the steps read straight from
 // global memory (no staging pipeline).
+// Chunks of a longer stream: the launch covers tiles tile0 .. tile0 +
+// gridDim.x - 1 of the n-step stream, s holds its steps from position
+// pos_base on (one past the range when the stream continues), out its output
+// from position out_shift on.
 template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_apply_emit_flat(const int32_t *__restrict__ s, uint64_t n,
+__global__ void __launch_bounds__(BLOCK) k_apply_emit_flat(const int32_t *__restrict__ s, uint64_t pos_base,
+                                                           uint64_t tile0, uint64_t n,
                                                            const uint32_t *__restrict__ tword,
                                                            const unsigned long long *__restrict__ tile_agg,
                                                            const unsigned long long *__restrict__ state,
                                                            const uint64_t *__restrict__ off, uint64_t ntrav,
                                                            const uint64_t *__restrict__ tile_trav, PairTable tab,
                                                            int32_t temp_base, int32_t *__restrict__ out,
-                                                           uint64_t *__restrict__ new_off, uint32_t *used_bits,
-                                                           DevStatus *status) {
+                                                           uint64_t out_shift, uint64_t *__restrict__ new_off,
+                                                           uint32_t *used_bits, DevStatus *status) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
   static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
   __shared__ __align__(16) int32_t so[TILE + 4];
   __shared__ __align__(16) uint16_t lidx[TILE];
   __shared__ uint64_t s_tlo;
-  const uint64_t tile = blockIdx.x;
+  const uint64_t tile = tile0 + blockIdx.x;
   if (threadIdx.x == 0) s_tlo = tile_trav[tile];
   const uint32_t tw = tword[tile * BLOCK + threadIdx.x];
   const unsigned long long st = state[tile], ag = tile_agg[tile];
-  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;  // stream position
+  const int32_t *sl = s + (p0 - pos_base);
   int32_t v[ITEMS + 1];
-  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
-    const int4 a = *reinterpret_cast<const int4 *>(s + p0);
-    const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
+  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(sl) & 15u) == 0) {
+    const int4 a = *reinterpret_cast<const int4 *>(sl);
+    const int4 b = *reinterpret_cast<const int4 *>(sl + 4);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
     v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    v[8] = s[p0 + ITEMS];
+    v[8] = sl[ITEMS];
   } else {
 #pragma unroll
-    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? sl[k] : 0;
   }
-  emit_tile<BLOCK, ITEMS>(v, tile, n, tw, st, ag, &s_tlo, off, ntrav, tab, temp_base, out, new_off, used_bits, status,
-                          so, lidx);
+  emit_tile<BLOCK, ITEMS>(v, tile, n, tw, st, ag, &s_tlo, off, ntrav, tab, temp_base, out, out_shift, new_off,
+                          used_bits, status, so, lidx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1288,6 +1328,7 @@ inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
 constexpr int kDeltaItems = 16;
 constexpr int kCountItems = 8;
 constexpr int kApplyItems = 8;
+static_assert(kBlock * kApplyItems == kApplyTile, "apply tile size");
 
 void launch_delta_encode(const int32_t *in, int32_t *out, uint64_t n, const uint64_t *off, uint64_t ntrav,
                          uint32_t *max_abs, cudaStream_t st) {
@@ -1343,6 +1384,34 @@ void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, Pai
   }
 }
 
+void launch_head_bits_range(const uint64_t *off, uint64_t ntrav, uint64_t lo, uint64_t span, uint32_t *bits,
+                            cudaStream_t st) {
+  k_head_bits_range<<<grid_for(ntrav + 1, kBlock), kBlock, 0, st>>>(off, ntrav, lo, span, bits);
+}
+
+void launch_delta_chunk(const int32_t *in, int32_t *out, uint64_t len, const uint32_t *heads, uint32_t *max_abs,
+                        cudaStream_t st) {
+  if (!len) return;
+  k_delta_chunk<<<grid_for(len, kBlock), kBlock, 0, st>>>(in, out, len, heads, max_abs);
+}
+
+void launch_classify_chunk(const int32_t *s, uint64_t n_pos, uint64_t n_data, const uint32_t *heads, PairTable tab,
+                           uint64_t tile0, const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+  if (!n_pos) return;
+  k_apply_classify_flat<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n_pos), kBlock, 0, st>>>(
+      s, n_pos, n_data, heads, tab, w.tword + tile0 * kBlock, w.tile_agg + tile0, status);
+}
+
+void launch_emit_chunk(const int32_t *s, uint64_t pos_base, uint64_t tile0, uint64_t tiles, uint64_t n,
+                       const uint64_t *off, uint64_t ntrav, const uint64_t *tile_trav, PairTable tab,
+                       int32_t temp_base, int32_t *out, uint64_t out_shift, uint64_t *new_off, uint32_t *used_bits,
+                       const ApplyScratch &w, DevStatus *status, cudaStream_t st) {
+  if (!tiles) return;
+  k_apply_emit_flat<kBlock, kApplyItems><<<(unsigned)tiles, kBlock, 0, st>>>(
+      s, pos_base, tile0, n, w.tword, w.tile_agg, w.state, off, ntrav, tile_trav, tab, temp_base, out, out_shift,
+      new_off, used_bits, status);
+}
+
 uint64_t apply_num_tiles(uint64_t n) {
   constexpr uint64_t TILE = kBlock * kApplyItems;
   return (n + TILE - 1) / TILE;
@@ -1366,7 +1435,7 @@ void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, 
   if (!n) return;
   if (flat) {
     k_apply_classify_flat<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
-        s, n, heads, tab, w.tword, w.tile_agg, status);
+        s, n, n, heads, tab, w.tword, w.tile_agg, status);
     return;
   }
   auto k = k_apply_classify<kBlock, kApplyItems>;
@@ -1387,7 +1456,8 @@ void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, cons
   if (!n) return;
   if (flat) {
     k_apply_emit_flat<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
-        s, n, w.tword, w.tile_agg, w.state, off, ntrav, tile_trav, tab, temp_base, out, new_off, used_bits, status);
+        s, 0, 0, n, w.tword, w.tile_agg, w.state, off, ntrav, tile_trav, tab, temp_base, out, 0, new_off, used_bits,
+        status);
     return;
   }
   auto k = k_apply_emit<kBlock, kApplyItems>;

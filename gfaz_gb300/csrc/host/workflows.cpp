@@ -381,14 +381,9 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   for (uint64_t t = 0; t < np; ++t) off[t + 1] = g.paths.offsets[t + 1];
   for (uint64_t t = 0; t < nw; ++t) off[np + t + 1] = NP + g.walks.offsets[t + 1];
   cudaStream_t st = ctx.stream();
-  DevVec<int32_t> d_in(st);
-  d_in.resize(std::max<uint64_t>(NP + NW, 1));
-  if (NP) cuda_check(cudaMemcpyAsync(d_in.ptr, g.paths.steps.data(), NP * 4, cudaMemcpyHostToDevice, st), "upload");
-  if (NW)
-    cuda_check(cudaMemcpyAsync(d_in.ptr + NP, g.walks.steps.data(), NW * 4, cudaMemcpyHostToDevice, st), "upload");
   Grammar gram(st);
-  encode_traversals(ctx, d_in.ptr, off, EncodeParams{rounds, delta_round}, gram);
-  d_in.release();
+  encode_host(ctx, {HostSeg{g.paths.steps.data(), NP}, HostSeg{g.walks.steps.data(), NW}}, off,
+              EncodeParams{rounds, delta_round}, gram);
 
   // rule columns (split + delta on the device)
   DevVec<int32_t> dfirst(st), dsecond(st);

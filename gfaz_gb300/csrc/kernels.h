@@ -80,12 +80,34 @@ void launch_apply_emit(const int32_t *s, uint64_t n, const uint32_t *heads, cons
                        uint32_t *used_bits, const ApplyScratch &w, bool flat, DevStatus *status,
                        cudaStream_t st);
 uint64_t apply_num_tiles(uint64_t n);
+constexpr uint64_t kApplyTile = 2048;  // steps per apply tile
 // (key with the sign bit flipped, slot) of every slot set in the used bitmap
 // (cap bits), in no particular order; count in status->u64[3], entries
 // beyond cap_out dropped with kErrLength.
 void launch_collect_used(const uint32_t *bits, uint64_t cap, PairTable tab, unsigned long long *keys_out,
                          uint32_t *slots_out, uint64_t cap_out, DevStatus *status, cudaStream_t st);
 uint64_t apply_state_blocks(uint64_t n);
+// ---- chunks of a stream too long for HBM ---------------------------------
+// Head bitmap of positions lo .. lo + span (head_words(span) words, zeroed).
+void launch_head_bits_range(const uint64_t *off, uint64_t ntrav, uint64_t lo, uint64_t span, uint32_t *bits,
+                            cudaStream_t st);
+// One delta round over len steps: in[0] = the step before the chunk,
+// in[1 .. len] the chunk; heads chunk-relative; max |out| into *max_abs.
+void launch_delta_chunk(const int32_t *in, int32_t *out, uint64_t len, const uint32_t *heads, uint32_t *max_abs,
+                        cudaStream_t st);
+// Classification of n_pos positions (a whole number of apply tiles unless
+// the stream ends) whose words go to tiles tile0 ... of w; s holds n_data
+// steps (n_pos + 1 when the stream continues).
+void launch_classify_chunk(const int32_t *s, uint64_t n_pos, uint64_t n_data, const uint32_t *heads, PairTable tab,
+                           uint64_t tile0, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+// Emit of tiles tile0 .. tile0 + tiles - 1 of the n-step stream: s holds
+// the steps from position pos_base on, out the output from output position
+// out_shift on; offsets, states and words are the whole stream's.
+void launch_emit_chunk(const int32_t *s, uint64_t pos_base, uint64_t tile0, uint64_t tiles, uint64_t n,
+                       const uint64_t *off, uint64_t ntrav, const uint64_t *tile_trav, PairTable tab,
+                       int32_t temp_base, int32_t *out, uint64_t out_shift, uint64_t *new_off, uint32_t *used_bits,
+                       const ApplyScratch &w, DevStatus *status, cudaStream_t st);
+
 // tile_trav[k] = first traversal t with off[t] >= k * (apply tile), for the
 // apply_num_tiles(n) tiles.
 void launch_tile_trav(const uint64_t *off, uint64_t ntrav, uint64_t n, uint64_t *tile_trav, cudaStream_t st);

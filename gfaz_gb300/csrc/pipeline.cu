@@ -249,6 +249,44 @@ void Context::clear_kernel_stats() {
 // ---------------------------------------------------------------------------
 // Compression
 // ---------------------------------------------------------------------------
+// Used rules of one round: the (key, slot) list and the sort's scratch.
+struct SortWork {
+  explicit SortWork(cudaStream_t st) : keys(st), keys_tmp(st), slots(st), slots_tmp(st), hist(st) {}
+  DevVec<unsigned long long> keys, keys_tmp;
+  DevVec<uint32_t> slots, slots_tmp, hist;
+};
+
+// Sorts the U used rules of su.keys / su.slots by signed key (on the key
+// bytes in byte_mask), gives them ids next_id + rank in the table and
+// appends their keys to rules after the first nrules entries.
+static void sort_used_rules(Context &ctx, PairTable tab, uint64_t U, uint32_t byte_mask, uint32_t next_id,
+                            SortWork &su, DevVec<long long> &rules, uint64_t nrules) {
+  cudaStream_t st = ctx.stream();
+  DevStatus *ds = ctx.dstatus();
+  su.keys_tmp.resize(U);
+  su.slots_tmp.resize(U);
+  su.hist.resize(8 * 256);
+  cuda_check(cudaMemsetAsync(su.hist.ptr, 0, 8 * 256 * sizeof(uint32_t), st), "histogram clear");
+  ctx.reset_status();
+  bool in_tmp = false;
+  GFZ_TIMED(ctx, "radix_sort", launch_sort_hist(su.keys.ptr, U, byte_mask, su.hist.ptr, st));
+  for (int b = 0; b < 8; ++b) {
+    if (!((byte_mask >> b) & 1u)) continue;
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(sort_tiles(U) * 256, &counter);
+    GFZ_TIMED(ctx, "radix_sort",
+              launch_sort_pass(in_tmp ? su.keys_tmp.ptr : su.keys.ptr, in_tmp ? su.slots_tmp.ptr : su.slots.ptr,
+                               in_tmp ? su.keys.ptr : su.keys_tmp.ptr, in_tmp ? su.slots.ptr : su.slots_tmp.ptr, U, b,
+                               su.hist.ptr, desc, counter, &ds->err, st));
+    in_tmp = !in_tmp;
+  }
+  rules.reserve(nrules + U, true);
+  rules.size = nrules + U;
+  GFZ_TIMED(ctx, "assign_ids",
+            launch_assign_ids(in_tmp ? su.keys_tmp.ptr : su.keys.ptr, in_tmp ? su.slots_tmp.ptr : su.slots.ptr, U,
+                              next_id, tab, rules.ptr + nrules, st));
+}
+
 // Greedy left-to-right replacement of A[0, n) (traversal offsets offA, head
 // bitmap heads): inside each traversal, a position whose canonical pair is
 // REPEATED in tab and whose predecessor was not replaced becomes
@@ -339,8 +377,10 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
 
   DevVec<long long> rules(st);
   Table tab(st);
-  DevVec<unsigned long long> ukeys(st), ukeys_tmp(st);
-  DevVec<uint32_t> uslots(st), uslots_tmp(st), hist(st), heads(st), used_bits(st);
+  SortWork su(st);
+  DevVec<unsigned long long> &ukeys = su.keys;
+  DevVec<uint32_t> &uslots = su.slots;
+  DevVec<uint32_t> heads(st), used_bits(st);
   ReplaceWork rw(st);
 
   uint64_t n = N;
@@ -449,28 +489,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     uint32_t byte_mask = 0;
     for (int b = 0; b < 8; ++b)
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
-    ukeys_tmp.resize(U);
-    uslots_tmp.resize(U);
-    hist.resize(8 * 256);
-    cuda_check(cudaMemsetAsync(hist.ptr, 0, 8 * 256 * sizeof(uint32_t), st), "histogram clear");
-    ctx.reset_status();
-    bool in_tmp = false;
-    GFZ_TIMED(ctx, "radix_sort", launch_sort_hist(ukeys.ptr, U, byte_mask, hist.ptr, st));
-    for (int b = 0; b < 8; ++b) {
-      if (!((byte_mask >> b) & 1u)) continue;
-      uint32_t *counter;
-      unsigned long long *desc = ctx.lookback(sort_tiles(U) * 256, &counter);
-      GFZ_TIMED(ctx, "radix_sort",
-                launch_sort_pass(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr,
-                                 in_tmp ? ukeys.ptr : ukeys_tmp.ptr, in_tmp ? uslots.ptr : uslots_tmp.ptr, U, b,
-                                 hist.ptr, desc, counter, &ds->err, st));
-      in_tmp = !in_tmp;
-    }
-    rules.reserve(g.nrules + U, true);
-    rules.size = g.nrules + U;
-    GFZ_TIMED(ctx, "assign_ids",
-              launch_assign_ids(in_tmp ? ukeys_tmp.ptr : ukeys.ptr, in_tmp ? uslots_tmp.ptr : uslots.ptr, U, next_id,
-                                tab.view(cap), rules.ptr + g.nrules, st));
+    sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
     GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
     ctx.read_status();
     ctx.check_status("rule sort");
@@ -495,6 +514,308 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   rules.size = g.nrules;
   g.rules = std::move(rules);
   cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+// ---------------------------------------------------------------------------
+// Compression of a host-resident stream in HBM-sized chunks
+// ---------------------------------------------------------------------------
+namespace {
+
+// Host buffer of int32 steps, page-locked when the allocation succeeds.
+struct HostBuf {
+  int32_t *p = nullptr;
+  bool pinned = false;
+  std::vector<int32_t> v;
+  explicit HostBuf(uint64_t n) {
+    if (cudaHostAlloc(reinterpret_cast<void **>(&p), std::max<uint64_t>(n, 1) * sizeof(int32_t),
+                      cudaHostAllocDefault) == cudaSuccess) {
+      pinned = true;
+    } else {
+      cudaGetLastError();
+      v.resize(std::max<uint64_t>(n, 1));
+      p = v.data();
+    }
+  }
+  ~HostBuf() {
+    if (pinned) cudaFreeHost(p);
+  }
+  HostBuf(const HostBuf &) = delete;
+  HostBuf &operator=(const HostBuf &) = delete;
+};
+
+// Copies steps [a, b) of the stream made of segs (back to back) to dst.
+void upload_range(const std::vector<HostSeg> &segs, uint64_t a, uint64_t b, int32_t *dst, cudaStream_t st) {
+  uint64_t base = 0;
+  for (const HostSeg &g : segs) {
+    const uint64_t lo = std::max(a, base), hi = std::min(b, base + g.n);
+    if (lo < hi)
+      cuda_check(cudaMemcpyAsync(dst + (lo - a), g.p + (lo - base), (hi - lo) * sizeof(int32_t), cudaMemcpyDefault, st),
+                 "chunk upload");
+    base += g.n;
+  }
+}
+
+}  // namespace
+
+void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
+                         const EncodeParams &p, uint64_t chunk, Grammar &g) {
+  cudaStream_t st = ctx.stream();
+  if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
+  const uint64_t ntrav = h_off.size() - 1;
+  const uint64_t N = h_off.back();
+  for (uint64_t t = 0; t < ntrav; ++t)
+    if (h_off[t + 1] < h_off[t]) throw std::invalid_argument("traversal offsets must be non-decreasing");
+  if (h_off[0] != 0) throw std::invalid_argument("offsets must start at 0");
+  uint64_t have = 0;
+  for (const HostSeg &sg : input) have += sg.n;
+  if (have != N) throw std::invalid_argument("input segments do not hold the offsets' steps");
+  const uint64_t TILE = kApplyTile;
+  const uint64_t C = std::max<uint64_t>(TILE, chunk / TILE * TILE);
+  const int dr = std::max(0, p.delta_round);
+  g.ntrav = ntrav;
+  g.delta_round = dr;
+  g.rounds_done = 0;
+  g.nrules = 0;
+
+  DevVec<uint64_t> offA(st), offB(st);
+  offA.resize(ntrav + 1);
+  offB.resize(ntrav + 1);
+  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
+             "offsets upload");
+  // chunk buffers: steps in (one before / one after the chunk), steps out,
+  // chunk-relative head bitmap
+  DevVec<int32_t> cin(st), cout(st);
+  cin.resize(C + 2);
+  cout.resize(C);
+  DevVec<uint32_t> hloc(st);
+  hloc.resize(head_words(C + 1));
+  auto local_heads = [&](const uint64_t *off, uint64_t lo, uint64_t span) {
+    cuda_check(cudaMemsetAsync(hloc.ptr, 0, head_words(C + 1) * sizeof(uint32_t), st), "head bitmap clear");
+    launch_head_bits_range(off, ntrav, lo, span, hloc.ptr, st);
+  };
+  HostBuf X(N), Y(N);
+  ctx.reset_status();
+  DevStatus *ds = ctx.dstatus();
+  // delta rounds (or the max |x| of the raw steps), chunk by chunk
+  std::vector<HostSeg> cur = input;
+  HostBuf *nxt = &X;
+  if (dr == 0) {
+    for (uint64_t c0 = 0; c0 < N; c0 += C) {
+      const uint64_t c1 = std::min(c0 + C, N);
+      upload_range(cur, c0, c1, cin.ptr, st);
+      GFZ_TIMED_B(ctx, "max_abs", 4.0 * (c1 - c0), launch_max_abs(cin.ptr, c1 - c0, &ds->aux, st));
+    }
+  }
+  for (int r = 0; r < dr; ++r) {
+    for (uint64_t c0 = 0; c0 < N; c0 += C) {
+      const uint64_t c1 = std::min(c0 + C, N);
+      if (c0) {
+        upload_range(cur, c0 - 1, c1, cin.ptr, st);
+      } else {
+        cuda_check(cudaMemsetAsync(cin.ptr, 0, sizeof(int32_t), st), "chunk clear");
+        upload_range(cur, 0, c1, cin.ptr + 1, st);
+      }
+      local_heads(offA.ptr, c0, c1 - c0);
+      GFZ_TIMED_B(ctx, "delta_encode", 8.0 * (c1 - c0),
+                  launch_delta_chunk(cin.ptr, cout.ptr, c1 - c0, hloc.ptr, &ds->aux, st));
+      cuda_check(cudaMemcpyAsync(nxt->p + c0, cout.ptr, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                 "chunk download");
+    }
+    cuda_check(cudaStreamSynchronize(st), "stream sync");
+    cur = {HostSeg{nxt->p, N}};
+    nxt = nxt == &X ? &Y : &X;
+  }
+  const DevStatus &s0 = ctx.read_status();
+  const uint32_t max_abs = s0.aux;
+  if (max_abs == UINT32_MAX)
+    throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
+  uint32_t next_id = max_abs + 1;
+  g.layer_start = next_id;
+
+  DevVec<long long> rules(st);
+  Table tab(st);
+  SortWork su(st);
+  DevVec<uint32_t> used_bits(st);
+  ReplaceWork rw(st);
+  std::vector<unsigned long long> h_state;
+  uint64_t n = N;
+  uint64_t prev_distinct = 0;
+  for (int round = 0; round < p.rounds; ++round) {
+    if (n < 2) break;
+    uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
+    est = std::min(est, n);
+    uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
+    if (round == 0 && ctx.first_table_cap) cap = ctx.first_table_cap;
+    // the chunk with the step after it (pairs across chunk edges)
+    auto load_chunk = [&](uint64_t c0, uint64_t c1) {
+      const uint64_t e = std::min(c1 + 1, n);
+      upload_range(cur, c0, e, cin.ptr, st);
+      local_heads(offA.ptr, c0, c1 - c0);
+      return e - c0;
+    };
+    const CountKernel kind = round == 0 ? CountKernel::kFlat4 : CountKernel::kFlat;
+    uint64_t distinct = 0, repeated = 0;
+    for (;;) {
+      if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
+      tab.prepare(cap, st);
+      ctx.reset_status();
+      for (uint64_t c0 = 0; c0 < n; c0 += C) {
+        const uint64_t c1 = std::min(c0 + C, n);
+        const uint64_t nd = load_chunk(c0, c1);
+        GFZ_TIMED_B(ctx, "count_pairs", 4.0 * (c1 - c0),
+                    launch_count_pairs(cin.ptr, nd, hloc.ptr, tab.view(cap), ds, kind, st));
+      }
+      const DevStatus &s = ctx.read_status();
+      distinct = s.u64[0];
+      repeated = s.u64[1];
+      if ((s.err & kErrTableFull) || distinct * 10 > cap * 8) {
+        cap *= 4;
+        continue;
+      }
+      ctx.check_status("count_pairs");
+      break;
+    }
+    prev_distinct = distinct;
+    if (repeated == 0) break;
+    if ((uint64_t)next_id + cap >= (1ULL << 31))
+      throw std::overflow_error("Compression workflow error: rule id space exhausted");
+    const int32_t temp_base = (int32_t)next_id;
+    // classification of every chunk, then the carried-in state of every tile
+    const uint64_t tiles = apply_num_tiles(n);
+    rw.tile_trav.resize(tiles);
+    rw.tword.resize(tiles * 256);
+    rw.tile_agg.resize(tiles);
+    rw.tile_state.resize(tiles);
+    ctx.reset_status();
+    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
+    used_bits.resize((cap + 31) / 32);
+    cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
+    const ApplyScratch sc{rw.tword.ptr, rw.tile_agg.ptr, rw.tile_state.ptr, desc, counter};
+    for (uint64_t c0 = 0; c0 < n; c0 += C) {
+      const uint64_t c1 = std::min(c0 + C, n);
+      const uint64_t nd = load_chunk(c0, c1);
+      GFZ_TIMED_B(ctx, "apply_classify", 4.0 * (c1 - c0),
+                  launch_classify_chunk(cin.ptr, c1 - c0, nd, hloc.ptr, tab.view(cap), c0 / TILE, sc, ds, st));
+    }
+    GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
+    GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, rw.tile_trav.ptr, st));
+    h_state.resize(tiles);
+    cuda_check(cudaMemcpyAsync(h_state.data(), rw.tile_state.ptr, tiles * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st),
+               "tile states");
+    ctx.read_status();
+    ctx.check_status("apply");
+    // output position of a chunk's first kept step: tile start minus the
+    // steps consumed before it, plus its own carried-in consumption
+    auto out_start = [&](uint64_t c0) {
+      if (c0 >= n) return (uint64_t)0;
+      const unsigned long long stt = h_state[c0 / TILE];
+      return c0 - (uint64_t)(stt >> 1) + (uint64_t)(stt & 1u);
+    };
+    for (uint64_t c0 = 0; c0 < n; c0 += C) {
+      const uint64_t c1 = std::min(c0 + C, n);
+      load_chunk(c0, c1);
+      const uint64_t o0 = out_start(c0);
+      GFZ_TIMED_B(ctx, "apply_emit", 4.0 * (c1 - c0),
+                  launch_emit_chunk(cin.ptr, c0, c0 / TILE, apply_num_tiles(c1 - c0), n, offA.ptr, ntrav,
+                                    rw.tile_trav.ptr, tab.view(cap), temp_base, cout.ptr, o0, offB.ptr,
+                                    used_bits.ptr, sc, ds, st));
+      if (c1 < n) {
+        const uint64_t o1 = out_start(c1);
+        if (o1 > o0)
+          cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                     "chunk download");
+      } else {
+        const DevStatus &se = ctx.read_status();
+        const uint64_t n_end = se.u64[2];
+        if (n_end > o0)
+          cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (n_end - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                     "chunk download");
+      }
+    }
+    su.keys.resize(std::max<uint64_t>(repeated, 1));
+    su.slots.resize(std::max<uint64_t>(repeated, 1));
+    GFZ_TIMED_B(ctx, "collect_used", cap / 8.0,
+                launch_collect_used(used_bits.ptr, cap, tab.view(cap), su.keys.ptr, su.slots.ptr,
+                                    std::max<uint64_t>(repeated, 1), ds, st));
+    const DevStatus &s1 = ctx.read_status();
+    ctx.check_status("apply");
+    const uint64_t n_out = s1.u64[2];
+    const uint64_t U = s1.u64[3];
+    const unsigned long long diff = s1.u64[4] ^ s1.u64[5];
+    if (U == 0) break;
+    uint32_t byte_mask = 0;
+    for (int b = 0; b < 8; ++b)
+      if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
+    sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
+    // final ids into the round's output, chunk by chunk
+    for (uint64_t o0 = 0; o0 < n_out; o0 += C) {
+      const uint64_t o1 = std::min(o0 + C, n_out);
+      cuda_check(cudaMemcpyAsync(cout.ptr, nxt->p + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                 "chunk upload");
+      GFZ_TIMED_B(ctx, "remap", 8.0 * (o1 - o0), launch_remap(cout.ptr, o1 - o0, temp_base, tab.slots.ptr, st));
+      cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                 "chunk download");
+    }
+    ctx.read_status();
+    ctx.check_status("rule sort");
+    if (debug_enabled())
+      fprintf(stderr, "[gfaz gb300] chunked round %d: n=%llu chunk=%llu cap=%llu distinct=%llu used=%llu n_out=%llu\n",
+              round + 1, (unsigned long long)n, (unsigned long long)C, (unsigned long long)cap,
+              (unsigned long long)distinct, (unsigned long long)U, (unsigned long long)n_out);
+    g.nrules += U;
+    next_id += (uint32_t)U;
+    n = n_out;
+    cur = {HostSeg{nxt->p, n}};
+    nxt = nxt == &X ? &Y : &X;
+    offA.swap(offB);
+    g.rounds_done++;
+  }
+  g.next_id = next_id;
+  g.enc.resize(std::max<uint64_t>(n, 1));
+  g.enc.size = n;
+  upload_range(cur, 0, n, g.enc.ptr, st);
+  g.off = std::move(offA);
+  g.h_off.resize(ntrav + 1);
+  cuda_check(cudaMemcpyAsync(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
+             "offsets download");
+  rules.size = g.nrules;
+  g.rules = std::move(rules);
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
+                 const EncodeParams &p, Grammar &g) {
+  const uint64_t N = h_off.empty() ? 0 : h_off.back();
+  uint64_t chunk = ctx.encode_chunk;
+  if (!chunk && ctx.hbm_budget) {
+    // resident: input, two stream buffers, per-tile words, a pair table
+    const uint64_t resident = 12 * N + N / 2 + (64ull << 20) + 16 * std::min<uint64_t>(N, 1ull << 23);
+    if (resident > ctx.hbm_budget) {
+      // chunked: per-tile words and tile arrays of the whole stream, a pair
+      // table, the final stream; chunk buffers of 12 bytes per step
+      const uint64_t fixed = N / 2 + N / 64 + 4 * N / 8 + (64ull << 20) + 16 * std::min<uint64_t>(N, 1ull << 24);
+      if (ctx.hbm_budget <= fixed + 12 * kApplyTile)
+        throw std::runtime_error("HBM budget too small for " + std::to_string(N) + " steps");
+      chunk = (ctx.hbm_budget - fixed) / 12;
+    }
+  }
+  if (chunk) {
+    encode_host_chunked(ctx, input, h_off, p, chunk, g);
+    return;
+  }
+  cudaStream_t st = ctx.stream();
+  DevVec<int32_t> d(st);
+  d.resize(std::max<uint64_t>(N, 1));
+  uint64_t at = 0;
+  for (const HostSeg &sg : input) {
+    if (sg.n) cuda_check(cudaMemcpyAsync(d.ptr + at, sg.p, sg.n * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload");
+    at += sg.n;
+  }
+  if (at != N) throw std::invalid_argument("input segments do not hold the offsets' steps");
+  encode_traversals(ctx, d.ptr, h_off, p, g);
 }
 
 void rule_columns_delta(Context &ctx, const Grammar &g, DevVec<int32_t> &first, DevVec<int32_t> &second) {

@@ -128,6 +128,8 @@ class Context {
   bool warp_dedup = false;
   uint64_t first_table_cap = 0;  // pair-table slots of the first round (0 = automatic)
   uint64_t append_chunk = 0;     // steps per chunk of the chunked stack pass (0 = the automatic ladder)
+  uint64_t hbm_budget = 0;       // device bytes host-input compression may use (0 = no limit)
+  uint64_t encode_chunk = 0;     // steps per chunk of host-input compression (0 = from the budget)
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   // Tuner: (kernel, stream class) -> the variant that was faster the first
@@ -192,6 +194,24 @@ struct EncodeParams {
 // host offsets).  The input is not modified.
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
                        const EncodeParams &p, Grammar &g);
+
+// A piece of a host-resident stream.
+struct HostSeg {
+  const int32_t *p;
+  uint64_t n;
+};
+// The same compression for a stream in host memory (the segments back to
+// back), moved through HBM in chunks of `chunk` steps (rounded down to whole
+// apply tiles): only the pair table, per-tile words and chunk buffers live
+// on the device, and the result is identical to encode_traversals'.
+void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
+                         const EncodeParams &p, uint64_t chunk, Grammar &g);
+
+// Compression of host-resident input: resident in HBM when its working set
+// (about 12.5 bytes per step) fits ctx.hbm_budget, else in chunks
+// (encode_host_chunked) sized from the budget or ctx.encode_chunk.
+void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
+                 const EncodeParams &p, Grammar &g);
 
 // Splits the packed rulebook into first/second columns on the device and
 // delta-codes each column (compression_utils.cpp:165-193).

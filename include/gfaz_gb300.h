@@ -80,7 +80,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * tiled with warp folding, 2 = flat (one pair per thread), 3 = flat with
  * four pairs per thread and run folding; "classify_kernel"
  * = the candidate classification pass, tuned alike: -1 (default), 0 =
- * persistent with staged tiles, 1 = flat (one tile per block). */
+ * persistent with staged tiles, 1 = flat (one tile per block);
+ * "hbm_budget" = device bytes that compression of host-resident input may
+ * use (default 0 = no limit): above it the stream stays in host memory and
+ * passes through HBM in chunks, with identical output; "encode_chunk" =
+ * steps per such chunk, forcing chunked compression (default 0). */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
