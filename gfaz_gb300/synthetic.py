@@ -10,6 +10,12 @@ synthetic graphs with their shapes stand in for them:
   10-200 segments, 90 haplotypes of ~6M steps, 1% reversed alleles.
 * ``cfg3`` - 2M-segment bubble graph with 2,000 W-lines whose step counts
   are lognormal (median 50k, sigma 2, clamped to [100, 20M]).
+* ``cfg4`` - whole-genome shape: 24 independent components built by the
+  config-1 rules, 180 haplotypes each walking every component once (4,320
+  W-lines), 3.6B steps in all.  The shape's stated 40M segments and ~20M
+  steps per haplotype cannot both hold for a config-1 graph (a haplotype
+  takes 11 of every 12 segments); the step count is kept, which gives ~21.8M
+  segments.
 
 Randomness is integer-only (splitmix64 over counters, comparisons against
 exact integer thresholds) so that the same seed yields the same graph on
@@ -282,6 +288,46 @@ def cfg3_stream(seed: int = 3, n_backbone: int = 1_666_667, n_walks: int = 2000,
     off = np.zeros(n_walks + 1, np.uint64)
     np.cumsum(lens, out=off[1:])
     return np.concatenate(walks), off, nblk * blk, meta
+
+
+def cfg4_stream(seed: int = 4, n_components: int = 24, n_haps: int = 180, line_steps: int = 833_327,
+                rev_num: int = 2, rev_den: int = 100):
+    """Whole-genome-shaped walk stream: component c holds blocks of 10
+    backbone segments followed by a 2-allele bubble; haplotype h walks every
+    component from its first block to its last, taking allele (bit of a
+    per-(c, h) random stream) reversed with rev_num/rev_den probability.
+    W-line (c, h) is traversal h * n_components + c.  line_steps is rounded
+    down to whole blocks (11 steps).  Returns (steps int32, offsets uint64,
+    num_segments, walk_meta)."""
+    bubble_every = 10
+    per_blk = bubble_every + 1
+    blk = bubble_every + 2
+    nblk = max(1, line_steps // per_blk)
+    L = nblk * per_blk
+    seg_per_comp = nblk * blk
+    n_lines = n_components * n_haps
+    steps = np.empty(n_lines * L, np.int32)
+    cols = np.arange(bubble_every, dtype=np.int64)
+
+    def fill(line):
+        h, c = divmod(line, n_components)
+        base = 1 + c * seg_per_comp + np.arange(nblk, dtype=np.int64) * blk
+        u = rng_u64(seed, 100_000 + line, nblk)
+        choice = (u & np.uint64(1)).astype(np.int64)
+        rev = _bernoulli(u >> np.uint64(1), rev_num, rev_den)
+        out = steps[line * L:(line + 1) * L].reshape(nblk, per_blk)
+        out[:, :bubble_every] = base[:, None] + cols[None, :]
+        allele = base + bubble_every + choice
+        out[:, bubble_every] = np.where(rev, -allele, allele)
+        return None
+
+    _parallel_map(fill, range(n_lines))
+    off = np.arange(n_lines + 1, dtype=np.uint64) * np.uint64(L)
+    meta = []
+    for line in range(n_lines):
+        h, c = divmod(line, n_components)
+        meta.append((f"HG{h // 2:03d}", h % 2 + 1, f"chr{c + 1}", 0, L * 30))
+    return steps, off, n_components * seg_per_comp, meta
 
 
 def serve_paths(seed: int = 5, n_backbone: int = 600_000, n_paths: int = 64, median: float = 2e5,
