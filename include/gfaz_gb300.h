@@ -59,7 +59,10 @@ int gfz_has_gpu(void);
 unsigned gfz_zstd_version(void);
 
 /* ---- contexts ------------------------------------------------------------ */
-/* cuda_stream may be NULL (the context creates its own stream). */
+/* cuda_stream may be NULL (the context creates its own stream).  Grammars
+ * free their device memory on the stream of the context that made them:
+ * free them before that context, and keep a caller's stream alive until
+ * the context is destroyed. */
 gfz_status gfz_context_create(int device, void *cuda_stream, gfz_context **out);
 void gfz_context_destroy(gfz_context *ctx);
 /* Records CUDA events around every kernel launch when enabled. */
