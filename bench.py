@@ -47,7 +47,7 @@ HBM_FALLBACK = 6800.0
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the cfg2 workload (testing)")
@@ -93,18 +93,29 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Starts sampling every 50 ms and waits (up to 3 s) for the first
+        sample, so that the timed region that follows is covered."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.perf_counter(), ln.strip()))
+
+    def begin(self):
+        self.t_begin = time.perf_counter()
+
+    def end(self):
+        self.t_end = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
@@ -114,9 +125,12 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        lo, hi = getattr(self, "t_begin", 0.0), getattr(self, "t_end", float("inf"))
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
+            if not lo <= t <= hi:
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -370,6 +384,7 @@ def main():
     with torch.cuda.stream(stream):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
+        clocks.begin()
         t0.record(stream)
         for i in range(args.steps):
             ev[3 * i].record(stream)
@@ -380,6 +395,7 @@ def main():
             del g
         t1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     barrier()
     clk = clocks.stop()
     ms = t0.elapsed_time(t1) / args.steps

@@ -117,6 +117,24 @@ Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullp
   std::memset(h_status_, 0, sizeof(DevStatus));
   cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
   counter_.resize(1);
+  // earlier tuner decisions: lines "kernel class variant" of GFAZ_TUNE_FILE
+  if (const char *f = std::getenv("GFAZ_TUNE_FILE")) {
+    if (FILE *fp = std::fopen(f, "r")) {
+      int k, c, v;
+      while (std::fscanf(fp, "%d %d %d", &k, &c, &v) == 3) tuned[{k, c}] = v;
+      std::fclose(fp);
+    }
+  }
+}
+
+void Context::record_tuned(int kernel, int cls, int variant) {
+  tuned[{kernel, cls}] = variant;
+  if (const char *f = std::getenv("GFAZ_TUNE_FILE")) {
+    if (FILE *fp = std::fopen(f, "a")) {
+      std::fprintf(fp, "%d %d %d\n", kernel, cls, variant);
+      std::fclose(fp);
+    }
+  }
 }
 
 Context::~Context() {
@@ -319,7 +337,7 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
       const float t_tiled = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, false, ds, st); });
       const float t_flat = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, true, ds, st); });
       flat = t_flat < t_tiled;
-      ctx.tuned[{Context::kTuneClassify, cls}] = flat ? 1 : 0;
+      ctx.record_tuned(Context::kTuneClassify, cls, flat ? 1 : 0);
       if (debug_enabled())
         fprintf(stderr, "[gfaz gb300] classify tuner: class %d n=%llu persistent %.3f ms, flat %.3f ms\n", cls,
                 (unsigned long long)n, t_tiled, t_flat);
@@ -440,7 +458,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
           cap *= 4;
           continue;
         }
-        ctx.tuned[{Context::kTuneCount, cls}] = (int)kind;
+        ctx.record_tuned(Context::kTuneCount, cls, (int)kind);
         if (debug_enabled())
           fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f, flat %.3f, flat4 %.3f ms\n", cls,
                   (unsigned long long)n, t[0], t[1], t[2]);

@@ -133,9 +133,13 @@ class Context {
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   // Tuner: (kernel, stream class) -> the variant that was faster the first
-  // time the class came up (see encode_traversals).
+  // time the class came up (see encode_traversals).  With GFAZ_TUNE_FILE
+  // set, decisions are loaded from that file when the context is made and
+  // appended to it when taken, so later processes (a profiler's replay of
+  // the same command) run the same variants.
   enum TunedKernel { kTuneCount = 0, kTuneClassify = 1 };
   std::map<std::pair<int, int>, int> tuned;
+  void record_tuned(int kernel, int cls, int variant);
   // Launches on this context's stream and returns their device time (ms).
   float time_launches(const std::function<void()> &launch);
 

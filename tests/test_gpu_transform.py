@@ -200,3 +200,20 @@ def test_text_incompressible_and_long_pieces(delta_round, gpu_ctx):
     # a name longer than a tile's text staging: that tile writes straight to HBM
     names[2] = "n" * 40_000
     assert g.text(0, n, names=names, overlaps=ovs) == oracle.format_p(steps, off, names, ovs)
+
+
+def test_tuner_decisions_file(tmp_path, monkeypatch, gpu_ctx):
+    """GFAZ_TUNE_FILE: a context appends the decisions it takes and a later
+    context starts from them (same grammar either way)."""
+    f = tmp_path / "tune.txt"
+    monkeypatch.setenv("GFAZ_TUNE_FILE", str(f))
+    steps, off, _ = synthetic.cfg2_stream(seed=9, n_segments=40_000, n_paths=4)
+    a = gz.encode(steps, off, ctx=gz.Context(0)).arrays()
+    rows = [tuple(int(x) for x in line.split()) for line in f.read_text().splitlines()]
+    assert rows and all(len(r) == 3 and r[0] in (0, 1) for r in rows)
+    # force the other classification variant for every recorded class
+    f.write_text("".join("%d %d %d\n" % (k, c, (1 - v) if k == 1 else v) for k, c, v in rows))
+    b = gz.encode(steps, off, ctx=gz.Context(0)).arrays()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    assert f.read_text().count("\n") == len(rows)  # nothing new to decide
