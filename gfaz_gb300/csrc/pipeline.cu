@@ -6,6 +6,8 @@
 //   signed packed key -> final ids next_id + rank -> remap temporaries.
 #include "pipeline.h"
 
+#include <chrono>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -149,7 +151,29 @@ Context::~Context() {
   cudaStreamSynchronize(stream_);
   cudaFree(d_status_);
   cudaFreeHost(h_status_);
+  for (auto &h : host_) {
+    if (h.pinned) cudaFreeHost(h.p);
+    else std::free(h.p);
+  }
   if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+int32_t *Context::host_buffer(int i, uint64_t n) {
+  HostStage &h = host_[i];
+  n = std::max<uint64_t>(n, 1);
+  if (h.n >= n) return h.p;
+  if (h.pinned) cudaFreeHost(h.p);
+  else std::free(h.p);
+  h = HostStage{};
+  if (cudaHostAlloc(reinterpret_cast<void **>(&h.p), n * sizeof(int32_t), cudaHostAllocDefault) == cudaSuccess) {
+    h.pinned = true;
+  } else {
+    cudaGetLastError();
+    h.p = static_cast<int32_t *>(std::malloc(n * sizeof(int32_t)));
+    if (!h.p) throw std::bad_alloc();
+  }
+  h.n = n;
+  return h.p;
 }
 
 void Context::reset_status() {
@@ -350,50 +374,16 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
                                 ds, st));
 }
 
-void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
-                       const EncodeParams &p, Grammar &g) {
+// Grammar rounds round0 .. rounds - 1 over the device-resident stream A (n
+// steps, offsets offA; B / offB the other buffers), continuing from next_id
+// and the previous round's distinct pair count.  Used rules are appended to
+// rules (g.nrules so far) and g's counters advance; on return A / offA hold
+// the result, n its length.
+static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, DevVec<uint64_t> &offA,
+                       DevVec<uint64_t> &offB, uint64_t ntrav, uint64_t &n, uint32_t &next_id, uint64_t &prev_distinct,
+                       int round0, int rounds, DevVec<long long> &rules, Grammar &g) {
   cudaStream_t st = ctx.stream();
-  if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
-  const uint64_t ntrav = h_off.size() - 1;
-  const uint64_t N = h_off.back();
-  for (uint64_t t = 0; t < ntrav; ++t)
-    if (h_off[t + 1] < h_off[t]) throw std::invalid_argument("traversal offsets must be non-decreasing");
-  if (h_off[0] != 0) throw std::invalid_argument("offsets must start at 0");
-  const int dr = std::max(0, p.delta_round);
-  g.ntrav = ntrav;
-  g.delta_round = dr;
-  g.rounds_done = 0;
-  g.nrules = 0;
-
-  DevVec<uint64_t> offA(st), offB(st);
-  offA.resize(ntrav + 1);
-  offB.resize(ntrav + 1);
-  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
-             "offsets upload");
-  DevVec<int32_t> A(st), B(st);
-  A.resize(std::max<uint64_t>(N, 1));
-  B.resize(std::max<uint64_t>(N, 1));
-
-  ctx.reset_status();
   DevStatus *ds = ctx.dstatus();
-  if (dr == 0) {
-    if (N) cuda_check(cudaMemcpyAsync(A.ptr, d_steps, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
-    GFZ_TIMED_B(ctx, "max_abs", 4.0 * N, launch_max_abs(A.ptr, N, &ds->aux, st));
-  } else {
-    GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(d_steps, A.ptr, N, offA.ptr, ntrav, &ds->aux, st));
-    for (int r = 1; r < dr; ++r) {
-      GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(A.ptr, B.ptr, N, offA.ptr, ntrav, &ds->aux, st));
-      A.swap(B);
-    }
-  }
-  const DevStatus &s0 = ctx.read_status();
-  const uint32_t max_abs = s0.aux;
-  if (max_abs == UINT32_MAX)
-    throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
-  uint32_t next_id = max_abs + 1;
-  g.layer_start = next_id;
-
-  DevVec<long long> rules(st);
   Table tab(st);
   SortWork su(st);
   DevVec<unsigned long long> &ukeys = su.keys;
@@ -401,9 +391,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   DevVec<uint32_t> heads(st), used_bits(st);
   ReplaceWork rw(st);
 
-  uint64_t n = N;
-  uint64_t prev_distinct = 0;
-  for (int round = 0; round < p.rounds; ++round) {
+  for (int round = round0; round < rounds; ++round) {
     if (n < 2) break;
     // first round: at most 4M distinct pairs expected (delta-coded
     // traversals repeat few pairs); the table grows when it runs fuller
@@ -522,6 +510,55 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     offA.swap(offB);
     g.rounds_done++;
   }
+}
+
+void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
+                       const EncodeParams &p, Grammar &g) {
+  cudaStream_t st = ctx.stream();
+  if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
+  const uint64_t ntrav = h_off.size() - 1;
+  const uint64_t N = h_off.back();
+  for (uint64_t t = 0; t < ntrav; ++t)
+    if (h_off[t + 1] < h_off[t]) throw std::invalid_argument("traversal offsets must be non-decreasing");
+  if (h_off[0] != 0) throw std::invalid_argument("offsets must start at 0");
+  const int dr = std::max(0, p.delta_round);
+  g.ntrav = ntrav;
+  g.delta_round = dr;
+  g.rounds_done = 0;
+  g.nrules = 0;
+
+  DevVec<uint64_t> offA(st), offB(st);
+  offA.resize(ntrav + 1);
+  offB.resize(ntrav + 1);
+  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
+             "offsets upload");
+  DevVec<int32_t> A(st), B(st);
+  A.resize(std::max<uint64_t>(N, 1));
+  B.resize(std::max<uint64_t>(N, 1));
+
+  ctx.reset_status();
+  DevStatus *ds = ctx.dstatus();
+  if (dr == 0) {
+    if (N) cuda_check(cudaMemcpyAsync(A.ptr, d_steps, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+    GFZ_TIMED_B(ctx, "max_abs", 4.0 * N, launch_max_abs(A.ptr, N, &ds->aux, st));
+  } else {
+    GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(d_steps, A.ptr, N, offA.ptr, ntrav, &ds->aux, st));
+    for (int r = 1; r < dr; ++r) {
+      GFZ_TIMED_B(ctx, "delta_encode", 8.0 * N, launch_delta_encode(A.ptr, B.ptr, N, offA.ptr, ntrav, &ds->aux, st));
+      A.swap(B);
+    }
+  }
+  const DevStatus &s0 = ctx.read_status();
+  const uint32_t max_abs = s0.aux;
+  if (max_abs == UINT32_MAX)
+    throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
+  uint32_t next_id = max_abs + 1;
+  g.layer_start = next_id;
+
+  DevVec<long long> rules(st);
+  uint64_t n = N;
+  uint64_t prev_distinct = 0;
+  run_rounds(ctx, A, B, offA, offB, ntrav, n, next_id, prev_distinct, 0, p.rounds, rules, g);
   g.next_id = next_id;
   A.size = n;
   g.enc = std::move(A);
@@ -539,27 +576,15 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
 // ---------------------------------------------------------------------------
 namespace {
 
-// Host buffer of int32 steps, page-locked when the allocation succeeds.
-struct HostBuf {
-  int32_t *p = nullptr;
-  bool pinned = false;
-  std::vector<int32_t> v;
-  explicit HostBuf(uint64_t n) {
-    if (cudaHostAlloc(reinterpret_cast<void **>(&p), std::max<uint64_t>(n, 1) * sizeof(int32_t),
-                      cudaHostAllocDefault) == cudaSuccess) {
-      pinned = true;
-    } else {
-      cudaGetLastError();
-      v.resize(std::max<uint64_t>(n, 1));
-      p = v.data();
-    }
-  }
-  ~HostBuf() {
-    if (pinned) cudaFreeHost(p);
-  }
-  HostBuf(const HostBuf &) = delete;
-  HostBuf &operator=(const HostBuf &) = delete;
-};
+// Device bytes the resident rounds need for an n-step stream: two stream
+// buffers, head bitmap, per-tile words and tile arrays, the pair table with
+// its used bitmap and sort lists, the rulebook and some slack.
+uint64_t resident_bytes(uint64_t n, uint64_t prev_distinct, uint64_t nrules) {
+  uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
+  est = std::min(est, n);
+  const uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
+  return 8 * n + n / 8 + n / 2 + n / 32 + 16 * cap + cap / 8 + 6 * cap + 8 * (nrules + n / 2) + (64ull << 20);
+}
 
 // Copies steps [a, b) of the stream made of segs (back to back) to dst.
 void upload_range(const std::vector<HostSeg> &segs, uint64_t a, uint64_t b, int32_t *dst, cudaStream_t st) {
@@ -576,7 +601,7 @@ void upload_range(const std::vector<HostSeg> &segs, uint64_t a, uint64_t b, int3
 }  // namespace
 
 void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
-                         const EncodeParams &p, uint64_t chunk, Grammar &g) {
+                         const EncodeParams &p, uint64_t chunk, uint64_t budget, Grammar &g) {
   cudaStream_t st = ctx.stream();
   if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
   const uint64_t ntrav = h_off.size() - 1;
@@ -611,12 +636,14 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     cuda_check(cudaMemsetAsync(hloc.ptr, 0, head_words(C + 1) * sizeof(uint32_t), st), "head bitmap clear");
     launch_head_bits_range(off, ntrav, lo, span, hloc.ptr, st);
   };
-  HostBuf X(N), Y(N);
+  // host stream buffers (the context keeps them for later calls)
+  int32_t *const X = ctx.host_buffer(0, N);
+  int32_t *const Y = ctx.host_buffer(1, N);
   ctx.reset_status();
   DevStatus *ds = ctx.dstatus();
   // delta rounds (or the max |x| of the raw steps), chunk by chunk
   std::vector<HostSeg> cur = input;
-  HostBuf *nxt = &X;
+  int32_t *nxt = X;
   if (dr == 0) {
     for (uint64_t c0 = 0; c0 < N; c0 += C) {
       const uint64_t c1 = std::min(c0 + C, N);
@@ -636,12 +663,12 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       local_heads(offA.ptr, c0, c1 - c0);
       GFZ_TIMED_B(ctx, "delta_encode", 8.0 * (c1 - c0),
                   launch_delta_chunk(cin.ptr, cout.ptr, c1 - c0, hloc.ptr, &ds->aux, st));
-      cuda_check(cudaMemcpyAsync(nxt->p + c0, cout.ptr, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
+      cuda_check(cudaMemcpyAsync(nxt + c0, cout.ptr, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
                  "chunk download");
     }
     cuda_check(cudaStreamSynchronize(st), "stream sync");
-    cur = {HostSeg{nxt->p, N}};
-    nxt = nxt == &X ? &Y : &X;
+    cur = {HostSeg{nxt, N}};
+    nxt = nxt == X ? Y : X;
   }
   const DevStatus &s0 = ctx.read_status();
   const uint32_t max_abs = s0.aux;
@@ -649,6 +676,16 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
   uint32_t next_id = max_abs + 1;
   g.layer_start = next_id;
+  using clk = std::chrono::steady_clock;
+  auto t_phase = clk::now();
+  auto phase = [&](const char *what) {
+    if (!debug_enabled()) return;
+    const auto now = clk::now();
+    fprintf(stderr, "[gfaz gb300] chunked %s: %.1f ms\n", what,
+            std::chrono::duration<double, std::milli>(now - t_phase).count());
+    t_phase = now;
+  };
+  phase("delta");
 
   DevVec<long long> rules(st);
   Table tab(st);
@@ -658,8 +695,30 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   std::vector<unsigned long long> h_state;
   uint64_t n = N;
   uint64_t prev_distinct = 0;
+  DevVec<int32_t> A(st), B(st);
+  bool resident = false;  // the remaining rounds ran on a device-resident stream
   for (int round = 0; round < p.rounds; ++round) {
     if (n < 2) break;
+    if (budget && resident_bytes(n, prev_distinct, g.nrules) <= budget) {
+      // the rest fits the budget: one upload, then the resident rounds
+      cin.release();
+      cout.release();
+      tab.slots.release();
+      used_bits.release();
+      rw.tword.release();
+      rw.tile_agg.release();
+      rw.tile_state.release();
+      rw.tile_trav.release();
+      A.resize(std::max<uint64_t>(n, 1));
+      B.resize(std::max<uint64_t>(n, 1));
+      upload_range(cur, 0, n, A.ptr, st);
+      phase("upload for the resident rounds");
+      run_rounds(ctx, A, B, offA, offB, ntrav, n, next_id, prev_distinct, round, p.rounds, rules, g);
+      cuda_check(cudaStreamSynchronize(st), "stream sync");
+      phase("resident rounds");
+      resident = true;
+      break;
+    }
     uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
     est = std::min(est, n);
     uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
@@ -743,13 +802,13 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       if (c1 < n) {
         const uint64_t o1 = out_start(c1);
         if (o1 > o0)
-          cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+          cuda_check(cudaMemcpyAsync(nxt + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
                      "chunk download");
       } else {
         const DevStatus &se = ctx.read_status();
         const uint64_t n_end = se.u64[2];
         if (n_end > o0)
-          cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (n_end - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+          cuda_check(cudaMemcpyAsync(nxt + o0, cout.ptr, (n_end - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
                      "chunk download");
       }
     }
@@ -771,10 +830,10 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     // final ids into the round's output, chunk by chunk
     for (uint64_t o0 = 0; o0 < n_out; o0 += C) {
       const uint64_t o1 = std::min(o0 + C, n_out);
-      cuda_check(cudaMemcpyAsync(cout.ptr, nxt->p + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+      cuda_check(cudaMemcpyAsync(cout.ptr, nxt + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
                  "chunk upload");
       GFZ_TIMED_B(ctx, "remap", 8.0 * (o1 - o0), launch_remap(cout.ptr, o1 - o0, temp_base, tab.slots.ptr, st));
-      cuda_check(cudaMemcpyAsync(nxt->p + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+      cuda_check(cudaMemcpyAsync(nxt + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
                  "chunk download");
     }
     ctx.read_status();
@@ -786,15 +845,21 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     g.nrules += U;
     next_id += (uint32_t)U;
     n = n_out;
-    cur = {HostSeg{nxt->p, n}};
-    nxt = nxt == &X ? &Y : &X;
+    phase("round");
+    cur = {HostSeg{nxt, n}};
+    nxt = nxt == X ? Y : X;
     offA.swap(offB);
     g.rounds_done++;
   }
   g.next_id = next_id;
-  g.enc.resize(std::max<uint64_t>(n, 1));
-  g.enc.size = n;
-  upload_range(cur, 0, n, g.enc.ptr, st);
+  if (resident) {
+    A.size = n;
+    g.enc = std::move(A);
+  } else {
+    g.enc.resize(std::max<uint64_t>(n, 1));
+    g.enc.size = n;
+    upload_range(cur, 0, n, g.enc.ptr, st);
+  }
   g.off = std::move(offA);
   g.h_off.resize(ntrav + 1);
   cuda_check(cudaMemcpyAsync(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
@@ -821,7 +886,8 @@ void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vec
     }
   }
   if (chunk) {
-    encode_host_chunked(ctx, input, h_off, p, chunk, g);
+    // with a budget the rounds turn resident once the stream fits it
+    encode_host_chunked(ctx, input, h_off, p, chunk, ctx.encode_chunk ? 0 : ctx.hbm_budget, g);
     return;
   }
   cudaStream_t st = ctx.stream();

@@ -142,6 +142,10 @@ class Context {
   void record_tuned(int kernel, int cls, int variant);
   // Launches on this context's stream and returns their device time (ms).
   float time_launches(const std::function<void()> &launch);
+  // Page-locked host buffer i (0 or 1) of at least n int32, kept for later
+  // calls (chunked compression's host stream buffers); pageable memory when
+  // page-locking fails.
+  int32_t *host_buffer(int i, uint64_t n);
 
  private:
   int device_ = 0, sms_ = 152;
@@ -162,6 +166,11 @@ class Context {
   double open_bytes_ = 0;
   cudaEvent_t open_a_ = nullptr;
   std::map<std::string, KernelStat> stats_;
+  struct HostStage {
+    int32_t *p = nullptr;
+    uint64_t n = 0;
+    bool pinned = false;
+  } host_[2];
   uint64_t launches_ = 0;
   cudaEvent_t take_event();
 };
@@ -207,9 +216,11 @@ struct HostSeg {
 // The same compression for a stream in host memory (the segments back to
 // back), moved through HBM in chunks of `chunk` steps (rounded down to whole
 // apply tiles): only the pair table, per-tile words and chunk buffers live
-// on the device, and the result is identical to encode_traversals'.
+// on the device, and the result is identical to encode_traversals'.  With
+// budget > 0, the rounds continue resident once a round's stream fits the
+// budget (rounds shrink the stream).
 void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
-                         const EncodeParams &p, uint64_t chunk, Grammar &g);
+                         const EncodeParams &p, uint64_t chunk, uint64_t budget, Grammar &g);
 
 // Compression of host-resident input: resident in HBM when its working set
 // (about 12.5 bytes per step) fits ctx.hbm_budget, else in chunks
