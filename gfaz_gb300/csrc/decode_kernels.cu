@@ -30,7 +30,7 @@ inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
 // Rule lengths
 // ---------------------------------------------------------------------------
 __global__ void k_rule_len_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
-                                uint64_t nrules, uint32_t min_id, uint32_t *rlen, DevStatus *status) {
+                                uint64_t nrules, uint32_t min_id, uint32_t *rlen, DevStatus *status, int slot) {
   uint32_t open = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nrules;
        i += (uint64_t)gridDim.x * blockDim.x) {
@@ -51,7 +51,7 @@ __global__ void k_rule_len_pass(const int32_t *__restrict__ first, const int32_t
     }
   }
   open = __reduce_add_sync(0xffffffffu, open);
-  if ((threadIdx.x & 31) == 0 && open) atomicAdd(&status->u64[6], (unsigned long long)open);
+  if ((threadIdx.x & 31) == 0 && open) atomicAdd(&status->pass_open[slot], (unsigned long long)open);
 }
 
 // ---------------------------------------------------------------------------
@@ -342,9 +342,9 @@ constexpr int kDeltaItems = 16;
 constexpr int kTextItems = 8;
 
 void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
-                          uint32_t *rlen, DevStatus *status, cudaStream_t st) {
+                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st) {
   if (!nrules) return;
-  k_rule_len_pass<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(first, second, nrules, min_id, rlen, status);
+  k_rule_len_pass<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(first, second, nrules, min_id, rlen, status, slot);
 }
 
 uint64_t scan_num_tiles(uint64_t n) {

@@ -51,7 +51,7 @@ __device__ __forceinline__ uint32_t child_prefix(int32_t c, uint32_t o, const Ru
 // One build pass: every rule whose rule children were built in an earlier
 // pass (built[c] in [1, pass)) writes pre_R = pre_first ++ (total_first +
 // pre_second) and records built[R] = pass.  Rules still waiting are counted
-// in status->u64[6].
+// in status->pass_open[slot].
 // Prefix value at offset o of rule i = first ++ second (lf steps of first).
 __device__ __forceinline__ uint32_t rule_prefix_at(int32_t f, int32_t g, uint32_t lf, uint32_t tf, uint32_t o,
                                                    const RulePrefixView &rv) {
@@ -77,7 +77,7 @@ constexpr uint32_t kWarpRule = 16;  // rules longer than this are written by a w
 
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
                                    RulePrefixView rv, int32_t *rpre, int4 *rstat, int delta, uint32_t *built,
-                                   uint32_t pass, DevStatus *status) {
+                                   uint32_t pass, DevStatus *status, int slot) {
   __shared__ uint32_t s_open;
   if (threadIdx.x == 0) s_open = 0;
   __syncthreads();
@@ -160,7 +160,7 @@ __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int3
   open = __reduce_add_sync(0xffffffffu, open);
   if (lane == 0 && open) atomicAdd(&s_open, open);
   __syncthreads();
-  if (threadIdx.x == 0 && s_open) atomicAdd(&status->u64[6], (unsigned long long)s_open);
+  if (threadIdx.x == 0 && s_open) atomicAdd(&status->pass_open[slot], (unsigned long long)s_open);
 }
 
 // Exclusive scan of n values into out[0 .. n] (out[n] = total), decoupled
@@ -665,11 +665,11 @@ uint64_t excl_scan_tiles(uint64_t n) {
 }
 
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
-                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status,
+                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status, int slot,
                              cudaStream_t st) {
   if (!rv.nrules) return;
   k_rule_prefix_pass<<<grid_for(rv.nrules, kBlock, 152u * 32u), kBlock, 0, st>>>(first, second, rv, rpre, rstat,
-                                                                                 delta, built, pass, status);
+                                                                                 delta, built, pass, status, slot);
 }
 
 void launch_excl_scan_u32(const uint32_t *in, uint64_t n, uint64_t *out, unsigned long long *desc,

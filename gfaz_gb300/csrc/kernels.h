@@ -12,6 +12,9 @@ struct DevStatus {
   uint32_t err;            // OR of kErr* bits
   uint32_t aux;            // u32 result slot (max |x| of delta coding)
   unsigned long long u64[8];  // kernel result slots (see each launcher)
+  unsigned long long pass_open[4];  // rules still open after each pass of a batch of level passes
+  uint32_t sticky_err;     // error bits carried past reset_status (a grammar round's sort)
+  uint32_t pad;
 };
 
 // ---- encode side ----------------------------------------------------------
@@ -158,9 +161,10 @@ void launch_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, uint64_
 
 // ---- decode side ------------------------------------------------------------
 // Rule expansion lengths: len[i] for rule min_id + i.  One pass resolves the
-// rules whose children are resolved; status->u64[6] counts rules still open.
+// rules whose children are resolved; status->pass_open[slot] counts rules
+// still open.
 void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
-                          uint32_t *rlen, DevStatus *status, cudaStream_t st);
+                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st);
 // Exclusive scan of the expansion length of every encoded symbol into
 // pos[0..m] (pos[m] = total); desc/tile_counter zeroed.
 void launch_symbol_positions(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules,
@@ -237,9 +241,10 @@ struct TextSource {
   uint32_t *err;  // kErrLength when the text would not fit where its lengths say
 };
 // One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
-// waiting, zero before pass 1).  status->u64[6] += rules still waiting.
+// waiting, zero before pass 1).  status->pass_open[slot] += rules still
+// waiting.
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
-                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status,
+                             int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status, int slot,
                              cudaStream_t st);
 // out[0 .. n] = exclusive scan of in[0 .. n) (out[n] = total); desc: one u64
 // per excl_scan_tiles(n) tile (at least one), zeroed; tile_counter zeroed.

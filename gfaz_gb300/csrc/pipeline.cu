@@ -57,6 +57,8 @@ uint64_t ceil_log2(uint64_t x) {
 }
 
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
+constexpr int kPassBatch = 4;  // level passes launched per status read (DevStatus::pass_open slots)
+static_assert(kPassBatch <= (int)(sizeof(DevStatus::pass_open) / sizeof(unsigned long long)), "pass slots");
 
 
 struct Table {
@@ -177,7 +179,7 @@ int32_t *Context::host_buffer(int i, uint64_t n) {
 }
 
 void Context::reset_status() {
-  cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
+  cuda_check(cudaMemsetAsync(d_status_, 0, offsetof(DevStatus, sticky_err), stream_), "status clear");
 }
 
 const DevStatus &Context::read_status() {
@@ -188,8 +190,12 @@ const DevStatus &Context::read_status() {
 }
 
 void Context::check_status(const char *stage) {
-  const uint32_t e = h_status_->err;
+  const uint32_t e = h_status_->err | h_status_->sticky_err;
   if (!e) return;
+  if (h_status_->sticky_err) {
+    h_status_->sticky_err = 0;
+    cudaMemsetAsync(&d_status_->sticky_err, 0, sizeof(uint32_t), stream_);
+  }
   std::string msg = std::string("device error in ") + stage + ":";
   if (e & kErrTableFull) msg += " pair table full;";
   if (e & kErrLookupMiss) msg += " counted pair missing from table;";
@@ -497,8 +503,10 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
     sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
     GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
-    ctx.read_status();
-    ctx.check_status("rule sort");
+    // the sort's error bits reach the host with the next round's count (or
+    // the read after the last round): no wait here
+    cuda_check(cudaMemcpyAsync(&ds->sticky_err, &ds->err, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
+               "status carry");
     if (debug_enabled())
       fprintf(stderr, "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu\n",
               round + 1, (unsigned long long)n, (unsigned long long)cap, (unsigned long long)distinct,
@@ -510,6 +518,8 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     offA.swap(offB);
     g.rounds_done++;
   }
+  ctx.read_status();
+  ctx.check_status("rule sort");
 }
 
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
@@ -986,14 +996,17 @@ static void ensure_rule_lengths(Context &ctx, Grammar &g) {
                 (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, g.first.ptr, g.second.ptr)));
     }
     cuda_check(cudaMemsetAsync(g.rlen.ptr, 0, R * sizeof(uint32_t), st), "rlen clear");
+    // level passes in batches, one status read per batch (extra passes
+    // after the last level find nothing to do)
     uint64_t prev_open = UINT64_MAX;
-    for (int pass = 0;; ++pass) {
+    for (;;) {
       ctx.reset_status();
-      GFZ_TIMED(ctx, "rule_len", launch_rule_len_pass(g.first.ptr, g.second.ptr, R, g.layer_start, g.rlen.ptr,
-                                                      ctx.dstatus(), st));
+      for (int k = 0; k < kPassBatch; ++k)
+        GFZ_TIMED(ctx, "rule_len", launch_rule_len_pass(g.first.ptr, g.second.ptr, R, g.layer_start, g.rlen.ptr,
+                                                        ctx.dstatus(), k, st));
       const DevStatus &s = ctx.read_status();
       ctx.check_status("rule lengths");
-      const uint64_t open = s.u64[6];
+      const uint64_t open = s.pass_open[kPassBatch - 1];
       if (open == 0) break;
       if (open >= prev_open)
         throw std::runtime_error("rule lengths do not resolve: the rulebook references itself");
@@ -1035,14 +1048,15 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
     cuda_check(cudaMemsetAsync(built.ptr, 0, R * sizeof(uint32_t), st), "prefix clear");
     const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, R};
     uint64_t prev_open = UINT64_MAX;
-    for (uint32_t pass = 1;; ++pass) {
+    for (uint32_t pass = 1;; pass += kPassBatch) {
       ctx.reset_status();
-      GFZ_TIMED_B(ctx, "rule_prefix", 0,
-                  launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, g.rstat.ptr,
-                                          g.delta_round == 1 ? 1 : 0, built.ptr, pass, ctx.dstatus(), st));
+      for (int k = 0; k < kPassBatch; ++k)
+        GFZ_TIMED_B(ctx, "rule_prefix", 0,
+                    launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, g.rstat.ptr,
+                                            g.delta_round == 1 ? 1 : 0, built.ptr, pass + k, ctx.dstatus(), k, st));
       const DevStatus &s = ctx.read_status();
       ctx.check_status("rule prefix");
-      const uint64_t open = s.u64[6];
+      const uint64_t open = s.pass_open[kPassBatch - 1];
       if (open == 0) break;
       if (open >= prev_open) throw std::runtime_error("rule expansions do not resolve: the rulebook references itself");
       prev_open = open;
