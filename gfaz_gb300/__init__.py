@@ -220,6 +220,8 @@ class GfaGraph:
     num_links: int = 0
     num_jumps: int = 0
     num_containments: int = 0
+    segment_names: List[str] = field(default_factory=list)      # filled by parse_gfa
+    segment_sequences: List[str] = field(default_factory=list)  # filled by parse_gfa
 
 
 def _split_lines(text: bytes) -> List[str]:
@@ -433,52 +435,84 @@ def add_haplotypes(data: CompressedData, haplotypes_path, threads: int = DEFAULT
     return out
 
 
+def _graph_from_handle(L, h) -> GfaGraph:
+    """GfaGraph copy of a gfz_graph handle (the caller frees the handle)."""
+    g = GfaGraph()
+
+    def strings(name):
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        check(L.gfz_graph_strings(h, _cstr(name), ctypes.byref(p), ctypes.byref(n)))
+        s = take_bytes(p, n.value).decode()
+        return s.split("\n")[:-1] if s else []
+
+    def trav(kind):
+        sp, op, nt = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
+        check(L.gfz_graph_traversals(h, kind, ctypes.byref(sp), ctypes.byref(op), ctypes.byref(nt)))
+        if nt.value == 0:
+            return []
+        off = np.ctypeslib.as_array(ctypes.cast(op, ctypes.POINTER(ctypes.c_uint64)), (nt.value + 1,)).copy()
+        total = int(off[-1])
+        steps = (np.ctypeslib.as_array(ctypes.cast(sp, ctypes.POINTER(ctypes.c_int32)), (total,)).copy()
+                 if total else np.zeros(0, np.int32))
+        return [steps[int(off[i]):int(off[i + 1])] for i in range(nt.value)]
+
+    hp, sp_, ep, nw = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
+    check(L.gfz_graph_walk_numbers(h, ctypes.byref(hp), ctypes.byref(sp_), ctypes.byref(ep), ctypes.byref(nw)))
+    hdr = ctypes.c_void_p()
+    hn = ctypes.c_size_t()
+    check(L.gfz_graph_strings(h, b"header", ctypes.byref(hdr), ctypes.byref(hn)))
+    g.header_line = take_bytes(hdr, hn.value).decode()
+    g.path_names = strings("path_names")
+    g.path_overlaps = strings("path_overlaps")
+    g.walk_sample_ids = strings("walk_sample_ids")
+    g.walk_seq_ids = strings("walk_seq_ids")
+    g.paths = trav(0)
+    g.walks = trav(1)
+    n = nw.value
+    if n:
+        g.walk_hap_indices = np.ctypeslib.as_array(ctypes.cast(hp, ctypes.POINTER(ctypes.c_uint32)), (n,)).tolist()
+        g.walk_seq_starts = np.ctypeslib.as_array(ctypes.cast(sp_, ctypes.POINTER(ctypes.c_int64)), (n,)).tolist()
+        g.walk_seq_ends = np.ctypeslib.as_array(ctypes.cast(ep, ctypes.POINTER(ctypes.c_int64)), (n,)).tolist()
+    c = [ctypes.c_uint64() for _ in range(4)]
+    check(L.gfz_graph_counts(h, *[ctypes.byref(x) for x in c]))
+    g.num_segments, g.num_links, g.num_jumps, g.num_containments = [x.value for x in c]
+    return g
+
+
+# ---------------------------------------------------------------------------
+# reference API (bindings.cpp:323-743)
+def parse_gfa(file_path, threads: int = DEFAULT_NUM_THREADS, ctx: Optional[Context] = None,
+              device: bool = True) -> GfaGraph:
+    """parse / parse_gfa (bindings.cpp:659-660): the GFA file as a graph.
+    device=True parses with the GPU front end (line index and P/W steps on
+    the device), device=False with the host parser; the graphs are equal.
+    The graph also carries segment_names / segment_sequences."""
+    L = lib()
+    h = ctypes.c_void_p()
+    check(L.gfz_parse_gfa(_ctx(ctx) if device else None, _cstr(file_path), int(threads), int(bool(device)),
+                          ctypes.byref(h)))
+    try:
+        g = _graph_from_handle(L, h)
+        for name in ("segment_names", "segment_sequences"):
+            p, n = ctypes.c_void_p(), ctypes.c_size_t()
+            check(L.gfz_graph_strings(h, _cstr(name), ctypes.byref(p), ctypes.byref(n)))
+            s = take_bytes(p, n.value).decode()
+            setattr(g, name, s.split("\n")[:-1] if s else [])
+        return g
+    finally:
+        L.gfz_graph_free(h)
+
+
+parse = parse_gfa
+
+
 def decompress_data(data: CompressedData, threads: int = DEFAULT_NUM_THREADS,
                     ctx: Optional[Context] = None) -> GfaGraph:
     L = lib()
     h = ctypes.c_void_p()
     check(L.gfz_decompress_graph(_ctx(ctx), data.handle, int(threads), ctypes.byref(h)))
     try:
-        g = GfaGraph()
-
-        def strings(name):
-            p, n = ctypes.c_void_p(), ctypes.c_size_t()
-            check(L.gfz_graph_strings(h, _cstr(name), ctypes.byref(p), ctypes.byref(n)))
-            s = take_bytes(p, n.value).decode()
-            return s.split("\n")[:-1] if s else []
-
-        def trav(kind):
-            sp, op, nt = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
-            check(L.gfz_graph_traversals(h, kind, ctypes.byref(sp), ctypes.byref(op), ctypes.byref(nt)))
-            if nt.value == 0:
-                return []
-            off = np.ctypeslib.as_array(ctypes.cast(op, ctypes.POINTER(ctypes.c_uint64)), (nt.value + 1,)).copy()
-            total = int(off[-1])
-            steps = (np.ctypeslib.as_array(ctypes.cast(sp, ctypes.POINTER(ctypes.c_int32)), (total,)).copy()
-                     if total else np.zeros(0, np.int32))
-            return [steps[int(off[i]):int(off[i + 1])] for i in range(nt.value)]
-
-        hp, sp_, ep, nw = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
-        check(L.gfz_graph_walk_numbers(h, ctypes.byref(hp), ctypes.byref(sp_), ctypes.byref(ep), ctypes.byref(nw)))
-        hdr = ctypes.c_void_p()
-        hn = ctypes.c_size_t()
-        check(L.gfz_graph_strings(h, b"header", ctypes.byref(hdr), ctypes.byref(hn)))
-        g.header_line = take_bytes(hdr, hn.value).decode()
-        g.path_names = strings("path_names")
-        g.path_overlaps = strings("path_overlaps")
-        g.walk_sample_ids = strings("walk_sample_ids")
-        g.walk_seq_ids = strings("walk_seq_ids")
-        g.paths = trav(0)
-        g.walks = trav(1)
-        n = nw.value
-        if n:
-            g.walk_hap_indices = np.ctypeslib.as_array(ctypes.cast(hp, ctypes.POINTER(ctypes.c_uint32)), (n,)).tolist()
-            g.walk_seq_starts = np.ctypeslib.as_array(ctypes.cast(sp_, ctypes.POINTER(ctypes.c_int64)), (n,)).tolist()
-            g.walk_seq_ends = np.ctypeslib.as_array(ctypes.cast(ep, ctypes.POINTER(ctypes.c_int64)), (n,)).tolist()
-        c = [ctypes.c_uint64() for _ in range(4)]
-        check(L.gfz_graph_counts(h, *[ctypes.byref(x) for x in c]))
-        g.num_segments, g.num_links, g.num_jumps, g.num_containments = [x.value for x in c]
-        return g
+        return _graph_from_handle(L, h)
     finally:
         L.gfz_graph_free(h)
 

@@ -76,6 +76,7 @@ SIGNATURES = {
     "gfz_extract_walk_lines_by_name": (I, [P, P, ctypes.POINTER(CP), SZ, I, PP, PSZ]),
     "gfz_add_haplotypes": (I, [P, P, CP, I]),
     "gfz_decompress_graph": (I, [P, P, I, PP]),
+    "gfz_parse_gfa": (I, [P, CP, I, I, PP]),
     "gfz_graph_free": (None, [P]),
     "gfz_compressed_info": (I, [P, ctypes.POINTER(ContainerInfo)]),
     "gfz_compressed_layers": (I, [P, ctypes.POINTER(I64), SZ]),

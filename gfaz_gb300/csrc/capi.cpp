@@ -229,6 +229,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "encode_chunk") {
       require(value >= 0, "encode_chunk must be >= 0");
       c.encode_chunk = (uint64_t)value;
+    } else if (std::string(name) == "front_end") {
+      require(value == 0 || value == 1, "front_end must be 0 (host parser) or 1 (device)");
+      c.front_end = (int)value;
     } else if (std::string(name) == "append_chunk") {
       require(value >= 0, "append_chunk must be >= 0");
       c.append_chunk = (uint64_t)value;
@@ -368,6 +371,27 @@ gfz_status gfz_add_haplotypes(gfz_context *ctx, gfz_compressed *c, const char *p
   });
 }
 
+gfz_status gfz_parse_gfa(gfz_context *ctx, const char *path, int threads, int device, gfz_graph **out) {
+  return guard([&] {
+    require(path && out, "path/out are NULL");
+    auto *g = new gfz_graph();
+    try {
+      if (device) {
+        gfz::Context &c = ctx_of(ctx);
+        gfz::DeviceParse r = gfz::parse_gfa_device(c, path, threads);
+        gfz::download_steps(c, r, r.graph);
+        g->g = std::move(r.graph);
+      } else {
+        g->g = gfz::parse_gfa(path, threads);
+      }
+    } catch (...) {
+      delete g;
+      throw;
+    }
+    *out = g;
+  });
+}
+
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out) {
   return guard([&] {
     require(c && out, "NULL argument");
@@ -459,10 +483,14 @@ gfz_status gfz_graph_strings(const gfz_graph *g, const char *field, char **out, 
     else if (f == "path_overlaps") v = &g->g.path_overlaps;
     else if (f == "walk_sample_ids") v = &g->g.walk_sample_ids;
     else if (f == "walk_seq_ids") v = &g->g.walk_seq_ids;
+    else if (f == "segment_names") v = &g->g.node_names;
+    else if (f == "segment_sequences") v = &g->g.node_sequences;
     else if (f == "header") s = g->g.header_line;
     else throw std::invalid_argument("unknown string field: " + f);
+    // segment columns: index 0 is the 1-based ids' placeholder
+    const size_t first = f.rfind("segment_", 0) == 0 ? 1 : 0;
     if (v)
-      for (size_t i = 0; i < v->size(); ++i) s += (*v)[i] + "\n";
+      for (size_t i = first; i < v->size(); ++i) s += (*v)[i] + "\n";
     *out = dup_bytes(s.data(), s.size());
     *len = s.size();
   });

@@ -21,6 +21,7 @@
 #include <unistd.h>
 
 #include <cerrno>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -30,7 +31,9 @@
 #include <string_view>
 #include <unordered_map>
 
+#include "codec.h"
 #include "model.h"
+#include "workflows.h"
 
 namespace gfz {
 
@@ -233,6 +236,14 @@ struct Mapped {
   const char *data = nullptr;
   size_t size = 0;
   int fd = -1;
+  Mapped() = default;
+  Mapped(const Mapped &) = delete;
+  Mapped &operator=(const Mapped &) = delete;
+  Mapped(Mapped &&o) noexcept : data(o.data), size(o.size), fd(o.fd) {
+    o.data = nullptr;
+    o.size = 0;
+    o.fd = -1;
+  }
   ~Mapped() {
     if (data && size) munmap(const_cast<char *>(data), size);
     if (fd >= 0) close(fd);
@@ -243,12 +254,7 @@ struct Line {
   size_t off, len;
 };
 
-}  // namespace
-
-Graph parse_gfa(const std::string &path, int threads) {
-  Graph g;
-  g.node_names.emplace_back();
-  g.node_sequences.emplace_back();
+Mapped map_file(const std::string &path) {
   Mapped m;
   m.fd = open(path.c_str(), O_RDONLY);
   if (m.fd < 0)
@@ -264,71 +270,134 @@ Graph parse_gfa(const std::string &path, int threads) {
     m.data = static_cast<const char *>(p);
     madvise(p, m.size, MADV_SEQUENTIAL);
   }
-  const char *d = m.data;
+  return m;
+}
+
+// Lines by record type, in file order.
+struct Lines {
   std::vector<Line> S, L, P, W, J, C;
+  void add(const char *d, size_t start, size_t len, Graph &g) {
+    switch (d[start]) {
+      case 'S': S.push_back({start, len}); break;
+      case 'H': g.header_line.assign(d + start, len); break;
+      case 'L': L.push_back({start, len}); break;
+      case 'P': P.push_back({start, len}); break;
+      case 'W': W.push_back({start, len}); break;
+      case 'J': J.push_back({start, len}); break;
+      case 'C': C.push_back({start, len}); break;
+      default: break;
+    }
+  }
+};
+
+void scan_lines(const char *d, size_t n, Lines &ls, Graph &g) {
   size_t start = 0;
-  for (size_t i = 0; i <= m.size; ++i) {
-    if (i == m.size || d[i] == '\n') {
-      const size_t len = i - start;
-      if (len > 0) {
-        switch (d[start]) {
-          case 'S': S.push_back({start, len}); break;
-          case 'H': g.header_line.assign(d + start, len); break;
-          case 'L': L.push_back({start, len}); break;
-          case 'P': P.push_back({start, len}); break;
-          case 'W': W.push_back({start, len}); break;
-          case 'J': J.push_back({start, len}); break;
-          case 'C': C.push_back({start, len}); break;
-          default: break;
-        }
-      }
-      start = i + 1;
-    }
+  while (start < n) {
+    const void *nl = std::memchr(d + start, '\n', n - start);
+    const size_t end = nl ? (size_t)(static_cast<const char *>(nl) - d) : n;
+    if (end > start) ls.add(d, start, end - start, g);
+    start = end + 1;
   }
+}
 
-  // S lines: sequential, assigning ids in first-seen order
+// Segment names: numeric (every name the decimal form of its id) or the
+// name table built from the S lines.
+struct Names {
   std::unordered_map<std::string_view, uint32_t> lookup;
-  lookup.reserve(S.size());
+  std::vector<std::string_view> by_id;  // 1-based; filled when not numeric
   bool numeric = true;
-  g.node_names.reserve(S.size() + 1);
-  g.node_sequences.reserve(S.size() + 1);
-  OptSet seg_opt{&g.segment_optional, {}, ""};
-  for (const Line &ln : S) {
-    const std::string_view line(d + ln.off, ln.len);
-    size_t pos = 1;
-    const std::string_view name = next_field(line, pos);
-    const std::string_view seq = next_field(line, pos);
-    size_t index;
-    auto it = lookup.find(name);
-    if (it == lookup.end()) {
-      if (numeric && !all_digits(name)) numeric = false;
-      const uint32_t id = (uint32_t)g.node_names.size();
-      if (numeric && parse_u32(name) != id) numeric = false;
-      g.node_names.emplace_back(name);
-      g.node_sequences.emplace_back(seq);
-      // names stay valid: they point into the mapped file
-      lookup.emplace(name, id);
-      index = id - 1;
-    } else {
-      index = it->second - 1;
-    }
-    while (pos < line.size()) {
-      const std::string_view f = next_field(line, pos);
-      if (f.empty()) break;
-      seg_opt.add(f, index);
-    }
-  }
-  const size_t nseg = g.node_names.size() - 1;
-  for (auto &c : g.segment_optional) pad_column(c, nseg);
-
-  auto resolve = [&](std::string_view name) -> uint32_t {
+  uint32_t resolve(std::string_view name) const {
     if (name.empty()) return 0;
     if (numeric) return parse_u32(name);
     auto it = lookup.find(name);
     return it == lookup.end() ? 0 : it->second;
-  };
+  }
+};
 
-  // L lines
+// S lines, assigning ids in first-seen order.  When the i-th S line is
+// named i + 1 for every i (the common numeric layout: no duplicate can
+// occur and every id equals its name), the lines are read in parallel;
+// otherwise in order with the name table.
+void parse_segments(const char *d, const std::vector<Line> &S, Graph &g, Names &nm, int threads) {
+  OptSet seg_opt{&g.segment_optional, {}, ""};
+  const int64_t ns = (int64_t)S.size();
+  const int nth = resolve_threads(threads);
+  std::vector<uint8_t> plain(ns, 0);
+  std::vector<uint32_t> rest(ns, 0);  // offset of the optional fields in the line (0: none)
+  bool simple = true;
+#pragma omp parallel for schedule(static) num_threads(nth) reduction(&& : simple)
+  for (int64_t i = 0; i < ns; ++i) {
+    const std::string_view line(d + S[i].off, S[i].len);
+    size_t pos = 1;
+    const std::string_view name = next_field(line, pos);
+    next_field(line, pos);
+    while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
+    rest[i] = pos < line.size() ? (uint32_t)std::min<size_t>(pos, UINT32_MAX) : 0;
+    bool ok = all_digits(name) && name.size() <= 10;
+    if (ok) {
+      uint64_t v = 0;
+      for (char c : name) v = v * 10 + (uint64_t)(c - '0');
+      ok = v == (uint64_t)i + 1;
+    }
+    simple = simple && ok && (rest[i] == 0 || S[i].len <= UINT32_MAX);
+  }
+  if (simple) {
+    g.node_names.resize(ns + 1);
+    g.node_sequences.resize(ns + 1);
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int64_t i = 0; i < ns; ++i) {
+      const std::string_view line(d + S[i].off, S[i].len);
+      size_t pos = 1;
+      g.node_names[i + 1].assign(next_field(line, pos));
+      g.node_sequences[i + 1].assign(next_field(line, pos));
+    }
+    for (int64_t i = 0; i < ns; ++i) {
+      if (!rest[i]) continue;
+      const std::string_view line(d + S[i].off, S[i].len);
+      size_t pos = rest[i];
+      while (pos < line.size()) {
+        const std::string_view f = next_field(line, pos);
+        if (f.empty()) break;
+        seg_opt.add(f, (size_t)i);
+      }
+    }
+  } else {
+    nm.lookup.reserve(S.size());
+    g.node_names.reserve(S.size() + 1);
+    g.node_sequences.reserve(S.size() + 1);
+    nm.by_id.assign(1, std::string_view());
+    for (const Line &ln : S) {
+      const std::string_view line(d + ln.off, ln.len);
+      size_t pos = 1;
+      const std::string_view name = next_field(line, pos);
+      const std::string_view seq = next_field(line, pos);
+      size_t index;
+      auto it = nm.lookup.find(name);
+      if (it == nm.lookup.end()) {
+        if (nm.numeric && !all_digits(name)) nm.numeric = false;
+        const uint32_t id = (uint32_t)g.node_names.size();
+        if (nm.numeric && parse_u32(name) != id) nm.numeric = false;
+        g.node_names.emplace_back(name);
+        g.node_sequences.emplace_back(seq);
+        // names stay valid: they point into the mapped file
+        nm.lookup.emplace(name, id);
+        nm.by_id.push_back(name);
+        index = id - 1;
+      } else {
+        index = it->second - 1;
+      }
+      while (pos < line.size()) {
+        const std::string_view f = next_field(line, pos);
+        if (f.empty()) break;
+        seg_opt.add(f, index);
+      }
+    }
+  }
+  const size_t nseg = g.node_names.size() - 1;
+  for (auto &c : g.segment_optional) pad_column(c, nseg);
+}
+
+void parse_links(const char *d, const std::vector<Line> &L, const Names &nm, Graph &g) {
   OptSet link_opt{&g.link_optional, {}, "link "};
   for (const Line &ln : L) {
     const std::string_view line(d + ln.off, ln.len);
@@ -336,7 +405,7 @@ Graph parse_gfa(const std::string &path, int threads) {
     const std::string_view fn = next_field(line, pos), fo = next_field(line, pos);
     const std::string_view tn = next_field(line, pos), to = next_field(line, pos);
     const std::string_view ov = next_field(line, pos);
-    const uint32_t a = resolve(fn), b = resolve(tn);
+    const uint32_t a = nm.resolve(fn), b = nm.resolve(tn);
     if (a == 0 || b == 0) continue;
     g.link_from.push_back(a);
     g.link_to.push_back(b);
@@ -358,16 +427,52 @@ Graph parse_gfa(const std::string &path, int threads) {
     }
   }
   for (auto &c : g.link_optional) pad_column(c, g.link_from.size());
+}
 
-  // P / W lines in parallel, one vector per line, then flattened
+// P line header: the name and, from the end of the steps field, the
+// overlap (the rest of the line after the blanks that follow the steps).
+void path_header(std::string_view line, size_t steps_end, Graph &g, size_t i) {
+  size_t pos = 1;
+  while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
+  const size_t b = pos;
+  while (pos < line.size() && line[pos] != ' ' && line[pos] != '\t') ++pos;
+  g.path_names[i].assign(line.substr(b, pos - b));
+  pos = steps_end;
+  while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
+  g.path_overlaps[i].assign(line.substr(pos));
+}
+
+// W line header fields (sample, hap, seq id, start, end); throws on a
+// malformed start / end.
+void walk_header(std::string_view line, Graph &g, size_t i) {
+  size_t pos = 1;
+  const std::string_view sample = next_field(line, pos), hap = next_field(line, pos);
+  const std::string_view seqid = next_field(line, pos), st = next_field(line, pos);
+  const std::string_view en = next_field(line, pos);
+  g.walk_sample_ids[i].assign(sample);
+  uint32_t h = 0;
+  for (char c : hap) h = h * 10 + (uint32_t)(c - '0');
+  g.walk_hap_indices[i] = h;
+  g.walk_seq_ids[i].assign(seqid);
+  g.walk_seq_starts[i] = st == "*" ? -1 : parse_i64(st);
+  g.walk_seq_ends[i] = en == "*" ? -1 : parse_i64(en);
+}
+
+void size_traversals(Graph &g, size_t np, size_t nw) {
+  g.path_names.resize(np);
+  g.path_overlaps.resize(np);
+  g.walk_sample_ids.resize(nw);
+  g.walk_seq_ids.resize(nw);
+  g.walk_hap_indices.resize(nw);
+  g.walk_seq_starts.resize(nw);
+  g.walk_seq_ends.resize(nw);
+}
+
+// P / W lines on the host, in parallel, one vector per line, then flattened.
+void parse_traversals_host(const char *d, const Lines &ls, const Names &nm, int threads, Graph &g) {
+  const std::vector<Line> &P = ls.P, &W = ls.W;
   std::vector<std::vector<int32_t>> ptrav(P.size()), wtrav(W.size());
-  g.path_names.resize(P.size());
-  g.path_overlaps.resize(P.size());
-  g.walk_sample_ids.resize(W.size());
-  g.walk_seq_ids.resize(W.size());
-  g.walk_hap_indices.resize(W.size());
-  g.walk_seq_starts.resize(W.size());
-  g.walk_seq_ends.resize(W.size());
+  size_traversals(g, P.size(), W.size());
   const int nth = resolve_threads(threads);
   std::string first_error;
   bool failed = false;
@@ -377,15 +482,12 @@ Graph parse_gfa(const std::string &path, int threads) {
       const std::string_view line(d + P[i].off, P[i].len);
       size_t pos = 1;
       while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
-      size_t b = pos;
       while (pos < line.size() && line[pos] != ' ' && line[pos] != '\t') ++pos;
-      g.path_names[i].assign(line.substr(b, pos - b));
       while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
-      b = pos;
+      const size_t b = pos;
       while (pos < line.size() && line[pos] != ' ' && line[pos] != '\t') ++pos;
       const std::string_view steps = line.substr(b, pos - b);
-      while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
-      g.path_overlaps[i].assign(line.substr(pos));
+      path_header(line, pos, g, (size_t)i);
       std::vector<int32_t> &out = ptrav[i];
       size_t commas = 0;
       for (char c : steps) commas += c == ',';
@@ -396,7 +498,7 @@ Graph parse_gfa(const std::string &path, int threads) {
           if (k > s0) {
             const std::string_view tok = steps.substr(s0, k - s0);
             const char o = tok.back();
-            const uint32_t id = resolve(tok.substr(0, tok.size() - 1));
+            const uint32_t id = nm.resolve(tok.substr(0, tok.size() - 1));
             if (id != 0) out.push_back(o == '-' ? -(int32_t)id : (int32_t)id);
           }
           s0 = k + 1;
@@ -415,9 +517,8 @@ Graph parse_gfa(const std::string &path, int threads) {
     try {
       const std::string_view line(d + W[i].off, W[i].len);
       size_t pos = 1;
-      const std::string_view sample = next_field(line, pos), hap = next_field(line, pos);
-      const std::string_view seqid = next_field(line, pos), st = next_field(line, pos);
-      const std::string_view en = next_field(line, pos), walk = next_field(line, pos);
+      for (int f = 0; f < 5; ++f) next_field(line, pos);
+      const std::string_view walk = next_field(line, pos);
       std::vector<int32_t> &out = wtrav[i];
       size_t nsteps = 0;
       for (char c : walk) nsteps += (c == '>' || c == '<');
@@ -432,18 +533,12 @@ Graph parse_gfa(const std::string &path, int threads) {
         size_t e = p + 1;
         while (e < walk.size() && walk[e] != '>' && walk[e] != '<') ++e;
         if (e > p + 1) {
-          const uint32_t id = resolve(walk.substr(p + 1, e - p - 1));
+          const uint32_t id = nm.resolve(walk.substr(p + 1, e - p - 1));
           if (id != 0) out.push_back(o == '<' ? -(int32_t)id : (int32_t)id);
         }
         p = e;
       }
-      g.walk_sample_ids[i].assign(sample);
-      uint32_t h = 0;
-      for (char c : hap) h = h * 10 + (uint32_t)(c - '0');
-      g.walk_hap_indices[i] = h;
-      g.walk_seq_ids[i].assign(seqid);
-      g.walk_seq_starts[i] = st == "*" ? -1 : parse_i64(st);
-      g.walk_seq_ends[i] = en == "*" ? -1 : parse_i64(en);
+      walk_header(line, g, (size_t)i);
     } catch (const std::exception &e) {
 #pragma omp critical
       {
@@ -464,15 +559,16 @@ Graph parse_gfa(const std::string &path, int threads) {
   };
   flatten(ptrav, g.paths);
   flatten(wtrav, g.walks);
+}
 
-  // J / C lines
-  for (const Line &ln : J) {
+void parse_jumps_containments(const char *d, const Lines &ls, const Names &nm, Graph &g) {
+  for (const Line &ln : ls.J) {
     const std::string_view line(d + ln.off, ln.len);
     size_t pos = 1;
     const std::string_view fn = next_field(line, pos), fo = next_field(line, pos);
     const std::string_view tn = next_field(line, pos), to = next_field(line, pos);
     const std::string_view dist = next_field(line, pos);
-    const uint32_t a = resolve(fn), b = resolve(tn);
+    const uint32_t a = nm.resolve(fn), b = nm.resolve(tn);
     if (a == 0 || b == 0) continue;
     g.jump_from.push_back(a);
     g.jump_from_orients.push_back(fo.empty() ? '+' : fo[0]);
@@ -488,13 +584,13 @@ Graph parse_gfa(const std::string &path, int threads) {
     }
     g.jump_rest.push_back(std::move(rest));
   }
-  for (const Line &ln : C) {
+  for (const Line &ln : ls.C) {
     const std::string_view line(d + ln.off, ln.len);
     size_t pos = 1;
     const std::string_view cn = next_field(line, pos), co = next_field(line, pos);
     const std::string_view tn = next_field(line, pos), to = next_field(line, pos);
     const std::string_view ps = next_field(line, pos), ov = next_field(line, pos);
-    const uint32_t a = resolve(cn), b = resolve(tn);
+    const uint32_t a = nm.resolve(cn), b = nm.resolve(tn);
     if (a == 0 || b == 0) continue;
     g.cont_container.push_back(a);
     g.cont_container_orients.push_back(co.empty() ? '+' : co[0]);
@@ -511,7 +607,269 @@ Graph parse_gfa(const std::string &path, int threads) {
     }
     g.cont_rest.push_back(std::move(rest));
   }
+}
+
+Graph empty_graph() {
+  Graph g;
+  g.node_names.emplace_back();
+  g.node_sequences.emplace_back();
   return g;
+}
+
+}  // namespace
+
+Graph parse_gfa(const std::string &path, int threads) {
+  Graph g = empty_graph();
+  const Mapped m = map_file(path);
+  const char *d = m.data;
+  Lines ls;
+  scan_lines(d, m.size, ls, g);
+  Names nm;
+  parse_segments(d, ls.S, g, nm, threads);
+  parse_links(d, ls.L, nm, g);
+  parse_traversals_host(d, ls, nm, threads, g);
+  parse_jumps_containments(d, ls, nm, g);
+  return g;
+}
+
+// ---------------------------------------------------------------------------
+// Device front end: the file in HBM; line index, P/W field bounds and step
+// tokens on the GPU (parse_kernels.cu); S/L/J/C lines and the short P/W
+// header fields on the host.  Same Graph as parse_gfa for every input,
+// errors included (with one thread, parse_gfa reports the first P error,
+// else the first W line's error, token errors before start/end errors).
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+T download_one(const T *p, cudaStream_t st) {
+  T v;
+  cuda_check(cudaMemcpyAsync(&v, p, sizeof(T), cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  return v;
+}
+
+// One launch bracketed by the context's kernel timer (algorithmic bytes).
+template <class F>
+void timed(Context &ctx, const char *name, double bytes, F &&launch) {
+  ctx.tbegin(name, bytes);
+  launch();
+  ctx.tend();
+}
+
+void scan_u32(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out) {
+  uint32_t *counter = nullptr;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(n), &counter);
+  timed(ctx, "gfa_scan", 12.0 * n,
+        [&] { launch_excl_scan_u32(in, n, out, desc, counter, ctx.dstatus(), ctx.stream()); });
+}
+
+struct PhaseClock {
+  bool on = debug_enabled();
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char *what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::cerr << "[gfa front end] " << what << ": " << std::chrono::duration<double, std::milli>(now - t).count()
+              << " ms" << std::endl;
+    t = now;
+  }
+};
+
+const char *token_error(uint32_t code) {
+  return code == kParseOverflow ? "parse_uint32: overflow" : "parse_uint32: no digits";
+}
+
+}  // namespace
+
+DeviceParse parse_gfa_device(Context &ctx, const std::string &path, int threads) {
+  DeviceParse r(ctx.stream());
+  Graph &g = r.graph;
+  g = empty_graph();
+  const Mapped m = map_file(path);
+  const char *d = m.data;
+  const uint64_t n = m.size;
+  cudaStream_t st = ctx.stream();
+  Lines ls;
+  Names nm;
+  if (!n) {
+    size_traversals(g, 0, 0);
+    g.paths.offsets.assign(1, 0);
+    g.walks.offsets.assign(1, 0);
+    r.offsets.assign(1, 0);
+    return r;
+  }
+  ctx.reset_status();
+  PhaseClock clk;
+  // the file, zero-padded to 16 bytes
+  const uint64_t npad = (n + 15) & ~15ull;
+  DevVec<char> text(st);
+  text.resize(npad);
+  if (npad > n) cuda_check(cudaMemsetAsync(text.ptr + n, 0, npad - n, st), "memset");
+  cuda_check(cudaMemcpyAsync(text.ptr, d, n, cudaMemcpyHostToDevice, st), "file upload");
+  // line index
+  const uint64_t nt = parse_num_tiles(n);
+  DevVec<uint32_t> cnt(st), cnt2(st);
+  DevVec<uint64_t> nl_off(st);
+  cnt.resize(nt);
+  nl_off.resize(nt + 1);
+  timed(ctx, "gfa_newlines", (double)n, [&] { launch_nl_count(text.ptr, n, cnt.ptr, st); });
+  scan_u32(ctx, cnt.ptr, nt, nl_off.ptr);
+  const uint64_t nl = download_one(nl_off.ptr + nt, st);
+  clk.mark("upload + newline count");
+  const uint64_t nlines = nl + (d[n - 1] != '\n' ? 1 : 0);
+  DevVec<uint64_t> eol(st), slotoff(st);
+  DevVec<uint8_t> type(st);
+  DevVec<uint32_t> ispw(st);
+  eol.resize(nl ? nl : 1);
+  type.resize(nlines);
+  ispw.resize(nlines);
+  slotoff.resize(nlines + 1);
+  timed(ctx, "gfa_newlines", (double)n + 8.0 * nl, [&] { launch_nl_write(text.ptr, n, nl_off.ptr, eol.ptr, st); });
+  timed(ctx, "gfa_line_heads", 13.0 * nlines,
+        [&] { launch_line_heads(text.ptr, n, eol.ptr, nl, nlines, type.ptr, ispw.ptr, st); });
+  scan_u32(ctx, ispw.ptr, nlines, slotoff.ptr);
+  std::vector<uint8_t> htype(nlines);
+  std::vector<uint64_t> heol(nl);
+  uint64_t npw = 0;
+  cuda_check(cudaMemcpyAsync(htype.data(), type.ptr, nlines, cudaMemcpyDeviceToHost, st), "download");
+  if (nl) cuda_check(cudaMemcpyAsync(heol.data(), eol.ptr, nl * 8, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaMemcpyAsync(&npw, slotoff.ptr + nlines, 8, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  DevVec<PWLine> pw(st);
+  pw.resize(npw ? npw : 1);
+  timed(ctx, "gfa_line_fields", 9.0 * nlines + 32.0 * npw,
+        [&] { launch_line_fields(text.ptr, n, eol.ptr, nl, nlines, type.ptr, slotoff.ptr, pw.ptr, st); });
+  timed(ctx, "gfa_field_ends", (double)n,
+        [&] { launch_field_ends(text.ptr, n, nl_off.ptr, nlines, slotoff.ptr, pw.ptr, st); });
+  std::vector<uint64_t> pslot, wslot;  // record slot of each P / W line
+  for (uint64_t i = 0, slot = 0; i < nlines; ++i) {
+    const uint64_t s = i ? heol[i - 1] + 1 : 0, e = i < nl ? heol[i] : n;
+    if (e == s) continue;
+    ls.add(d, s, e - s, g);
+    if (htype[i] == 'P') pslot.push_back(slot++);
+    else if (htype[i] == 'W') wslot.push_back(slot++);
+  }
+  std::vector<uint8_t>().swap(htype);
+  std::vector<uint64_t>().swap(heol);
+  clk.mark("line index");
+
+  parse_segments(d, ls.S, g, nm, threads);
+  clk.mark("S lines");
+  NameIndex ni{nullptr, 0, nullptr, nullptr};
+  DevVec<uint32_t> slots(st), nlen(st);
+  DevVec<uint64_t> noff(st);
+  if (!nm.numeric) {
+    const uint64_t nn = nm.by_id.size() - 1;
+    uint64_t cap = 1024;
+    while (cap < 2 * nn) cap <<= 1;
+    std::vector<uint64_t> ho(nn + 1, 0);
+    std::vector<uint32_t> hl(nn + 1, 0);
+    for (uint64_t id = 1; id <= nn; ++id) {
+      ho[id] = (uint64_t)(nm.by_id[id].data() - d);
+      hl[id] = (uint32_t)std::min<size_t>(nm.by_id[id].size(), UINT32_MAX);
+    }
+    slots.resize(cap);
+    noff.resize(nn + 1);
+    nlen.resize(nn + 1);
+    cuda_check(cudaMemsetAsync(slots.ptr, 0, cap * 4, st), "memset");
+    cuda_check(cudaMemcpyAsync(noff.ptr, ho.data(), (nn + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+    cuda_check(cudaMemcpyAsync(nlen.ptr, hl.data(), (nn + 1) * 4, cudaMemcpyHostToDevice, st), "upload");
+    timed(ctx, "gfa_name_table", 16.0 * nn,
+          [&] { launch_name_table(text.ptr, noff.ptr, nlen.ptr, nn, slots.ptr, cap - 1, st); });
+    ni = NameIndex{slots.ptr, cap - 1, noff.ptr, nlen.ptr};
+    cuda_check(cudaStreamSynchronize(st), "stream sync");  // ho / hl leave scope
+  }
+  parse_links(d, ls.L, nm, g);
+
+  // P / W steps
+  DevVec<uint64_t> offP(st), offW(st);
+  DevVec<unsigned long long> err(st);
+  cnt.resize(nt);
+  cnt2.resize(nt);
+  offP.resize(nt + 1);
+  offW.resize(nt + 1);
+  err.resize(1);
+  cuda_check(cudaMemsetAsync(err.ptr, 0xFF, 8, st), "memset");
+  timed(ctx, "gfa_tokens", (double)n,
+        [&] { launch_token_count(text.ptr, n, nl_off.ptr, nlines, slotoff.ptr, pw.ptr, ni, cnt.ptr, cnt2.ptr,
+                                 err.ptr, st); });
+  scan_u32(ctx, cnt.ptr, nt, offP.ptr);
+  scan_u32(ctx, cnt2.ptr, nt, offW.ptr);
+  uint64_t tot[2];
+  unsigned long long herr = 0;
+  cuda_check(cudaMemcpyAsync(&tot[0], offP.ptr + nt, 8, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaMemcpyAsync(&tot[1], offW.ptr + nt, 8, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaMemcpyAsync(&herr, err.ptr, 8, cudaMemcpyDeviceToHost, st), "download");
+  ctx.read_status();
+  ctx.check_status("GFA front end");
+  std::vector<PWLine> recs(npw);
+  if (npw) {
+    cuda_check(cudaMemcpyAsync(recs.data(), pw.ptr, npw * sizeof(PWLine), cudaMemcpyDeviceToHost, st), "download");
+    cuda_check(cudaStreamSynchronize(st), "stream sync");
+  }
+  const size_t np = ls.P.size(), nw = ls.W.size();
+  size_traversals(g, np, nw);
+  // errors: the first P step error, else the first W line with an error
+  // (its step error before its start/end error)
+  if (herr != ~0ull && !(herr >> 62)) throw std::runtime_error(token_error((uint32_t)(herr & 3)));
+  uint64_t wbad = nw;  // W line of the step error
+  if (herr != ~0ull) {
+    const uint64_t at = (herr & ((1ull << 62) - 1)) >> 2;
+    for (uint64_t k = 0; k < nw; ++k) {
+      const PWLine &rec = recs[wslot[k]];
+      if (at >= rec.fstart && at < rec.fend) {
+        wbad = k;
+        break;
+      }
+    }
+  }
+  for (uint64_t k = 0; k < nw; ++k) {
+    if (k == wbad) throw std::runtime_error(token_error((uint32_t)(herr & 3)));
+    walk_header(std::string_view(d + ls.W[k].off, ls.W[k].len), g, k);
+  }
+  if (herr != ~0ull) throw std::runtime_error(token_error((uint32_t)(herr & 3)));
+  for (uint64_t k = 0; k < np; ++k)
+    path_header(std::string_view(d + ls.P[k].off, ls.P[k].len), recs[pslot[k]].fend - ls.P[k].off, g, k);
+
+  clk.mark("L lines + step count");
+  r.steps.resize(tot[0] + tot[1]);
+  timed(ctx, "gfa_tokens", (double)n + 4.0 * (tot[0] + tot[1]), [&] {
+    launch_token_write(text.ptr, n, nl_off.ptr, nlines, slotoff.ptr, pw.ptr, ni, offP.ptr, offW.ptr, r.steps.ptr,
+                       r.steps.ptr + tot[0], err.ptr, st);
+  });
+  if (npw) cuda_check(cudaMemcpyAsync(recs.data(), pw.ptr, npw * sizeof(PWLine), cudaMemcpyDeviceToHost, st),
+                      "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  auto line_offsets = [&](const std::vector<uint64_t> &slot, uint64_t total, std::vector<uint64_t> &off) {
+    off.assign(slot.size() + 1, total);
+    for (size_t k = 0; k < slot.size(); ++k) {
+      const uint64_t o = recs[slot[k]].out;
+      off[k] = o == ~0ull ? total : o;
+    }
+  };
+  line_offsets(pslot, tot[0], g.paths.offsets);
+  line_offsets(wslot, tot[1], g.walks.offsets);
+  r.offsets.assign(np + nw + 1, 0);
+  for (size_t k = 0; k < np; ++k) r.offsets[k + 1] = g.paths.offsets[k + 1];
+  for (size_t k = 0; k < nw; ++k) r.offsets[np + k + 1] = tot[0] + g.walks.offsets[k + 1];
+  parse_jumps_containments(d, ls, nm, g);
+  clk.mark("steps + J/C lines");
+  return r;
+}
+
+void download_steps(Context &ctx, const DeviceParse &r, Graph &g) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t NP = g.paths.offsets.empty() ? 0 : g.paths.offsets.back();
+  const uint64_t NW = g.walks.offsets.empty() ? 0 : g.walks.offsets.back();
+  g.paths.steps.resize(NP);
+  g.walks.steps.resize(NW);
+  if (NP)
+    cuda_check(cudaMemcpyAsync(g.paths.steps.data(), r.steps.ptr, NP * 4, cudaMemcpyDeviceToHost, st), "download");
+  if (NW)
+    cuda_check(cudaMemcpyAsync(g.walks.steps.data(), r.steps.ptr + NP, NW * 4, cudaMemcpyDeviceToHost, st),
+               "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
 }
 
 }  // namespace gfz

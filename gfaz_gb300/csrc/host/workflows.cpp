@@ -4,6 +4,8 @@
 // text) runs on the GPU through the device pipeline.
 #include "workflows.h"
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cstring>
 #include <fstream>
@@ -358,7 +360,7 @@ TextPieces walk_pieces(const std::vector<std::string> &samples, const std::vecto
 // Compression
 // ---------------------------------------------------------------------------
 Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t threshold, int delta_round, int threads,
-                          bool show_stats) {
+                          bool show_stats, const int32_t *d_steps) {
   const int nth = resolve_threads(threads);
   set_zstd_threads(nth);
   Compressed out;
@@ -382,8 +384,11 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   for (uint64_t t = 0; t < nw; ++t) off[np + t + 1] = NP + g.walks.offsets[t + 1];
   cudaStream_t st = ctx.stream();
   Grammar gram(st);
-  encode_host(ctx, {HostSeg{g.paths.steps.data(), NP}, HostSeg{g.walks.steps.data(), NW}}, off,
-              EncodeParams{rounds, delta_round}, gram);
+  if (d_steps)
+    encode_traversals(ctx, d_steps, off, EncodeParams{rounds, delta_round}, gram);
+  else
+    encode_host(ctx, {HostSeg{g.paths.steps.data(), NP}, HostSeg{g.walks.steps.data(), NW}}, off,
+                EncodeParams{rounds, delta_round}, gram);
 
   // rule columns (split + delta on the device)
   DevVec<int32_t> dfirst(st), dsecond(st);
@@ -513,8 +518,39 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   return out;
 }
 
+namespace {
+uint64_t file_size(const std::string &path) {
+  struct stat sb;
+  return stat(path.c_str(), &sb) == 0 ? (uint64_t)sb.st_size : 0;
+}
+}  // namespace
+
+bool device_front_end_fits(const Context &ctx, uint64_t file_bytes) {
+  // the file, line and tile arrays, the steps (at most half the bytes / 2
+  // steps of 4 bytes)
+  return !ctx.hbm_budget || 3 * file_bytes + (64ull << 20) <= ctx.hbm_budget;
+}
+
+Graph parse_graph(Context &ctx, const std::string &gfa_path, int threads) {
+  if (ctx.front_end && device_front_end_fits(ctx, file_size(gfa_path))) {
+    DeviceParse r = parse_gfa_device(ctx, gfa_path, threads);
+    download_steps(ctx, r, r.graph);
+    return std::move(r.graph);
+  }
+  return parse_gfa(gfa_path, threads);
+}
+
 Compressed compress_gfa(Context &ctx, const std::string &gfa_path, int rounds, uint64_t threshold, int delta_round,
                         int threads, bool show_stats) {
+  if (ctx.front_end && device_front_end_fits(ctx, file_size(gfa_path))) {
+    DeviceParse r = parse_gfa_device(ctx, gfa_path, threads);
+    const uint64_t n = r.offsets.back();
+    if (resident_fits(ctx, n))
+      return compress_graph(ctx, r.graph, rounds, threshold, delta_round, threads, show_stats, r.steps.ptr);
+    download_steps(ctx, r, r.graph);
+    r.steps.release();
+    return compress_graph(ctx, r.graph, rounds, threshold, delta_round, threads, show_stats);
+  }
   const Graph g = parse_gfa(gfa_path, threads);
   return compress_graph(ctx, g, rounds, threshold, delta_round, threads, show_stats);
 }

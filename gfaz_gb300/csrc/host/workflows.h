@@ -19,12 +19,33 @@ struct WalkKey {
   int64_t seq_start = -1, seq_end = -1;
 };
 
+// GFA front end on the device (src/io/gfa_parser.cpp:306-590 with the P/W
+// steps resolved on the GPU): the graph as parse_gfa returns it, except
+// that graph.paths / graph.walks hold only their offsets; the steps stay on
+// the device, paths then walks back to back (offsets: np + nw + 1 entries).
+struct DeviceParse {
+  explicit DeviceParse(cudaStream_t st) : steps(st) {}
+  Graph graph;
+  DevVec<int32_t> steps;
+  std::vector<uint64_t> offsets;
+};
+DeviceParse parse_gfa_device(Context &ctx, const std::string &path, int threads);
+// Copies the parsed steps into graph.paths.steps / graph.walks.steps.
+void download_steps(Context &ctx, const DeviceParse &r, Graph &g);
+// Whether the device front end fits ctx's HBM budget for a file this size.
+bool device_front_end_fits(const Context &ctx, uint64_t file_bytes);
+// The parsed graph: the device front end when ctx.front_end is set and it
+// fits the budget, else the host parser.
+Graph parse_graph(Context &ctx, const std::string &gfa_path, int threads);
+
 // src/workflows/compression_workflow.cpp:706 compress_gfa
 Compressed compress_gfa(Context &ctx, const std::string &gfa_path, int rounds, uint64_t threshold, int delta_round,
                         int threads, bool show_stats);
-// Same, from an already parsed graph (the graph's traversals are left as is).
+// Same, from an already parsed graph (the graph's traversals are left as
+// is).  d_steps (optional): the traversals' steps on the device, paths then
+// walks back to back, used in place of g's host steps.
 Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t threshold, int delta_round,
-                          int threads, bool show_stats);
+                          int threads, bool show_stats, const int32_t *d_steps = nullptr);
 
 // src/io/gfa_writer.cpp:376 write_gfa_from_compressed_data (H,S,L,J,C,P,W)
 void write_gfa(Context &ctx, const Compressed &c, const std::string &out_path, int threads);

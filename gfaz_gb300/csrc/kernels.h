@@ -282,4 +282,63 @@ void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, co
 // unordered.
 void launch_find_newlines(const char *text, uint64_t n, unsigned long long *out, uint64_t cap, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// GFA front end (parse_kernels.cu).  The text buffer holds the file's n
+// bytes padded with zeros to a multiple of 16 bytes; work runs in tiles of
+// 4 KB (parse_num_tiles).
+// ---------------------------------------------------------------------------
+// One P or W line: its steps / walk field [fstart, fend) and the index of
+// its first step in the P or W output.
+struct PWLine {
+  uint64_t fstart;
+  unsigned long long fend;
+  uint64_t out;
+  uint32_t kind;  // 0 = P, 1 = W
+  uint32_t pad;
+};
+// Segment-name lookup: slots == nullptr resolves names as decimal numbers;
+// otherwise slots[mask + 1] hold the ids of the names (linear probing) and
+// name id sits at text[noff[id] .. + nlen[id]).
+struct NameIndex {
+  const uint32_t *slots;
+  uint64_t mask;
+  const uint64_t *noff;
+  const uint32_t *nlen;
+};
+// Error codes in the low two bits of the front end's error word (the
+// smallest of W << 62 | byte position << 2 | code over the file).
+constexpr uint32_t kParseNoDigits = 1;  // parse_uint32: no digits
+constexpr uint32_t kParseOverflow = 2;  // parse_uint32: overflow
+
+uint64_t parse_num_tiles(uint64_t n);
+// cnt[tile] = '\n' bytes in the tile.
+void launch_nl_count(const char *text, uint64_t n, uint32_t *cnt, cudaStream_t st);
+// eol[nl_off[tile] + j] = position of the tile's j-th '\n' (nl_off: the
+// exclusive scan of cnt).
+void launch_nl_write(const char *text, uint64_t n, const uint64_t *nl_off, uint64_t *eol, cudaStream_t st);
+// Line i = [i ? eol[i-1] + 1 : 0, i < nl ? eol[i] : n): type[i] = its first
+// byte (0 when empty), ispw[i] = whether it is a P or W line.
+void launch_line_heads(const char *text, uint64_t n, const uint64_t *eol, uint64_t nl, uint64_t nlines,
+                       uint8_t *type, uint32_t *ispw, cudaStream_t st);
+// pw[slotoff[i]] for every P/W line i (slotoff: exclusive scan of ispw):
+// fstart after the leading fields, fend = the line end, out = ~0.
+void launch_line_fields(const char *text, uint64_t n, const uint64_t *eol, uint64_t nl, uint64_t nlines,
+                        const uint8_t *type, const uint64_t *slotoff, PWLine *pw, cudaStream_t st);
+// fend lowered to the first blank at or after fstart.
+void launch_field_ends(const char *text, uint64_t n, const uint64_t *nl_off, uint64_t nlines, const uint64_t *slotoff,
+                       PWLine *pw, cudaStream_t st);
+// Per-tile counts of the kept P and W steps; numeric parse errors to *err
+// (set it to ~0 first).
+void launch_token_count(const char *text, uint64_t n, const uint64_t *nl_off, uint64_t nlines,
+                        const uint64_t *slotoff, PWLine *pw, const NameIndex &ni, uint32_t *cntP, uint32_t *cntW,
+                        unsigned long long *err, cudaStream_t st);
+// The kept steps at offP / offW (exclusive scans of the counts) and every
+// P/W line's pw[].out.
+void launch_token_write(const char *text, uint64_t n, const uint64_t *nl_off, uint64_t nlines,
+                        const uint64_t *slotoff, PWLine *pw, const NameIndex &ni, const uint64_t *offP,
+                        const uint64_t *offW, int32_t *outP, int32_t *outW, unsigned long long *err, cudaStream_t st);
+// Inserts names 1 .. nnames (NameIndex layout) into slots (zeroed).
+void launch_name_table(const char *text, const uint64_t *noff, const uint32_t *nlen, uint64_t nnames,
+                       uint32_t *slots, uint64_t mask, cudaStream_t st);
+
 }  // namespace gfz

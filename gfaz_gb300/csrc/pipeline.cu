@@ -879,14 +879,19 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   cuda_check(cudaStreamSynchronize(st), "stream sync");
 }
 
+bool resident_fits(const Context &ctx, uint64_t n) {
+  if (ctx.encode_chunk) return false;
+  // input, two stream buffers, per-tile words, a pair table
+  return !ctx.hbm_budget ||
+         12 * n + n / 2 + (64ull << 20) + 16 * std::min<uint64_t>(n, 1ull << 23) <= ctx.hbm_budget;
+}
+
 void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
                  const EncodeParams &p, Grammar &g) {
   const uint64_t N = h_off.empty() ? 0 : h_off.back();
   uint64_t chunk = ctx.encode_chunk;
   if (!chunk && ctx.hbm_budget) {
-    // resident: input, two stream buffers, per-tile words, a pair table
-    const uint64_t resident = 12 * N + N / 2 + (64ull << 20) + 16 * std::min<uint64_t>(N, 1ull << 23);
-    if (resident > ctx.hbm_budget) {
+    if (!resident_fits(ctx, N)) {
       // chunked: per-tile words and tile arrays of the whole stream, a pair
       // table, the final stream; chunk buffers of 12 bytes per step
       const uint64_t fixed = N / 2 + N / 64 + 4 * N / 8 + (64ull << 20) + 16 * std::min<uint64_t>(N, 1ull << 24);

@@ -132,6 +132,7 @@ class Context {
   uint64_t encode_chunk = 0;     // steps per chunk of host-input compression (0 = from the budget)
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
+  int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
   // Tuner: (kernel, stream class) -> the variant that was faster the first
   // time the class came up (see encode_traversals).  With GFAZ_TUNE_FILE
   // set, decisions are loaded from that file when the context is made and
@@ -221,6 +222,10 @@ struct HostSeg {
 // budget (rounds shrink the stream).
 void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
                          const EncodeParams &p, uint64_t chunk, uint64_t budget, Grammar &g);
+
+// Whether compression of n steps runs resident in HBM under ctx's budget
+// and chunk options (working set about 12.5 bytes per step).
+bool resident_fits(const Context &ctx, uint64_t n);
 
 // Compression of host-resident input: resident in HBM when its working set
 // (about 12.5 bytes per step) fits ctx.hbm_budget, else in chunks

@@ -87,7 +87,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * "hbm_budget" = device bytes that compression of host-resident input may
  * use (default 0 = no limit): above it the stream stays in host memory and
  * passes through HBM in chunks, with identical output; "encode_chunk" =
- * steps per such chunk, forcing chunked compression (default 0). */
+ * steps per such chunk, forcing chunked compression (default 0);
+ * "front_end" = the GFA parse of file compression: 1 (default) = the
+ * device front end (line index and P/W steps on the GPU), 0 = the host
+ * parser; both give the same graph, and the host parser also runs when the
+ * file does not fit "hbm_budget" three times over. */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
@@ -127,6 +131,12 @@ gfz_status gfz_extract_walk_lines_by_name(gfz_context *ctx, const gfz_compressed
                                           size_t n, int threads, char **out, size_t *len);
 /* add_haplotypes, include/workflows/add_haplotypes_workflow.hpp:9-10 (in place) */
 gfz_status gfz_add_haplotypes(gfz_context *ctx, gfz_compressed *c, const char *path, int threads);
+/* parse_gfa_file, src/python/bindings.cpp:659-660 (GfaParser::parse,
+ * src/io/gfa_parser.cpp:306-590): device != 0 parses with the device front
+ * end on ctx (NULL: the default context), device == 0 with the host parser
+ * (ctx unused; no GPU needed).  Parse errors are "GFA parser error: ..." or
+ * the value parser's own message, as in the reference. */
+gfz_status gfz_parse_gfa(gfz_context *ctx, const char *path, int threads, int device, gfz_graph **out);
 /* decompress_gfa, include/workflows/decompression_workflow.hpp:8-9 */
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out);
 void gfz_graph_free(gfz_graph *g);
@@ -151,7 +161,8 @@ gfz_status gfz_compressed_block(const gfz_compressed *c, const char *field, void
 gfz_status gfz_graph_traversals(const gfz_graph *g, int kind, const int32_t **steps, const uint64_t **offsets,
                                 uint64_t *ntrav);
 /* Newline-joined string fields: "path_names", "path_overlaps",
- * "walk_sample_ids", "walk_seq_ids", "header". */
+ * "walk_sample_ids", "walk_seq_ids", "segment_names", "segment_sequences"
+ * (segments in id order), "header". */
 gfz_status gfz_graph_strings(const gfz_graph *g, const char *field, char **out, size_t *len);
 gfz_status gfz_graph_walk_numbers(const gfz_graph *g, const uint32_t **haps, const int64_t **starts,
                                   const int64_t **ends, uint64_t *n);

@@ -1,0 +1,78 @@
+"""GFA inputs for the parser tests: edge cases of the reference parser's
+traversal rules (src/io/gfa_parser.cpp:353-404, 600-625, 676-795,
+1210-1218) and error cases with the message each must raise."""
+from __future__ import annotations
+
+import numpy as np
+
+from gfaz_gb300 import synthetic
+
+
+def _segs(n, named=False):
+    return "".join("S\t%s\t%s\n" % (("n%dx" % i) if named else str(i), "ACGT"[: 1 + i % 4]) for i in range(1, n + 1))
+
+
+# name -> GFA text (bytes)
+CASES = {
+    "numeric_edges": (
+        "H\tVN:Z:1.0\n" + _segs(12)
+        + "P\tp1\t1+,2-,3+\t*\n"
+        + "P\tp2\t4+,,5-,\t4M,3M\n"            # empty pieces, trailing comma
+        + "P\tp3\t6\t*\n"                        # no orientation: name is empty
+        + "P\tp4\t007+,0+,12-\t*\tXX:i:1\n"      # leading zeros, id 0, extra field
+        + "P  p5  1+,2+  *\n"                     # spaces as separators
+        + "P\tp6\t\t*\n"                         # the steps field is '*'
+        + "P\tp7\n"                              # name only
+        + "W\ts1\t1\tchr1\t0\t100\tjunk>1<2><>3\tXY:Z:a\n"  # junk, empty name
+        + "W\ts2\t2\tchr2\t*\t*\t>11<12\n"
+        + "P\tp8\t1+,2+\r\n"                     # CR kept in the last piece
+        + "W\ts3\t0\tchr3\t5\t6\n"               # no walk field
+        + "\n#comment\n"
+        + "P\tp9\t" + "0" * 5000 + "3+,4-\t*\n"  # a token longer than a tile
+        + "W\tlong\t3\tc\t1\t2\t" + ">1<2" * 3000 + "\n"
+        + "P\tp10\t9-,10+"                       # no final newline
+    ).encode(),
+    "named": (
+        "S\tsA\tAC\nS\tsB\tG\nS\tsA\tT\nS\t3\tC\n"     # duplicate name, numeric-looking name
+        + "P\tq1\tsA+,sB-,3+,zz+,sA-\t*\n"              # zz is not a segment
+        + "W\tx\t1\tc\t0\t1\t>sA<sB>3>nope<sA\n"
+    ).encode(),
+    "out_of_order": "S\t2\tA\nS\t1\tC\nP\tp\t1+,2-\t*\nW\ts\t0\tc\t*\t*\t<1>2\n".encode(),
+    "only_walks": (_segs(5) + "W\ta\t0\tc\t0\t9\t>1>2>3\nW\tb\t1\tc\t*\t*\t<5<4\n").encode(),
+    "no_traversals": (_segs(3) + "L\t1\t+\t2\t-\t0M\n").encode(),
+    "empty_file": b"",
+    "header_only": b"H\tVN:Z:1.0",
+}
+
+# name -> (text, message of the raised error)
+ERRORS = {
+    "p_no_digits": ((_segs(3) + "P\tp\t1+,x+\t*\n").encode(), "parse_uint32: no digits"),
+    "p_overflow": ((_segs(3) + "P\tp\t1+,99999999999+\t*\n").encode(), "parse_uint32: overflow"),
+    "w_no_digits": ((_segs(3) + "W\ts\t1\tc\t0\t1\t>1>y\n").encode(), "parse_uint32: no digits"),
+    # a P error wins over a W error earlier in the file
+    "p_before_w": ((_segs(3) + "W\ts\t1\tc\t0\t1\t>1>y\nP\tp\t99999999999+\t*\n").encode(),
+                   "parse_uint32: overflow"),
+    # the first W line with an error decides; its start/end after its steps
+    "w_header_first": ((_segs(3) + "W\ts\t1\tc\t-\t1\t>1\nW\tt\t1\tc\t0\t1\t>x\n").encode(),
+                       "parse_int64: no digits"),
+    "w_steps_before_header": ((_segs(3) + "W\ts\t1\tc\t-\t1\t>x\n").encode(), "parse_uint32: no digits"),
+    "s_overflow": (("S\t99999999999\tA\nP\tp\t1+\t*\n").encode(), "parse_uint32: overflow"),
+}
+
+
+def random_text(seed: int, n_segments: int, n_paths: int, n_walks: int, named: bool = False) -> bytes:
+    """A P + W GFA text from the config-2 generator's paths (numeric or
+    named segments), P and W lines interleaved."""
+    steps, off, _ = synthetic.cfg2_stream(seed=seed, n_segments=n_segments, n_paths=n_paths + n_walks)
+    name = (lambda v: "n%dx" % v) if named else str
+    parts = ["H\tVN:Z:1.0\n", _segs(n_segments, named)]
+    for t in range(n_paths + n_walks):
+        s = steps[int(off[t]):int(off[t + 1])]
+        a = np.abs(s)
+        if t % 2 == 0 and t // 2 < n_walks:
+            parts.append("W\tsample%d\t%d\tchr%d\t0\t%d\t%s\n" % (
+                t, t % 3, t, len(s), "".join(("<" if v < 0 else ">") + name(int(x)) for v, x in zip(s, a))))
+        else:
+            parts.append("P\tpath%d\t%s\t*\n" % (
+                t, ",".join(name(int(x)) + ("-" if v < 0 else "+") for v, x in zip(s, a))))
+    return "".join(parts).encode()

@@ -1,0 +1,60 @@
+"""Host GFA parser (the front end's CPU path and the reference the device
+front end is compared with): traversals equal the reference parser's on the
+golden inputs (raw streams generated with the reference), and the edge and
+error cases follow the restated rules of src/io/gfa_parser.cpp."""
+import os
+
+import numpy as np
+import pytest
+
+import gfaz_gb300 as gz
+from conftest import GOLDEN, golden_raw
+from oracle import gfa_parse
+from parse_cases import CASES, ERRORS
+
+
+def same_as_oracle(g, want):
+    assert g.header_line == want["header"].decode()
+    assert g.num_segments == want["segments"]
+    assert [n.encode() for n in g.path_names] == [p[0] for p in want["paths"]]
+    assert [o.encode() for o in g.path_overlaps] == [p[1] for p in want["paths"]]
+    assert [list(map(int, p)) for p in g.paths] == [p[2] for p in want["paths"]]
+    ws = want["walks"]
+    assert [s.encode() for s in g.walk_sample_ids] == [w[0] for w in ws]
+    assert list(g.walk_hap_indices) == [w[1] for w in ws]
+    assert [s.encode() for s in g.walk_seq_ids] == [w[2] for w in ws]
+    assert list(g.walk_seq_starts) == [w[3] for w in ws]
+    assert list(g.walk_seq_ends) == [w[4] for w in ws]
+    assert [list(map(int, w)) for w in g.walks] == [w[5] for w in ws]
+
+
+@pytest.mark.parametrize("case", ["cfg1_mini", "named", "rich", "tiny"])
+def test_host_parse_matches_reference_streams(case, manifest):
+    g = gz.parse_gfa(os.path.join(GOLDEN, case + ".gfa"), device=False)
+    raw, off, _ = golden_raw(case, manifest["cases"][case])
+    trav = g.paths + g.walks
+    assert np.array_equal(np.concatenate(trav) if trav else np.zeros(0, np.int32), raw)
+    assert np.array_equal(np.cumsum([0] + [len(t) for t in trav]), np.asarray(off, np.int64))
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_host_parse_edge_cases(case, tmp_path):
+    p = tmp_path / "in.gfa"
+    p.write_bytes(CASES[case])
+    same_as_oracle(gz.parse_gfa(str(p), device=False), gfa_parse.parse(CASES[case]))
+
+
+@pytest.mark.parametrize("case", sorted(ERRORS))
+def test_host_parse_errors(case, tmp_path):
+    text, msg = ERRORS[case]
+    with pytest.raises(ValueError, match=msg):
+        gfa_parse.parse(text)
+    p = tmp_path / "in.gfa"
+    p.write_bytes(text)
+    with pytest.raises(gz.GfazError, match=msg):
+        gz.parse_gfa(str(p), threads=1, device=False)
+
+
+def test_host_parse_missing_file(tmp_path):
+    with pytest.raises(gz.GfazError, match="GFA parser error: failed to open input file"):
+        gz.parse_gfa(str(tmp_path / "nope.gfa"), device=False)
