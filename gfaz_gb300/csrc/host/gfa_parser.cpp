@@ -20,6 +20,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <array>
 #include <cerrno>
 #include <chrono>
 #include <cstdlib>
@@ -658,10 +659,7 @@ void timed(Context &ctx, const char *name, double bytes, F &&launch) {
 }
 
 void scan_u32(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out) {
-  uint32_t *counter = nullptr;
-  unsigned long long *desc = ctx.lookback(excl_scan_tiles(n), &counter);
-  timed(ctx, "gfa_scan", 12.0 * n,
-        [&] { launch_excl_scan_u32(in, n, out, desc, counter, ctx.dstatus(), ctx.stream()); });
+  exclusive_scan(ctx, in, n, out, "gfa_scan");
 }
 
 struct PhaseClock {
@@ -675,6 +673,55 @@ struct PhaseClock {
     t = now;
   }
 };
+
+// Lines by type from the device line index (type[i], line ends eol), in
+// parallel: per-thread counts, then each thread fills its share.  slot of
+// a P/W line = its rank among the P and W lines.
+void line_lists(const std::vector<uint8_t> &type, const std::vector<uint64_t> &eol, uint64_t nl, uint64_t n, int nth,
+                Lines &ls, std::vector<uint64_t> &pslot, std::vector<uint64_t> &wslot) {
+  const uint64_t nlines = type.size();
+  auto kind_of = [](uint8_t t) -> int {
+    switch (t) {
+      case 'S': return 0;
+      case 'L': return 1;
+      case 'P': return 2;
+      case 'W': return 3;
+      case 'J': return 4;
+      case 'C': return 5;
+      default: return -1;
+    }
+  };
+  std::vector<Line> *lists[6] = {&ls.S, &ls.L, &ls.P, &ls.W, &ls.J, &ls.C};
+  const int T = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nth, nlines / 65536 + 1));
+  std::vector<std::array<uint64_t, 6>> cnt(T + 1);
+  for (auto &c : cnt) c.fill(0);
+#pragma omp parallel for schedule(static) num_threads(T)
+  for (int t = 0; t < T; ++t) {
+    const uint64_t a = nlines * t / T, b = nlines * (t + 1) / T;
+    for (uint64_t i = a; i < b; ++i) {
+      const int k = kind_of(type[i]);
+      if (k >= 0) cnt[t + 1][k]++;
+    }
+  }
+  for (int t = 0; t < T; ++t)
+    for (int k = 0; k < 6; ++k) cnt[t + 1][k] += cnt[t][k];
+  for (int k = 0; k < 6; ++k) lists[k]->resize(cnt[T][k]);
+  pslot.resize(cnt[T][2]);
+  wslot.resize(cnt[T][3]);
+#pragma omp parallel for schedule(static) num_threads(T)
+  for (int t = 0; t < T; ++t) {
+    const uint64_t a = nlines * t / T, b = nlines * (t + 1) / T;
+    std::array<uint64_t, 6> at = cnt[t];
+    for (uint64_t i = a; i < b; ++i) {
+      const int k = kind_of(type[i]);
+      if (k < 0) continue;
+      const uint64_t s = i ? eol[i - 1] + 1 : 0, e = i < nl ? eol[i] : n;
+      if (k == 2) pslot[at[2]] = at[2] + at[3];
+      if (k == 3) wslot[at[3]] = at[2] + at[3];
+      (*lists[k])[at[k]++] = Line{(size_t)s, (size_t)(e - s)};
+    }
+  }
+}
 
 const char *token_error(uint32_t code) {
   return code == kParseOverflow ? "parse_uint32: overflow" : "parse_uint32: no digits";
@@ -743,13 +790,13 @@ DeviceParse parse_gfa_device(Context &ctx, const std::string &path, int threads)
   timed(ctx, "gfa_field_ends", (double)n,
         [&] { launch_field_ends(text.ptr, n, nl_off.ptr, nlines, slotoff.ptr, pw.ptr, st); });
   std::vector<uint64_t> pslot, wslot;  // record slot of each P / W line
-  for (uint64_t i = 0, slot = 0; i < nlines; ++i) {
-    const uint64_t s = i ? heol[i - 1] + 1 : 0, e = i < nl ? heol[i] : n;
-    if (e == s) continue;
-    ls.add(d, s, e - s, g);
-    if (htype[i] == 'P') pslot.push_back(slot++);
-    else if (htype[i] == 'W') wslot.push_back(slot++);
-  }
+  line_lists(htype, heol, nl, n, resolve_threads(threads), ls, pslot, wslot);
+  for (uint64_t i = nlines; i-- > 0;)
+    if (htype[i] == 'H') {  // the last H line is the header
+      const uint64_t s = i ? heol[i - 1] + 1 : 0, e = i < nl ? heol[i] : n;
+      g.header_line.assign(d + s, e - s);
+      break;
+    }
   std::vector<uint8_t>().swap(htype);
   std::vector<uint64_t>().swap(heol);
   clk.mark("line index");

@@ -230,11 +230,9 @@ StaticFields decode_static(const Compressed &d) {
   return s;
 }
 
-// H, S, L, J, C text (src/io/gfa_writer.cpp:597-700)
-std::string static_text(const Compressed &d, const StaticFields &s) {
-  std::string out;
-  if (!d.header_line.empty()) out += d.header_line + "\n";
-  const FieldOffsets so = field_offsets(s.seg_opt), lo = field_offsets(s.link_opt);
+// S lines (host formatting).
+void s_text_host(const StaticFields &s, std::string &out) {
+  const FieldOffsets so = field_offsets(s.seg_opt);
   std::string line;
   size_t sp = 0;
   for (size_t i = 0; i < s.seg_len.size(); ++i) {
@@ -250,6 +248,12 @@ std::string static_text(const Compressed &d, const StaticFields &s) {
     line += '\n';
     out += line;
   }
+}
+
+// L lines (host formatting).
+void l_text_host(const StaticFields &s, std::string &out) {
+  const FieldOffsets lo = field_offsets(s.link_opt);
+  std::string line;
   for (size_t i = 0; i < s.lf.size(); ++i) {
     line = "L\t";
     line += std::to_string(s.lf[i]);
@@ -270,6 +274,11 @@ std::string static_text(const Compressed &d, const StaticFields &s) {
     line += '\n';
     out += line;
   }
+}
+
+// J and C lines.
+void jc_text(const StaticFields &s, std::string &out) {
+  std::string line;
   for (size_t i = 0; i < s.jf.size(); ++i) {
     line = "J\t" + std::to_string(s.jf[i]) + "\t" + s.jfo[i] + "\t" + std::to_string(s.jt[i]) + "\t" + s.jto[i] + "\t";
     line += i < s.jdist.size() ? s.jdist[i] : "*";
@@ -285,6 +294,143 @@ std::string static_text(const Compressed &d, const StaticFields &s) {
     line += '\n';
     out += line;
   }
+}
+
+// H, S, L, J, C text on the host (src/io/gfa_writer.cpp:597-700)
+std::string static_text(const Compressed &d, const StaticFields &s) {
+  std::string out;
+  if (!d.header_line.empty()) out += d.header_line + "\n";
+  s_text_host(s, out);
+  l_text_host(s, out);
+  jc_text(s, out);
+  return out;
+}
+
+// The optional-field text of lines 0 .. n-1 (what append_opt_fields adds),
+// formatted in parallel: blob[off[i] .. off[i+1]).  Empty when there is no
+// column.
+void opt_extras(const std::vector<OptColumn> &cols, size_t n, int nth, std::string &blob,
+                std::vector<uint64_t> &off) {
+  blob.clear();
+  off.clear();
+  if (cols.empty() || !n) return;
+  const FieldOffsets fo = field_offsets(cols);
+  const int T = std::max(1, std::min<int>(nth, (int)(n / 4096 + 1)));
+  std::vector<std::string> part(T);
+  off.assign(n + 1, 0);
+#pragma omp parallel for schedule(static) num_threads(T)
+  for (int t = 0; t < T; ++t) {
+    const size_t a = n * t / T, b = n * (t + 1) / T;
+    for (size_t i = a; i < b; ++i) {
+      append_opt_fields(part[t], cols, fo, i);
+      off[i + 1] = part[t].size();  // relative to the part, fixed below
+    }
+  }
+  uint64_t base = 0;
+  for (int t = 0; t < T; ++t) {
+    const size_t a = n * t / T, b = n * (t + 1) / T;
+    for (size_t i = a; i < b; ++i) off[i + 1] += base;
+    base += part[t].size();
+    blob += part[t];
+    std::string().swap(part[t]);
+  }
+}
+
+template <typename T>
+void upload_vec(Context &ctx, DevVec<T> &d, const T *p, uint64_t n) {
+  d.resize(std::max<uint64_t>(n, 1));
+  if (n) cuda_check(cudaMemcpyAsync(d.ptr, p, n * sizeof(T), cudaMemcpyHostToDevice, ctx.stream()), "upload");
+}
+
+// Lines of one kind written on the device and appended to out.
+void static_lines_device(Context &ctx, StaticTextSource src, const std::string &ex, const std::vector<uint64_t> &exo,
+                         std::string &out) {
+  if (!src.n) return;
+  cudaStream_t st = ctx.stream();
+  DevVec<char> dex(st);
+  DevVec<uint64_t> dexo(st), len(st), loff(st);
+  if (!exo.empty()) {
+    upload_vec(ctx, dex, ex.data(), ex.size());
+    upload_vec(ctx, dexo, exo.data(), exo.size());
+    src.ex = dex.ptr;
+    src.ex_off = dexo.ptr;
+  }
+  len.resize(src.n);
+  loff.resize(src.n + 1);
+  ctx.tbegin("static_text", 0);
+  launch_static_len(src, len.ptr, st);
+  ctx.tend();
+  exclusive_scan(ctx, len.ptr, src.n, loff.ptr, "static_text");
+  uint64_t total = 0;
+  cuda_check(cudaMemcpyAsync(&total, loff.ptr + src.n, 8, cudaMemcpyDeviceToHost, st), "download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  DevVec<char> text(st);
+  text.resize((total + 15) & ~15ull);
+  ctx.tbegin("static_text", (double)total);
+  launch_static_write(src, loff.ptr, total, text.ptr, st);
+  ctx.tend();
+  const size_t o = out.size();
+  out.resize(o + total);
+  cuda_check(cudaMemcpyAsync(&out[o], text.ptr, total, cudaMemcpyDeviceToHost, st), "text download");
+  cuda_check(cudaStreamSynchronize(st), "stream sync");
+}
+
+// H, S, L, J, C text with the S and L lines written on the device.
+std::string static_text_device(Context &ctx, const Compressed &d, const StaticFields &s, int nth) {
+  std::string out;
+  if (!d.header_line.empty()) out += d.header_line + "\n";
+  cudaStream_t st = ctx.stream();
+  std::string ex;
+  std::vector<uint64_t> exo;
+  {
+    const uint64_t ns = s.seg_len.size();
+    uint64_t need = 0;
+    for (uint64_t i = 0; i < ns; ++i) need += s.seg_len[i];
+    if (need > s.seg_seq.size())
+      throw std::runtime_error(std::string(kWriterErr) + "segment sequence column is truncated");
+    DevVec<char> seq(st);
+    DevVec<uint32_t> slen(st);
+    DevVec<uint64_t> soff(st);
+    upload_vec(ctx, seq, s.seg_seq.data(), need);
+    upload_vec(ctx, slen, s.seg_len.data(), ns);
+    soff.resize(ns + 1);
+    exclusive_scan(ctx, slen.ptr, ns, soff.ptr, "static_text");
+    opt_extras(s.seg_opt, ns, nth, ex, exo);
+    StaticTextSource src{};
+    src.kind = 0;
+    src.n = ns;
+    src.seq = seq.ptr;
+    src.seq_off = soff.ptr;
+    src.seg_len = slen.ptr;
+    static_lines_device(ctx, src, ex, exo, out);
+  }
+  {
+    const uint64_t nl = s.lf.size();
+    std::vector<uint32_t> lnum(s.lnum);
+    std::vector<char> lop(s.lop);
+    lnum.resize(nl, 0);
+    lop.resize(nl, '\0');
+    DevVec<uint32_t> lf(st), lt(st), num(st);
+    DevVec<char> lfo(st), lto(st), op(st);
+    upload_vec(ctx, lf, s.lf.data(), nl);
+    upload_vec(ctx, lt, s.lt.data(), nl);
+    upload_vec(ctx, num, lnum.data(), nl);
+    upload_vec(ctx, lfo, s.lfo.data(), nl);
+    upload_vec(ctx, lto, s.lto.data(), nl);
+    upload_vec(ctx, op, lop.data(), nl);
+    opt_extras(s.link_opt, nl, nth, ex, exo);
+    StaticTextSource src{};
+    src.kind = 1;
+    src.n = nl;
+    src.lf = lf.ptr;
+    src.lt = lt.ptr;
+    src.lnum = num.ptr;
+    src.lfo = lfo.ptr;
+    src.lto = lto.ptr;
+    src.lop = op.ptr;
+    static_lines_device(ctx, src, ex, exo, out);
+  }
+  jc_text(s, out);
   return out;
 }
 
@@ -615,7 +761,7 @@ void download_text(Context &ctx, const DevVec<char> &text, uint64_t n, std::stri
 std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
   set_zstd_threads(resolve_threads(threads));
   const StaticFields s = decode_static(c);
-  std::string out = static_text(c, s);
+  std::string out = ctx.static_text ? static_text_device(ctx, c, s, resolve_threads(threads)) : static_text(c, s);
   Grammar g(ctx.stream());
   const LoadedStreams ls = load_all(ctx, c, g, kWriterErr);
   DevVec<char> text(ctx.stream());

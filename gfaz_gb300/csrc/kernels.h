@@ -310,6 +310,30 @@ struct NameIndex {
 constexpr uint32_t kParseNoDigits = 1;  // parse_uint32: no digits
 constexpr uint32_t kParseOverflow = 2;  // parse_uint32: overflow
 
+// ---------------------------------------------------------------------------
+// S and L line text (static_kernels.cu)
+// ---------------------------------------------------------------------------
+struct StaticTextSource {
+  int kind;  // 0 = S lines, 1 = L lines
+  uint64_t n;
+  // S: sequences back to back; seq_off = exclusive scan of seg_len
+  const char *seq;
+  const uint64_t *seq_off;
+  const uint32_t *seg_len;
+  // L: from / to ids and orientations, overlap number and operation (0: '*')
+  const uint32_t *lf, *lt, *lnum;
+  const char *lfo, *lto, *lop;
+  // per-line optional-field text ex[ex_off[i] .. ex_off[i+1]) or none (null)
+  const char *ex;
+  const uint64_t *ex_off;
+};
+// len[i] = the byte length of line i.
+void launch_static_len(const StaticTextSource &S, uint64_t *len, cudaStream_t st);
+// The lines at out[loff[i] ..] (loff: exclusive scan of len, total bytes;
+// out 16-byte aligned).
+void launch_static_write(const StaticTextSource &S, const uint64_t *loff, uint64_t total, char *out,
+                         cudaStream_t st);
+
 uint64_t parse_num_tiles(uint64_t n);
 // cnt[tile] = '\n' bytes in the tile.
 void launch_nl_count(const char *text, uint64_t n, uint32_t *cnt, cudaStream_t st);

@@ -879,6 +879,18 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   cuda_check(cudaStreamSynchronize(st), "stream sync");
 }
 
+void exclusive_scan(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out, const char *timer) {
+  uint32_t *counter = nullptr;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(n), &counter);
+  GFZ_TIMED_B(ctx, timer, 12.0 * n, launch_excl_scan_u32(in, n, out, desc, counter, ctx.dstatus(), ctx.stream()));
+}
+
+void exclusive_scan(Context &ctx, const uint64_t *in, uint64_t n, uint64_t *out, const char *timer) {
+  uint32_t *counter = nullptr;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(n), &counter);
+  GFZ_TIMED_B(ctx, timer, 16.0 * n, launch_excl_scan_u64(in, n, out, desc, counter, ctx.dstatus(), ctx.stream()));
+}
+
 bool resident_fits(const Context &ctx, uint64_t n) {
   if (ctx.encode_chunk) return false;
   // input, two stream buffers, per-tile words, a pair table

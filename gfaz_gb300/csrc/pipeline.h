@@ -133,6 +133,7 @@ class Context {
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
+  int static_text = 1;           // S/L text of the full-file writer: 1 = device, 0 = host
   // Tuner: (kernel, stream class) -> the variant that was faster the first
   // time the class came up (see encode_traversals).  With GFAZ_TUNE_FILE
   // set, decisions are loaded from that file when the context is made and
@@ -222,6 +223,11 @@ struct HostSeg {
 // budget (rounds shrink the stream).
 void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
                          const EncodeParams &p, uint64_t chunk, uint64_t budget, Grammar &g);
+
+// out[0 .. n] = exclusive scan of in[0 .. n) (out[n] = the total) on ctx's
+// stream; the launch is timed under `timer`.
+void exclusive_scan(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out, const char *timer);
+void exclusive_scan(Context &ctx, const uint64_t *in, uint64_t n, uint64_t *out, const char *timer);
 
 // Whether compression of n steps runs resident in HBM under ctx's budget
 // and chunk options (working set about 12.5 bytes per step).

@@ -91,7 +91,9 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * "front_end" = the GFA parse of file compression: 1 (default) = the
  * device front end (line index and P/W steps on the GPU), 0 = the host
  * parser; both give the same graph, and the host parser also runs when the
- * file does not fit "hbm_budget" three times over. */
+ * file does not fit "hbm_budget" three times over; "static_text" = the S and
+ * L lines of the full-file writer: 1 (default) = written on the device,
+ * 0 = on the host; the same bytes. */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
