@@ -286,8 +286,12 @@ __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict
   __syncthreads();
   InsertCounts c;
   const uint32_t mask = (uint32_t)(tab.cap - 1);
+  uint32_t it = 0;
   for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p + 1 < n;
        p += (uint64_t)gridDim.x * blockDim.x) {
+    // a full table (some chain ran past the probe limit) ends every thread
+    // within 16 of its pairs
+    if ((++it & 15u) == 0 && (*(volatile uint32_t *)&status->err & kErrTableFull)) break;
     const uint64_t q = p + 1;
     if ((heads[q >> 5] >> (q & 31)) & 1u) continue;  // q opens a traversal
     const unsigned long long key = canon2(pack2(s[p], s[q]));
@@ -330,8 +334,10 @@ __global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restric
   const uint32_t mask = (uint32_t)(tab.cap - 1);
   const bool aligned = (reinterpret_cast<uintptr_t>(s) & 15u) == 0;
   bool full = false;
+  uint32_t it = 0;
   for (uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * K; p0 + 1 < n && !full;
        p0 += (uint64_t)gridDim.x * blockDim.x * K) {
+    if ((++it & 3u) == 0 && (*(volatile uint32_t *)&status->err & kErrTableFull)) break;  // as in k_count_flat
     int32_t v[K + 1];
     if (aligned && p0 + K < n) {
       const int4 a = *reinterpret_cast<const int4 *>(s + p0);

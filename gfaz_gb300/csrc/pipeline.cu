@@ -406,7 +406,8 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
     est = std::min(est, n);
     uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
-    if (round == 0 && ctx.first_table_cap) cap = ctx.first_table_cap;
+    const bool forced_cap = round == 0 && ctx.first_table_cap;
+    if (forced_cap) cap = ctx.first_table_cap;
     uint64_t distinct = 0, repeated = 0;
     heads.resize(head_words(n));
     cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(n) * sizeof(uint32_t), st), "head bitmap clear");
@@ -418,6 +419,17 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     const int cls = (round == 0 ? 0 : 1) * 1000 + 4 * (int)ceil_log2(n) +
                     (round == 0 ? 0 : (int)std::min<uint64_t>(3, prev_distinct * 4 / std::max<uint64_t>(n, 1)));
     CountKernel kind = ctx.warp_dedup ? CountKernel::kTiledWarpDedup : CountKernel::kTiled;
+    // table size: the estimate's size shrunk by the factor the load-factor
+    // tuner kept for this class and round (tuned below, once the distinct
+    // pairs are known)
+    const int cap_cls = cls * 16 + std::min(round, 15);
+    const uint64_t cap_default = cap;
+    bool tune_cap = false;
+    if (ctx.table_tuner && !forced_cap) {
+      const auto it = ctx.tuned.find({Context::kTuneCap, cap_cls});
+      if (it != ctx.tuned.end()) cap = std::max<uint64_t>(cap >> it->second, 1u << 16);
+      else tune_cap = true;
+    }
     bool tune = false;
     if (ctx.count_kernel >= 0) {
       kind = (CountKernel)ctx.count_kernel;
@@ -472,6 +484,47 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       }
       ctx.check_status("count_pairs");
       break;
+    }
+    if (tune_cap) {
+      // hash load factor: the count (with its table clear) timed with the
+      // estimate's table and with 2, 4 and 8 times smaller ones that keep
+      // the load at 1/2 or below for the distinct pairs just counted; the
+      // fastest shrink factor is kept for the class and round
+      std::vector<uint64_t> caps = {cap};
+      for (int sh = 1; sh <= 3; ++sh) {
+        const uint64_t c = cap_default >> sh;
+        if (c >= 2 * distinct && c >= (1u << 16) && c < cap) caps.push_back(c);
+      }
+      uint64_t best = cap, last = cap;
+      float tbest = -1;
+      for (const uint64_t c : caps) {
+        ctx.reset_status();
+        const float t = ctx.time_launches([&] {
+          tab.prepare(c, st);
+          launch_count_pairs(A.ptr, n, heads.ptr, tab.view(c), ds, kind, st);
+        });
+        last = c;
+        // a probe chain past its limit at this load: not a candidate (the
+        // next reset clears the bit)
+        if (ctx.read_status().err & kErrTableFull) continue;
+        if (tbest < 0 || t < tbest) {
+          tbest = t;
+          best = c;
+        }
+      }
+      if (debug_enabled())
+        fprintf(stderr, "[gfaz gb300] load-factor tuner: class %d distinct=%llu table %llu -> %llu slots\n", cls,
+                (unsigned long long)distinct, (unsigned long long)cap, (unsigned long long)best);
+      ctx.record_tuned(Context::kTuneCap, cap_cls, (int)(ceil_log2(cap_default) - ceil_log2(best)));
+      cap = best;
+      ctx.reset_status();
+      if (last != best) {
+        tab.prepare(cap, st);
+        GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
+                    launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
+        ctx.read_status();
+        ctx.check_status("count_pairs");
+      }
     }
     prev_distinct = distinct;
     if (repeated == 0) break;  // no candidates: stop all rounds

@@ -139,7 +139,10 @@ class Context {
   // set, decisions are loaded from that file when the context is made and
   // appended to it when taken, so later processes (a profiler's replay of
   // the same command) run the same variants.
-  enum TunedKernel { kTuneCount = 0, kTuneClassify = 1 };
+  // kTuneCap: the pair table's shrink factor (log2) against the size the
+  // distinct-pair estimate gives, per class and round
+  enum TunedKernel { kTuneCount = 0, kTuneClassify = 1, kTuneCap = 2 };
+  bool table_tuner = true;  // pair-table size (hash load factor) tuned per stream class
   std::map<std::pair<int, int>, int> tuned;
   void record_tuned(int kernel, int cls, int variant);
   // Launches on this context's stream and returns their device time (ms).

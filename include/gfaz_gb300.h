@@ -93,7 +93,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * parser; both give the same graph, and the host parser also runs when the
  * file does not fit "hbm_budget" three times over; "static_text" = the S and
  * L lines of the full-file writer: 1 (default) = written on the device,
- * 0 = on the host; the same bytes. */
+ * 0 = on the host; the same bytes; "table_tuner" = 1 (default): the pair
+ * table's size (hash load factor) is tuned per stream class (the count
+ * timed with tables for load <= 3/4, 1/2, 1/4 and at the estimate's size,
+ * the fastest kept), 0 = sized from the estimate alone; results are the
+ * same either way. */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */

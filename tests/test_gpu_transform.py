@@ -156,13 +156,15 @@ def test_load_grammar_decodes_oracle_output(gpu_ctx):
 
 def test_count_kernels_give_same_result(gpu_ctx):
     """Every pair-count kernel (the tuner's pick, tiled, tiled with warp
-    folding, flat), both classification kernels and the warp folding switch
-    give the same grammar."""
+    folding, flat), both classification kernels, the warp folding switch
+    and the table size (load-factor tuner on and off, a forced first-round
+    size too small for the pairs) give the same grammar."""
     steps, off, _ = synthetic.cfg2_stream(seed=4, n_segments=80_000, n_paths=6)
     a = gz.encode(steps, off, ctx=gpu_ctx).arrays()
     for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("count_kernel", 3),
                      ("warp_dedup", 1),
-                     ("classify_kernel", 0), ("classify_kernel", 1)]:
+                     ("classify_kernel", 0), ("classify_kernel", 1),
+                     ("table_tuner", 0), ("first_table_cap", 1 << 16)]:
         ctx2 = gz.Context(0)
         ctx2.set_option(opt, val)
         b = gz.encode(steps, off, ctx=ctx2).arrays()
@@ -210,9 +212,11 @@ def test_tuner_decisions_file(tmp_path, monkeypatch, gpu_ctx):
     steps, off, _ = synthetic.cfg2_stream(seed=9, n_segments=40_000, n_paths=4)
     a = gz.encode(steps, off, ctx=gz.Context(0)).arrays()
     rows = [tuple(int(x) for x in line.split()) for line in f.read_text().splitlines()]
-    assert rows and all(len(r) == 3 and r[0] in (0, 1) for r in rows)
-    # force the other classification variant for every recorded class
-    f.write_text("".join("%d %d %d\n" % (k, c, (1 - v) if k == 1 else v) for k, c, v in rows))
+    assert rows and all(len(r) == 3 and r[0] in (0, 1, 2) for r in rows)
+    assert any(r[0] == 2 for r in rows)  # table shrink factors from the load-factor tuner
+    # force the other classification variant and tables four times smaller
+    # (some then refill) for every recorded class
+    f.write_text("".join("%d %d %d\n" % (k, c, (1 - v) if k == 1 else v + 2 if k == 2 else v) for k, c, v in rows))
     b = gz.encode(steps, off, ctx=gz.Context(0)).arrays()
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
