@@ -506,6 +506,50 @@ def parse_gfa(file_path, threads: int = DEFAULT_NUM_THREADS, ctx: Optional[Conte
 parse = parse_gfa
 
 
+@dataclass
+class GrowthResult:
+    """include/workflows/growth_workflow.hpp:27-32: hist[c] = nodes covered by
+    exactly c of the N haplotype groups; growth[k] = expected nodes covered
+    by a random k-subset (growth[0] unused)."""
+
+    num_haplotypes: int = 0
+    num_nodes: int = 0
+    hist: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint64))
+    growth: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+
+
+_GROUP_BY = {"path": 0, "per-line": 0, "sample-hap-seq": 1, "panacus": 1, "sample-hap": 2, "haplotype": 2,
+             "sample": 3}
+
+
+def compute_growth(data: CompressedData, num_threads: int = DEFAULT_NUM_THREADS, group_by: str = "path",
+                   ctx: Optional[Context] = None) -> GrowthResult:
+    """compute_growth (src/workflows/growth_workflow.cpp:261; `gfaz growth`):
+    the pangenome growth curve, node coverage computed on the GPU.  group_by
+    takes the CLI's --group-by values."""
+    if group_by not in _GROUP_BY:
+        raise ValueError("unknown group_by %r; expected one of %s" % (group_by, sorted(_GROUP_BY)))
+    nh, nn = ctypes.c_uint32(), ctypes.c_uint32()
+    hp, gp = ctypes.c_void_p(), ctypes.c_void_p()
+    L = lib()
+    check(L.gfz_growth(_ctx(ctx), data.handle, int(num_threads), _GROUP_BY[group_by], ctypes.byref(nh),
+                       ctypes.byref(nn), ctypes.byref(hp), ctypes.byref(gp)))
+    r = GrowthResult(nh.value, nn.value)
+    if nh.value:
+        r.hist = np.frombuffer(take_bytes(hp, 8 * (nh.value + 1)), np.uint64).copy()
+        r.growth = np.frombuffer(take_bytes(gp, 8 * (nh.value + 1)), np.float64).copy()
+    return r
+
+
+def growth_text(result: GrowthResult, group_by: str = "path") -> str:
+    """The `gfaz growth` table (src/cli/growth_command.cpp:74-97)."""
+    label = {0: "path", 1: "sample-hap-seq", 2: "sample-hap", 3: "sample"}[_GROUP_BY[group_by]]
+    out = ["# gfaz growth (count=node, coverage>=1, quorum>=0)\n# group-by=%s\n" % label,
+           "# num_haplotypes=%d num_nodes=%d\nk\tgrowth\n" % (result.num_haplotypes, result.num_nodes)]
+    out += ["%d\t%.4f\n" % (k, result.growth[k]) for k in range(1, result.num_haplotypes + 1)]
+    return "".join(out)
+
+
 def decompress_data(data: CompressedData, threads: int = DEFAULT_NUM_THREADS,
                     ctx: Optional[Context] = None) -> GfaGraph:
     L = lib()

@@ -398,6 +398,23 @@ gfz_status gfz_parse_gfa(gfz_context *ctx, const char *path, int threads, int de
   });
 }
 
+gfz_status gfz_growth(gfz_context *ctx, const gfz_compressed *c, int threads, int group_by, uint32_t *num_haplotypes,
+                      uint32_t *num_nodes, uint64_t **hist, double **growth) {
+  return guard([&] {
+    require(c && num_haplotypes && num_nodes && hist && growth, "NULL argument");
+    require(group_by >= 0 && group_by <= 3, "group_by must be 0 (path), 1 (sample-hap-seq), 2 (sample-hap) or 3 (sample)");
+    const gfz::GrowthResult r = gfz::compute_growth(ctx_of(ctx), c->c, threads, (gfz::GroupMode)group_by);
+    *num_haplotypes = r.num_haplotypes;
+    *num_nodes = r.num_nodes;
+    *hist = nullptr;
+    *growth = nullptr;
+    if (r.num_haplotypes) {
+      *hist = reinterpret_cast<uint64_t *>(dup_bytes(r.hist.data(), r.hist.size() * 8));
+      *growth = reinterpret_cast<double *>(dup_bytes(r.growth.data(), r.growth.size() * 8));
+    }
+  });
+}
+
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out) {
   return guard([&] {
     require(c && out, "NULL argument");

@@ -4,7 +4,7 @@
 // Commands, options, default output names and error behaviour follow the
 // reference CLI (src/cli/gfaz_cli.cpp, compress_command.cpp,
 // decompress_command.cpp, extract_path_command.cpp, extract_walk_command.cpp,
-// add_haplotypes_command.cpp): "Error: <message>" on stderr and exit code 1
+// add_haplotypes_command.cpp, growth_command.cpp): "Error: <message>" on stderr and exit code 1
 // on failure, extracted lines on stdout.  The transform always runs on the
 // GPU; --gpu is accepted for compatibility.
 #include <getopt.h>
@@ -35,7 +35,8 @@ void usage() {
                "    gfaz extract-path [OPTIONS] <input.gfaz> <path_name> [path_name ...]\n"
                "    gfaz extract-walk [OPTIONS] <input.gfaz>\n"
                "                      <sample_id> <hap_index> <seq_id> <seq_start> <seq_end> [...]\n"
-               "    gfaz add-haplotypes [OPTIONS] <input.gfaz> <paths_or_walks.gfa> [output.gfaz]\n\n"
+               "    gfaz add-haplotypes [OPTIONS] <input.gfaz> <paths_or_walks.gfa> [output.gfaz]\n"
+               "    gfaz growth [-j N] [-G path|sample-hap-seq|sample-hap|sample] <input.gfaz>\n\n"
                "compress options: -r/--rounds N (8)  -d/--delta N (1)  -t/--threshold N (2)\n"
                "                  -j/--threads N (0 = auto)  -g/--gpu  -s/--stats\n"
                "other commands:   -j/--threads N\n";
@@ -221,6 +222,58 @@ int do_add_haplotypes(int argc, char **argv) {
   return 0;
 }
 
+// src/cli/growth_command.cpp: the growth table on stdout.
+int do_growth(int argc, char **argv) {
+  int threads = 0, group = 0;
+  const char *label = "path";
+  static struct option lo[] = {{"threads", required_argument, 0, 'j'},
+                               {"group-by", required_argument, 0, 'G'},
+                               {"help", no_argument, 0, 'h'},
+                               {0, 0, 0, 0}};
+  int opt;
+  optind = 1;
+  while ((opt = getopt_long(argc, argv, "j:G:h", lo, nullptr)) != -1) {
+    if (opt == 'j') {
+      threads = std::atoi(optarg);
+    } else if (opt == 'G') {
+      const std::string v = optarg;
+      if (v == "path" || v == "per-line") group = 0, label = "path";
+      else if (v == "sample-hap-seq" || v == "panacus") group = 1, label = "sample-hap-seq";
+      else if (v == "sample-hap" || v == "haplotype") group = 2, label = "sample-hap";
+      else if (v == "sample") group = 3, label = "sample";
+      else {
+        std::cerr << "Error: unknown --group-by value '" << v
+                  << "'. Expected 'path', 'sample-hap-seq', 'sample-hap', or 'sample'.\n";
+        return 1;
+      }
+    } else if (opt == 'h') {
+      std::cout << "gfaz growth [-j N] [-G path|sample-hap-seq|sample-hap|sample] <input.gfaz>\n";
+      return 0;
+    } else {
+      return 1;
+    }
+  }
+  if (optind >= argc) {
+    std::cerr << "Error: Expected <input.gfaz>\n";
+    return 1;
+  }
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(argv[optind], &c) != GFZ_OK) return fail();
+  uint32_t nh = 0, nn = 0;
+  uint64_t *hist = nullptr;
+  double *growth = nullptr;
+  const gfz_status st = gfz_growth(nullptr, c, threads, group, &nh, &nn, &hist, &growth);
+  gfz_compressed_free(c);
+  if (st != GFZ_OK) return fail();
+  std::cout << "# gfaz growth (count=node, coverage>=1, quorum>=0)\n# group-by=" << label
+            << "\n# num_haplotypes=" << nh << " num_nodes=" << nn << "\nk\tgrowth\n";
+  std::fflush(stdout);
+  for (uint32_t k = 1; k <= nh; ++k) std::printf("%u\t%.4f\n", k, growth[k]);
+  gfz_free(hist);
+  gfz_free(growth);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -234,6 +287,7 @@ int main(int argc, char **argv) {
   if (cmd == "extract-path") return do_extract_path(argc - 1, argv + 1);
   if (cmd == "extract-walk") return do_extract_walk(argc - 1, argv + 1);
   if (cmd == "add-haplotypes") return do_add_haplotypes(argc - 1, argv + 1);
+  if (cmd == "growth") return do_growth(argc - 1, argv + 1);
   if (cmd == "-h" || cmd == "--help" || cmd == "help") {
     usage();
     return 0;

@@ -63,6 +63,24 @@ std::vector<std::string> extract_walk_lines(Context &ctx, const Compressed &c, c
 std::vector<std::string> extract_walk_lines_by_name(Context &ctx, const Compressed &c,
                                                     const std::vector<std::string> &names, int threads);
 
+// Pangenome growth, include/workflows/growth_workflow.hpp:21-41: how P/W
+// lines map to haplotypes (each line; PanSN sample#hap#seq with ":start-end"
+// cleared; sample#hap; sample), the coverage histogram hist[c] (nodes
+// covered by exactly c of the N groups, c = 0 .. N) and growth[k] (expected
+// nodes covered by a random k-subset, k = 1 .. N; growth[0] unused).
+enum class GroupMode { kPerPathWalk = 0, kSampleHapSeq = 1, kSampleHap = 2, kSample = 3 };
+struct GrowthResult {
+  uint32_t num_haplotypes = 0, num_nodes = 0;
+  std::vector<uint64_t> hist;
+  std::vector<double> growth;
+};
+// src/workflows/growth_workflow.cpp:261 compute_growth (coverage on the GPU)
+GrowthResult compute_growth(Context &ctx, const Compressed &c, int threads, GroupMode mode);
+// The group of every traversal (paths, then walks), first-seen order.
+std::vector<uint32_t> growth_groups(const Compressed &c, GroupMode mode, uint32_t &ngroups);
+// growth[k] from the coverage histogram (growth_workflow.cpp:106-118, 480-500).
+std::vector<double> growth_curve(const std::vector<uint64_t> &hist, uint32_t N, int threads);
+
 // src/workflows/add_haplotypes_workflow.cpp:579 add_haplotypes
 void add_haplotypes(Context &ctx, Compressed &c, const std::string &path, int threads);
 // Parsed add-haplotypes input: P-lines or W-lines (never both), with the

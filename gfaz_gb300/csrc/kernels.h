@@ -334,6 +334,21 @@ void launch_static_len(const StaticTextSource &S, uint64_t *len, cudaStream_t st
 void launch_static_write(const StaticTextSource &S, const uint64_t *loff, uint64_t total, char *out,
                          cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Pangenome growth (growth_kernels.cu)
+// ---------------------------------------------------------------------------
+// Bit (g & 63) of word (g >> 6) - w0 of node |x[p]|'s row (rows of w1 - w0
+// words, node ids 1 .. num_nodes; others skipped) for every step p of a
+// traversal t whose group g = gid[t] has g >> 6 in [w0, w1).
+void launch_cover_bits(const int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav, const uint32_t *gid,
+                       uint64_t num_nodes, uint32_t w0, uint32_t w1, unsigned long long *bits, cudaStream_t st);
+// cov[v] += bits set in row v (stride words), v = 1 .. num_nodes.
+void launch_cover_count(const unsigned long long *bits, uint64_t num_nodes, uint32_t stride, uint32_t *cov,
+                        cudaStream_t st);
+// hist[c] += nodes v = 1 .. num_nodes with cov[v] == c, c <= nh (zeroed first).
+void launch_cover_hist(const uint32_t *cov, uint64_t num_nodes, uint32_t nh, unsigned long long *hist,
+                       cudaStream_t st);
+
 uint64_t parse_num_tiles(uint64_t n);
 // cnt[tile] = '\n' bytes in the tile.
 void launch_nl_count(const char *text, uint64_t n, uint32_t *cnt, cudaStream_t st);

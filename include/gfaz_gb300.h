@@ -143,6 +143,14 @@ gfz_status gfz_add_haplotypes(gfz_context *ctx, gfz_compressed *c, const char *p
  * (ctx unused; no GPU needed).  Parse errors are "GFA parser error: ..." or
  * the value parser's own message, as in the reference. */
 gfz_status gfz_parse_gfa(gfz_context *ctx, const char *path, int threads, int device, gfz_graph **out);
+/* compute_growth, include/workflows/growth_workflow.hpp:36-41 (`gfaz growth`,
+ * src/cli/growth_command.cpp): group_by 0 = every P/W line ("path"), 1 =
+ * PanSN sample#hap#seq ("sample-hap-seq"), 2 = sample#hap ("sample-hap"),
+ * 3 = sample.  *hist gets num_haplotypes + 1 counts (nodes covered by
+ * exactly c groups) and *growth num_haplotypes + 1 values (growth[0] = 0),
+ * both released with gfz_free (NULL when num_haplotypes is 0). */
+gfz_status gfz_growth(gfz_context *ctx, const gfz_compressed *c, int threads, int group_by, uint32_t *num_haplotypes,
+                      uint32_t *num_nodes, uint64_t **hist, double **growth);
 /* decompress_gfa, include/workflows/decompression_workflow.hpp:8-9 */
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out);
 void gfz_graph_free(gfz_graph *g);
