@@ -16,7 +16,7 @@ from typing import List, Optional, Sequence
 
 import numpy as np
 
-from ._ffi import (GfazError, LineMeta, ContainerInfo, GrammarInfo, WalkKeyC, check, lib, take_bytes,
+from ._ffi import (GfazError, LineMeta, ContainerInfo, GrammarInfo, WalkKeyC, check, copy_bytes, lib, take_bytes,
                    WHERE_HOST, WHERE_DEVICE, P_LINES, W_LINES)
 
 DEFAULT_ROUNDS = 8
@@ -403,7 +403,7 @@ class Server:
         p, n, ms = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
         check(lib().gfz_server_wait(self._h, int(ticket), ctypes.byref(p), ctypes.byref(n), ctypes.byref(ms)))
         try:
-            line = ctypes.string_at(p, n.value) if n.value else b""
+            line = copy_bytes(p, n.value)
         finally:
             check(lib().gfz_server_release(self._h, int(ticket)))
         return (line if as_bytes else line.decode()), ms.value

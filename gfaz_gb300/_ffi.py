@@ -145,10 +145,25 @@ def check(status: int):
         raise GfazError(status, msg)
 
 
+COPY_PIECE = 1 << 30
+
+
+def copy_bytes(ptr, n: int) -> bytes:
+    """n bytes at ptr.  ctypes.string_at takes its size as a C int, so 2 GiB
+    and more are copied in pieces of COPY_PIECE bytes."""
+    if not n:
+        return b""
+    addr = ptr.value if isinstance(ptr, ctypes.c_void_p) else int(ptr)
+    piece = COPY_PIECE
+    if n <= piece:
+        return ctypes.string_at(addr, n)
+    return b"".join(ctypes.string_at(addr + o, min(piece, n - o)) for o in range(0, n, piece))
+
+
 def take_bytes(ptr: ctypes.c_void_p, n: int) -> bytes:
     """Copies a library-allocated buffer and frees it."""
     try:
-        return ctypes.string_at(ptr, n) if n else b""
+        return copy_bytes(ptr, n)
     finally:
         if ptr:
             lib().gfz_free(ptr)

@@ -87,3 +87,16 @@ def test_gpu_entry_points_fail_loudly_without_gpu(tmp_path):
     assert e.value.status_name == "CUDA"
     with pytest.raises(gz.GfazError):
         gz.Context(0)
+
+
+def test_copy_bytes_in_pieces(monkeypatch):
+    """Library buffers of 2 GiB and more are copied in pieces (ctypes.string_at
+    takes a C int size); the pieces join to the same bytes."""
+    import ctypes
+    from gfaz_gb300 import _ffi
+    data = bytes(range(256)) * 37
+    buf = ctypes.create_string_buffer(data, len(data))
+    monkeypatch.setattr(_ffi, "COPY_PIECE", 1000)
+    assert _ffi.copy_bytes(ctypes.addressof(buf), len(data)) == data
+    assert _ffi.copy_bytes(ctypes.c_void_p(ctypes.addressof(buf)), 5) == data[:5]
+    assert _ffi.copy_bytes(None, 0) == b""
