@@ -304,11 +304,86 @@ __global__ void __launch_bounds__(kPB) k_field_ends(const char *__restrict__ tex
   }
 }
 
+// Numeric names, whole window inside one steps / walk field: a straight-
+// line lexer over the thread's 16 bytes and the 16 that follow (no
+// per-token loops, so the warp does not diverge).  Tokens that start in
+// the first 16 bytes and end inside the 32 get their id at the position
+// of the byte that ends them (id[j], bit j of *mask); a token still open
+// at byte 31 is left for parse_token (*longk = its first byte, else -1).
+// The name of a P token excludes its last byte (the orientation), so the
+// digit state is also kept as it was before the last digit.
+template <bool P>
+__device__ __forceinline__ void lex_window(const uint4 &a, const uint4 &b, bool start0, uint64_t p0,
+                                           unsigned long long *err, int32_t (&id)[32], uint32_t &mask, int &longk) {
+  bool active = false, any = false, pany = false, stopped = false, lastacc = false, rev = false;
+  uint64_t v = 0, pv = 0;
+  int ts = 0;
+  uint32_t prevc = 0;
+  mask = 0;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const uint32_t c = j < 16 ? byte_of(a, j) : byte_of(b, j - 16);
+    const bool bound = P ? c == ',' : (c == '>' || c == '<');
+    id[j] = 0;
+    if (bound) {
+      if (active) {
+        // the token [ts, j): P name = [ts, j - 1) with orientation prevc;
+        // W name = (ts, j)
+        const bool empty = P ? j - ts < 2 : j - ts < 2;
+        const uint64_t nv = P && lastacc ? pv : v;
+        const bool nany = P && lastacc ? pany : any;
+        const uint64_t at = P ? p0 + ts : p0 + ts + 1;
+        if (!empty) {
+          if (!nany) {
+            atomicMin(err, ((unsigned long long)(P ? 0 : 1) << 62) | (at << 2) | kParseNoDigits);
+          } else if (nv > 0xFFFFFFFFull) {
+            atomicMin(err, ((unsigned long long)(P ? 0 : 1) << 62) | (at << 2) | kParseOverflow);
+          } else if (nv) {
+            const bool neg = P ? prevc == '-' : rev;
+            id[j] = neg ? (int32_t)(0u - (uint32_t)nv) : (int32_t)(uint32_t)nv;
+            mask |= 1u << j;
+          }
+        }
+        active = false;
+      }
+      if (!P && j < 16) {  // a W marker opens the next token
+        active = true;
+        ts = j;
+        rev = c == '<';
+        v = pv = 0;
+        any = pany = stopped = lastacc = false;
+      }
+    } else {
+      if (P && !active && j < 16 && (j == 0 ? start0 : prevc == ',')) {
+        active = true;
+        ts = j;
+        v = pv = 0;
+        any = pany = stopped = lastacc = false;
+      }
+      if (active) {
+        const bool dig = c - '0' < 10u;
+        if (!stopped && dig) {
+          pv = v;
+          pany = any;
+          if (v < (1ull << 40)) v = v * 10 + (c - '0');  // beyond 2^40 it overflows anyway
+          any = true;
+          lastacc = true;
+        } else {
+          stopped = stopped || !dig;
+          lastacc = false;
+        }
+      }
+    }
+    prevc = c;
+  }
+  longk = active ? ts : -1;
+}
+
 // Pass 1 (WRITE = false): per-tile counts of kept P and W steps.  Pass 2:
 // the steps written at the scanned offsets, and each P/W line's first
 // output index.
 template <bool WRITE>
-__global__ void __launch_bounds__(kPB) k_tokens(const char *__restrict__ text, uint64_t n,
+__global__ void __launch_bounds__(kPB, 2) k_tokens(const char *__restrict__ text, uint64_t n,
                                                 const uint64_t *__restrict__ nl_off, uint64_t nlines,
                                                 const uint64_t *__restrict__ slotoff, PWLine *pw, NameIndex ni,
                                                 uint32_t *cntP, uint32_t *cntW, const uint64_t *__restrict__ offP,
@@ -319,28 +394,49 @@ __global__ void __launch_bounds__(kPB) k_tokens(const char *__restrict__ text, u
   Walk w = begin_walk(text, n, nl_off);
   const uint64_t li0 = w.li;
   uint32_t prev = w.p0 && w.p0 <= n ? S.at(w.p0 - 1) : 0;
-  int32_t ids[kPBytes];
-  uint32_t tok = 0, wk = 0;  // bit k: a kept step starts at byte k / that step is a W step
-  LineView L = line_view(slotoff, pw, nlines, w.li);
+  const LineView L0 = line_view(slotoff, pw, nlines, w.li);
+  // fast: numeric names and all 32 bytes from p0 inside the line's field
+  const bool fast = !ni.slots && L0.pw && w.p0 >= L0.fstart && w.p0 + 32 <= L0.fend;
+  int32_t ids[32];
+  // slow: bit k = a kept step starts at byte k (wk: it is a W step);
+  // fast: bit j = a kept step ends at byte j
+  uint32_t tok = 0, wk = 0;
+  int32_t long_id = 0;
+  if (fast) {
+    const uint4 nx = smem[(w.p0 - S.base) / 16 + 1];
+    const bool start0 = L0.kind == 0 && (w.p0 == L0.fstart || prev == ',');
+    int longk;
+    if (L0.kind == 0) lex_window<true>(w.v, nx, start0, w.p0, err, ids, tok, longk);
+    else lex_window<false>(w.v, nx, false, w.p0, err, ids, tok, longk);
+    if (longk >= 0) {
+      const uint64_t q = w.p0 + longk;
+      long_id = parse_token(S, q, S.at(q), S.at(q - 1), L0, ni, err);
+    }
+    if (L0.kind) wk = tok;
+  } else {
+    LineView L = L0;
 #pragma unroll
-  for (int k = 0; k < kPBytes; ++k) {
-    ids[k] = 0;
-    const uint64_t p = w.p0 + k;
-    if (p < n) {
-      const uint32_t c = byte_of(w.v, k);
-      if (L.pw && p >= L.fstart && p < L.fend) {
-        const int32_t id = parse_token(S, p, c, prev, L, ni, err);
-        if (id) {
-          ids[k] = id;
-          tok |= 1u << k;
-          wk |= L.kind << k;
+    for (int k = 0; k < kPBytes; ++k) {
+      ids[k] = 0;
+      const uint64_t p = w.p0 + k;
+      if (p < n) {
+        const uint32_t c = byte_of(w.v, k);
+        if (L.pw && p >= L.fstart && p < L.fend) {
+          const int32_t id = parse_token(S, p, c, prev, L, ni, err);
+          if (id) {
+            ids[k] = id;
+            tok |= 1u << k;
+            wk |= L.kind << k;
+          }
         }
+        if (c == '\n') L = line_view(slotoff, pw, nlines, ++w.li);
+        prev = c;
       }
-      if (c == '\n') L = line_view(slotoff, pw, nlines, ++w.li);
-      prev = c;
     }
   }
-  const uint32_t cw = __popc(wk), cp = __popc(tok) - cw;
+  const uint32_t nlong = long_id != 0;
+  const uint32_t cw = __popc(wk) + (fast && L0.kind ? nlong : 0);
+  const uint32_t cp = __popc(tok) - __popc(wk) + (fast && !L0.kind ? nlong : 0);
   unsigned long long total;
   const unsigned long long ex = block_excl_sum<kPB>(((unsigned long long)cp << 32) | cw, total);
   if (!WRITE) {
@@ -351,9 +447,18 @@ __global__ void __launch_bounds__(kPB) k_tokens(const char *__restrict__ text, u
     return;
   }
   uint64_t ip = offP[blockIdx.x] + (ex >> 32), iw = offW[blockIdx.x] + (uint32_t)ex;
+  if (fast) {
+    if (w.p0 == L0.fstart) pw[L0.slot].out = L0.kind ? iw : ip;
+    int32_t *o = L0.kind ? outW + iw : outP + ip;
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if ((tok >> j) & 1u) *o++ = ids[j];
+    if (long_id) *o = long_id;
+    return;
+  }
   // first output index of every P/W line whose field starts in these bytes
   uint64_t li = li0;
-  LineView M = line_view(slotoff, pw, nlines, li);
+  LineView M = L0;
 #pragma unroll
   for (int k = 0; k < kPBytes; ++k) {
     const uint64_t p = w.p0 + k;

@@ -44,6 +44,43 @@ CASES = {
     "header_only": b"H\tVN:Z:1.0",
 }
 
+def _long_lines(seed: int) -> bytes:
+    """Long P and W lines (thousands of tokens, so the device lexer's
+    whole-window path runs) mixing odd tokens: no orientation, a letter
+    inside the name, empty pieces, id 0, leading zeros (also past 16 bytes),
+    UINT32_MAX-bounded ids, junk and empty names in walks."""
+    rng = np.random.default_rng(seed)
+    p_tok = ["%d+", "%d-", "%d", "%da7+", "0%d-", "", "0+", "+", "%d+", "%d-", "00000000000000000000%d+",
+             "%d+", "%d-"]
+    w_tok = [">%d", "<%d", ">%dx", "<", ">0", "<000000000000000000%d", ">%d", "<%d", "7junk"]
+    out = [_segs(50)]
+    for t in range(6):
+        toks = []
+        for _ in range(3000):
+            f = p_tok[int(rng.integers(0, len(p_tok)))]
+            toks.append(f % int(rng.integers(1, 51)) if "%d" in f else f)
+        out.append("P\tlong%d\t%s\t*\n" % (t, ",".join(toks)))
+        ws = []
+        for _ in range(3000):
+            f = w_tok[int(rng.integers(0, len(w_tok)))]
+            ws.append(f % int(rng.integers(1, 51)) if "%d" in f else f)
+        out.append("W\ts%d\t%d\tc\t0\t9\t%s\n" % (t, t, "".join(ws)))
+    out.append("P\tmax\t%s\t*\n" % ",".join(["4294967295+"] * 40 + ["3+"] * 40))
+    return "".join(out).encode()
+
+
+def _long_error(kind: str) -> bytes:
+    good = ",".join("%d+" % (1 + i % 50) for i in range(2000))
+    if kind == "p_overflow":
+        return (_segs(50) + "P\tp\t%s,4294967296+,%s\t*\n" % (good, good)).encode()
+    if kind == "p_no_digits":
+        return (_segs(50) + "P\tp\t%s,x+,%s\t*\n" % (good, good)).encode()
+    walk = "".join(">%d" % (1 + i % 50) for i in range(2000))
+    return (_segs(50) + "W\ts\t1\tc\t0\t1\t%s>9999999999%s\n" % (walk, walk)).encode()
+
+
+CASES["numeric_long_lines"] = _long_lines(3)
+
 # name -> (text, message of the raised error)
 ERRORS = {
     "p_no_digits": ((_segs(3) + "P\tp\t1+,x+\t*\n").encode(), "parse_uint32: no digits"),
@@ -57,6 +94,9 @@ ERRORS = {
                        "parse_int64: no digits"),
     "w_steps_before_header": ((_segs(3) + "W\ts\t1\tc\t-\t1\t>x\n").encode(), "parse_uint32: no digits"),
     "s_overflow": (("S\t99999999999\tA\nP\tp\t1+\t*\n").encode(), "parse_uint32: overflow"),
+    "p_overflow_long_line": (_long_error("p_overflow"), "parse_uint32: overflow"),
+    "p_no_digits_long_line": (_long_error("p_no_digits"), "parse_uint32: no digits"),
+    "w_overflow_long_line": (_long_error("w_overflow"), "parse_uint32: overflow"),
 }
 
 
