@@ -550,6 +550,66 @@ def growth_text(result: GrowthResult, group_by: str = "path") -> str:
     return "".join(out)
 
 
+@dataclass
+class PavResult:
+    """include/workflows/pav_workflow.hpp:30-36: BED ranges (chrom, start,
+    end, name), group names, denominators[range] and numerators[range,
+    group] in bases."""
+
+    ranges: List[tuple] = field(default_factory=list)
+    group_names: List[str] = field(default_factory=list)
+    denominators: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint64))
+    numerators: np.ndarray = field(default_factory=lambda: np.zeros((0, 0), np.uint64))
+
+    def ratios(self) -> np.ndarray:
+        den = self.denominators.astype(np.float64)[:, None]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            r = self.numerators.astype(np.float64) / den
+        return np.where(den == 0, 0.0, r)
+
+
+_PAV_GROUP = {"path": 0, "haplotype": 2, "sample-hap": 2, "sample": 3}
+
+
+def compute_pav(data: CompressedData, bed_path, num_threads: int = DEFAULT_NUM_THREADS, group_by: str = "path",
+                ctx: Optional[Context] = None) -> PavResult:
+    """compute_pav (src/workflows/pav_workflow.cpp:475; `gfaz pav`): PAV
+    ratios of the traversal groups over BED ranges on reference traversals;
+    traversals are decoded and node membership built on the GPU.  group_by:
+    "path" (each traversal name), "haplotype" (-H) or "sample" (-S)."""
+    if group_by not in _PAV_GROUP:
+        raise ValueError("unknown group_by %r; expected one of %s" % (group_by, sorted(_PAV_GROUP)))
+    rs, gs, dp, np_ = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    rl, gl, nr, ng = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().gfz_pav(_ctx(ctx), data.handle, _cstr(bed_path), int(num_threads), _PAV_GROUP[group_by],
+                        ctypes.byref(rs), ctypes.byref(rl), ctypes.byref(gs), ctypes.byref(gl), ctypes.byref(nr),
+                        ctypes.byref(ng), ctypes.byref(dp), ctypes.byref(np_)))
+    ranges = [tuple(l.split("\t")) for l in take_bytes(rs, rl.value).decode().split("\n")[:-1]]
+    groups = take_bytes(gs, gl.value).decode().split("\n")[:-1]
+    den = np.frombuffer(take_bytes(dp, 8 * nr.value), np.uint64).copy()
+    num = np.frombuffer(take_bytes(np_, 8 * nr.value * ng.value), np.uint64).copy().reshape(nr.value, ng.value)
+    return PavResult([(c, int(a), int(b), n) for c, a, b, n in ranges], groups, den, num)
+
+
+def pav_text(result: PavResult, matrix: bool = False, binary_threshold: Optional[float] = None) -> str:
+    """The `gfaz pav` table (src/cli/pav_command.cpp:95-137)."""
+    r = result.ratios()
+
+    def cell(x):
+        return ("1" if x >= binary_threshold else "0") if binary_threshold is not None else "%.5g" % x
+    out = ["chrom\tstart\tend\tname"]
+    if matrix:
+        out.append("".join("\t" + g for g in result.group_names) + "\n")
+        for w, (c, a, b, n) in enumerate(result.ranges):
+            out.append("%s\t%d\t%d\t%s%s\n" % (c, a, b, n, "".join("\t" + cell(x) for x in r[w])))
+    else:
+        out.append("\tgroup\tpav\n")
+        for w, (c, a, b, n) in enumerate(result.ranges):
+            for gi, g in enumerate(result.group_names):
+                out.append("%s\t%d\t%d\t%s\t%s\t%s\n" % (c, a, b, n, g, cell(r[w, gi])))
+    return "".join(out)
+
+
 def decompress_data(data: CompressedData, threads: int = DEFAULT_NUM_THREADS,
                     ctx: Optional[Context] = None) -> GfaGraph:
     L = lib()

@@ -77,6 +77,8 @@ SIGNATURES = {
     "gfz_add_haplotypes": (I, [P, P, CP, I]),
     "gfz_decompress_graph": (I, [P, P, I, PP]),
     "gfz_parse_gfa": (I, [P, CP, I, I, PP]),
+    "gfz_pav": (I, [P, P, CP, I, I, PP, PSZ, PP, PSZ, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                    PP, PP]),
     "gfz_growth": (I, [P, P, I, I, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), PP, PP]),
     "gfz_graph_free": (None, [P]),
     "gfz_compressed_info": (I, [P, ctypes.POINTER(ContainerInfo)]),

@@ -415,6 +415,30 @@ gfz_status gfz_growth(gfz_context *ctx, const gfz_compressed *c, int threads, in
   });
 }
 
+gfz_status gfz_pav(gfz_context *ctx, const gfz_compressed *c, const char *bed_path, int threads, int group_by,
+                   char **ranges, size_t *ranges_len, char **groups, size_t *groups_len, uint64_t *nranges,
+                   uint64_t *ngroups, uint64_t **denominators, uint64_t **numerators) {
+  return guard([&] {
+    require(c && bed_path && ranges && ranges_len && groups && groups_len && nranges && ngroups && denominators &&
+                numerators,
+            "NULL argument");
+    require(group_by == 0 || group_by == 2 || group_by == 3, "group_by must be 0 (per traversal), 2 (sample#hap) or 3 (sample)");
+    const gfz::PavResult r = gfz::compute_pav(ctx_of(ctx), c->c, bed_path, threads, (gfz::GroupMode)group_by);
+    std::string rs, gs;
+    for (const auto &q : r.ranges)
+      rs += q.chrom + "\t" + std::to_string(q.start) + "\t" + std::to_string(q.end) + "\t" + q.name + "\n";
+    for (const auto &n : r.group_names) gs += n + "\n";
+    *ranges = dup_bytes(rs.data(), rs.size());
+    *ranges_len = rs.size();
+    *groups = dup_bytes(gs.data(), gs.size());
+    *groups_len = gs.size();
+    *nranges = r.ranges.size();
+    *ngroups = r.group_names.size();
+    *denominators = reinterpret_cast<uint64_t *>(dup_bytes(r.denominators.data(), r.denominators.size() * 8));
+    *numerators = reinterpret_cast<uint64_t *>(dup_bytes(r.numerators.data(), r.numerators.size() * 8));
+  });
+}
+
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out) {
   return guard([&] {
     require(c && out, "NULL argument");

@@ -4,7 +4,7 @@
 // Commands, options, default output names and error behaviour follow the
 // reference CLI (src/cli/gfaz_cli.cpp, compress_command.cpp,
 // decompress_command.cpp, extract_path_command.cpp, extract_walk_command.cpp,
-// add_haplotypes_command.cpp, growth_command.cpp): "Error: <message>" on stderr and exit code 1
+// add_haplotypes_command.cpp, growth_command.cpp, pav_command.cpp): "Error: <message>" on stderr and exit code 1
 // on failure, extracted lines on stdout.  The transform always runs on the
 // GPU; --gpu is accepted for compatibility.
 #include <getopt.h>
@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <iomanip>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -36,7 +37,8 @@ void usage() {
                "    gfaz extract-walk [OPTIONS] <input.gfaz>\n"
                "                      <sample_id> <hap_index> <seq_id> <seq_start> <seq_end> [...]\n"
                "    gfaz add-haplotypes [OPTIONS] <input.gfaz> <paths_or_walks.gfa> [output.gfaz]\n"
-               "    gfaz growth [-j N] [-G path|sample-hap-seq|sample-hap|sample] <input.gfaz>\n\n"
+               "    gfaz growth [-j N] [-G path|sample-hap-seq|sample-hap|sample] <input.gfaz>\n"
+               "    gfaz pav -i <input.gfaz> -b <ranges.bed> [-S|-H] [-M] [-B T] [-t N]\n\n"
                "compress options: -r/--rounds N (8)  -d/--delta N (1)  -t/--threshold N (2)\n"
                "                  -j/--threads N (0 = auto)  -g/--gpu  -s/--stats\n"
                "other commands:   -j/--threads N\n";
@@ -274,6 +276,109 @@ int do_growth(int argc, char **argv) {
   return 0;
 }
 
+// src/cli/pav_command.cpp: PAV ratios over BED ranges on stdout, one line
+// per (range, group) or a matrix (-M); -B T prints 1 / 0 for ratio >= T.
+int do_pav(int argc, char **argv) {
+  std::string in, bed;
+  int threads = 0, group = 0;
+  bool by_sample = false, by_hap = false, matrix = false, binary = false;
+  double threshold = 0.0;
+  static struct option lo[] = {{"idx", required_argument, 0, 'i'},
+                               {"input", required_argument, 0, 'i'},
+                               {"bed-file", required_argument, 0, 'b'},
+                               {"group-by-sample", no_argument, 0, 'S'},
+                               {"group-by-haplotype", no_argument, 0, 'H'},
+                               {"matrix-output", no_argument, 0, 'M'},
+                               {"binary-values", required_argument, 0, 'B'},
+                               {"threads", required_argument, 0, 't'},
+                               {"help", no_argument, 0, 'h'},
+                               {0, 0, 0, 0}};
+  int opt;
+  optind = 1;
+  while ((opt = getopt_long(argc, argv, "i:b:SHMB:t:j:h", lo, nullptr)) != -1) {
+    switch (opt) {
+      case 'i': in = optarg; break;
+      case 'b': bed = optarg; break;
+      case 'S': by_sample = true, group = 3; break;
+      case 'H': by_hap = true, group = 2; break;
+      case 'M': matrix = true; break;
+      case 'B': binary = true, threshold = std::stod(optarg); break;
+      case 't':
+      case 'j': threads = std::atoi(optarg); break;
+      case 'h':
+        std::cout << "gfaz pav -i <input.gfaz> -b <ranges.bed> [-S|-H] [-M] [-B T] [-t N]\n";
+        return 0;
+      default: return 1;
+    }
+  }
+  if (by_sample && by_hap) {
+    std::cerr << "Error: select only one grouping option: -S or -H\n";
+    return 1;
+  }
+  if (binary && (threshold < 0.0 || threshold > 1.0)) {
+    std::cerr << "Error: --binary-values threshold must be in [0,1]\n";
+    return 1;
+  }
+  if (in.empty() && optind < argc) in = argv[optind++];
+  if (in.empty()) {
+    std::cerr << "Error: Expected -i <input.gfaz>\n";
+    return 1;
+  }
+  if (bed.empty()) {
+    std::cerr << "Error: Expected -b <ranges.bed>\n";
+    return 1;
+  }
+  gfz_compressed *c = nullptr;
+  if (gfz_deserialize(in.c_str(), &c) != GFZ_OK) return fail();
+  char *rs = nullptr, *gs = nullptr;
+  size_t rl = 0, gl = 0;
+  uint64_t nr = 0, ng = 0, *den = nullptr, *num = nullptr;
+  const gfz_status st = gfz_pav(nullptr, c, bed.c_str(), threads, group, &rs, &rl, &gs, &gl, &nr, &ng, &den, &num);
+  gfz_compressed_free(c);
+  if (st != GFZ_OK) return fail();
+  auto lines = [](const char *p, size_t n) {
+    std::vector<std::string> v;
+    size_t b = 0;
+    for (size_t i = 0; i < n; ++i)
+      if (p[i] == '\n') {
+        v.emplace_back(p + b, i - b);
+        b = i + 1;
+      }
+    return v;
+  };
+  const std::vector<std::string> ranges = lines(rs, rl), groups = lines(gs, gl);
+  auto ratio = [&](uint64_t w, uint64_t g) {
+    return den[w] == 0 ? 0.0 : (double)num[w * ng + g] / (double)den[w];
+  };
+  std::cout << "chrom\tstart\tend\tname";
+  if (matrix) {
+    for (const auto &g : groups) std::cout << '\t' << g;
+    std::cout << '\n';
+    for (uint64_t w = 0; w < nr; ++w) {
+      std::cout << ranges[w];
+      for (uint64_t g = 0; g < ng; ++g) {
+        if (binary) std::cout << '\t' << (ratio(w, g) >= threshold ? 1 : 0);
+        else std::cout << '\t' << std::setprecision(5) << ratio(w, g);
+      }
+      std::cout << '\n';
+    }
+  } else {
+    std::cout << "\tgroup\tpav\n";
+    for (uint64_t w = 0; w < nr; ++w)
+      for (uint64_t g = 0; g < ng; ++g) {
+        std::cout << ranges[w] << '\t' << groups[g] << '\t';
+        if (binary) std::cout << (ratio(w, g) >= threshold ? 1 : 0);
+        else std::cout << std::setprecision(5) << ratio(w, g);
+        std::cout << '\n';
+      }
+  }
+  gfz_free(rs);
+  gfz_free(gs);
+  gfz_free(den);
+  gfz_free(num);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -288,6 +393,7 @@ int main(int argc, char **argv) {
   if (cmd == "extract-walk") return do_extract_walk(argc - 1, argv + 1);
   if (cmd == "add-haplotypes") return do_add_haplotypes(argc - 1, argv + 1);
   if (cmd == "growth") return do_growth(argc - 1, argv + 1);
+  if (cmd == "pav") return do_pav(argc - 1, argv + 1);
   if (cmd == "-h" || cmd == "--help" || cmd == "help") {
     usage();
     return 0;

@@ -81,6 +81,25 @@ std::vector<uint32_t> growth_groups(const Compressed &c, GroupMode mode, uint32_
 // growth[k] from the coverage histogram (growth_workflow.cpp:106-118, 480-500).
 std::vector<double> growth_curve(const std::vector<uint64_t> &hist, uint32_t N, int threads);
 
+// Presence/absence ratios, include/workflows/pav_workflow.hpp:14-37: BED
+// ranges on reference traversals (P names, or W "sample#hap#seq[:start-end]");
+// numerators[range * groups + group] and denominators[range] in bases.
+// Grouping: kPerPathWalk (each name), kSample, kSampleHap (PAV's own
+// reading of PanSN names, pav_workflow.cpp:295-368).
+struct PavRange {
+  std::string chrom;
+  uint64_t start = 0, end = 0;
+  std::string name;
+};
+struct PavResult {
+  std::vector<PavRange> ranges;
+  std::vector<std::string> group_names;
+  std::vector<uint64_t> denominators, numerators;
+};
+// src/workflows/pav_workflow.cpp:475 compute_pav (traversals decoded and
+// node membership built on the GPU)
+PavResult compute_pav(Context &ctx, const Compressed &c, const std::string &bed_path, int threads, GroupMode mode);
+
 // src/workflows/add_haplotypes_workflow.cpp:579 add_haplotypes
 void add_haplotypes(Context &ctx, Compressed &c, const std::string &path, int threads);
 // Parsed add-haplotypes input: P-lines or W-lines (never both), with the

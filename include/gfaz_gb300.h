@@ -151,6 +151,15 @@ gfz_status gfz_parse_gfa(gfz_context *ctx, const char *path, int threads, int de
  * both released with gfz_free (NULL when num_haplotypes is 0). */
 gfz_status gfz_growth(gfz_context *ctx, const gfz_compressed *c, int threads, int group_by, uint32_t *num_haplotypes,
                       uint32_t *num_nodes, uint64_t **hist, double **growth);
+/* compute_pav, include/workflows/pav_workflow.hpp:35 (`gfaz pav`,
+ * src/cli/pav_command.cpp): group_by 0 = every traversal name, 2 =
+ * sample#hap (-H), 3 = sample (-S).  Outputs, released with gfz_free: the
+ * BED ranges as "chrom\tstart\tend\tname\n" lines, the group names
+ * newline-joined, denominators[nranges] and numerators[nranges * ngroups]
+ * (row = range), in bases. */
+gfz_status gfz_pav(gfz_context *ctx, const gfz_compressed *c, const char *bed_path, int threads, int group_by,
+                   char **ranges, size_t *ranges_len, char **groups, size_t *groups_len, uint64_t *nranges,
+                   uint64_t *ngroups, uint64_t **denominators, uint64_t **numerators);
 /* decompress_gfa, include/workflows/decompression_workflow.hpp:8-9 */
 gfz_status gfz_decompress_graph(gfz_context *ctx, const gfz_compressed *c, int threads, gfz_graph **out);
 void gfz_graph_free(gfz_graph *g);
