@@ -116,3 +116,54 @@ def random_text(seed: int, n_segments: int, n_paths: int, n_walks: int, named: b
             parts.append("P\tpath%d\t%s\t*\n" % (
                 t, ",".join(name(int(x)) + ("-" if v < 0 else "+") for v, x in zip(s, a))))
     return "".join(parts).encode()
+
+
+def fuzz_text(seed: int) -> bytes:
+    """A random GFA text for front-end parity: numeric (in order, shuffled
+    or duplicated) or named segments; P and W lines of random pieces
+    (digits, orientations, letters, empty pieces, long zero runs, huge
+    numbers), random blank runs between fields, CR, empty and unknown
+    lines, optional fields, and sometimes no final newline.  Some texts
+    are malformed on purpose (the parsers must then raise the same error)."""
+    rng = np.random.default_rng(seed)
+    nseg = int(rng.integers(1, 60))
+    mode = int(rng.integers(0, 4))  # 0,1 numeric in order; 2 shuffled / duplicates; 3 named
+    if mode == 3:
+        names = ["s%d" % i for i in range(1, nseg + 1)]
+    elif mode == 2:
+        names = [str(int(x)) for x in rng.permutation(nseg) + 1] + [str(int(rng.integers(1, nseg + 1)))]
+    else:
+        names = [str(i) for i in range(1, nseg + 1)]
+    pool = names + ["0", "007", "x", "99999999999", "4294967295", "4294967296", "", "1a"]
+    weights = np.array([8.0] * len(names) + [0.3] * 8)
+    weights /= weights.sum()
+
+    def blank():
+        return "".join(rng.choice(["\t", " "]) for _ in range(int(rng.integers(1, 3))))
+
+    def name():
+        return pool[int(rng.choice(len(pool), p=weights))]
+    lines = []
+    for n in names:
+        opt = (blank() + "LN:i:%d" % int(rng.integers(0, 99))) if rng.random() < 0.2 else ""
+        lines.append("S" + blank() + n + blank() + "ACGT"[: int(rng.integers(1, 5))] + opt)
+    for t in range(int(rng.integers(1, 9))):
+        if rng.random() < 0.5:
+            pieces = []
+            for _ in range(int(rng.integers(0, 400))):
+                r = rng.random()
+                pieces.append("" if r < 0.03 else name() + ("" if r < 0.06 else "+-"[int(rng.integers(0, 2))]))
+            tail = blank() + "*" if rng.random() < 0.8 else ""
+            lines.append("P" + blank() + "p%d" % t + blank() + ",".join(pieces) + tail)
+        else:
+            steps = "".join(("><"[int(rng.integers(0, 2))] if rng.random() < 0.97 else "") + name()
+                            for _ in range(int(rng.integers(0, 400))))
+            st = "*" if rng.random() < 0.3 else str(int(rng.integers(0, 100)))
+            lines.append("W" + blank() + "smp%d" % (t % 3) + blank() + str(t % 2) + blank() + "c" + blank() + st +
+                         blank() + "*" + blank() + ("junk" if rng.random() < 0.1 else "") + steps)
+    for _ in range(int(rng.integers(0, 4))):
+        lines.insert(int(rng.integers(0, len(lines) + 1)), rng.choice(["", "#x", "X\ty", "L\t1\t+\t2\t-\t0M"]))
+    text = "\n".join(l + ("\r" if rng.random() < 0.05 else "") for l in lines)
+    if rng.random() < 0.8:
+        text += "\n"
+    return text.encode()

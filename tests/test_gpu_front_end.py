@@ -12,7 +12,7 @@ import pytest
 import gfaz_gb300 as gz
 from conftest import GOLDEN
 from oracle import gfa_parse
-from parse_cases import CASES, ERRORS, random_text
+from parse_cases import CASES, ERRORS, fuzz_text, random_text
 from test_parse_cpu import same_as_oracle
 
 pytestmark = pytest.mark.gpu
@@ -76,3 +76,22 @@ def test_compress_file_front_ends_agree(case, tmp_path, gpu_ctx):
     gz.serialize(a, str(pa))
     gz.serialize(b, str(pb))
     assert pa.read_bytes() == pb.read_bytes()
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_device_parse_fuzz(seed, tmp_path, gpu_ctx):
+    """Random texts: the same graph, or the same error, as the host parser
+    on one thread (whose first error is deterministic)."""
+    p = tmp_path / "in.gfa"
+    p.write_bytes(fuzz_text(seed))
+
+    def run(**kw):
+        try:
+            return gz.parse_gfa(str(p), **kw), None
+        except gz.GfazError as e:
+            return None, str(e)
+    want, werr = run(threads=1, device=False)
+    got, gerr = run(ctx=gpu_ctx)
+    assert gerr == werr
+    if want is not None:
+        same_graph(got, want)

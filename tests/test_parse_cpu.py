@@ -10,7 +10,7 @@ import pytest
 import gfaz_gb300 as gz
 from conftest import GOLDEN, golden_raw
 from oracle import gfa_parse
-from parse_cases import CASES, ERRORS
+from parse_cases import CASES, ERRORS, fuzz_text
 
 
 def same_as_oracle(g, want):
@@ -58,3 +58,21 @@ def test_host_parse_errors(case, tmp_path):
 def test_host_parse_missing_file(tmp_path):
     with pytest.raises(gz.GfazError, match="GFA parser error: failed to open input file"):
         gz.parse_gfa(str(tmp_path / "nope.gfa"), device=False)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_host_parse_fuzz(seed, tmp_path):
+    """Random texts (tests/parse_cases.fuzz_text): the host parser on one
+    thread gives the restatement's traversals, or its error."""
+    text = fuzz_text(seed)
+    p = tmp_path / "in.gfa"
+    p.write_bytes(text)
+    try:
+        want, werr = gfa_parse.parse(text), None
+    except ValueError as e:
+        want, werr = None, str(e)
+    if werr is not None:
+        with pytest.raises(gz.GfazError, match=werr):
+            gz.parse_gfa(str(p), threads=1, device=False)
+    else:
+        same_as_oracle(gz.parse_gfa(str(p), threads=1, device=False), want)
