@@ -662,17 +662,6 @@ void scan_u32(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out) {
   exclusive_scan(ctx, in, n, out, "gfa_scan");
 }
 
-struct PhaseClock {
-  bool on = debug_enabled();
-  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
-  void mark(const char *what) {
-    if (!on) return;
-    const auto now = std::chrono::steady_clock::now();
-    std::cerr << "[gfa front end] " << what << ": " << std::chrono::duration<double, std::milli>(now - t).count()
-              << " ms" << std::endl;
-    t = now;
-  }
-};
 
 // Lines by type from the device line index (type[i], line ends eol), in
 // parallel: per-thread counts, then each thread fills its share.  slot of
@@ -747,7 +736,7 @@ DeviceParse parse_gfa_device(Context &ctx, const std::string &path, int threads)
     return r;
   }
   ctx.reset_status();
-  PhaseClock clk;
+  PhaseClock clk("gfa front end");
   // the file, zero-padded to 16 bytes
   const uint64_t npad = (n + 15) & ~15ull;
   DevVec<char> text(st);

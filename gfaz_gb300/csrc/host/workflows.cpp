@@ -529,6 +529,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   for (uint64_t t = 0; t < np; ++t) off[t + 1] = g.paths.offsets[t + 1];
   for (uint64_t t = 0; t < nw; ++t) off[np + t + 1] = NP + g.walks.offsets[t + 1];
   cudaStream_t st = ctx.stream();
+  PhaseClock clk("compress");
   Grammar gram(st);
   if (d_steps)
     encode_traversals(ctx, d_steps, off, EncodeParams{rounds, delta_round}, gram);
@@ -548,6 +549,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   if (!enc.empty())
     cuda_check(cudaMemcpyAsync(enc.data(), gram.enc.ptr, enc.size() * 4, cudaMemcpyDeviceToHost, st), "download");
   cuda_check(cudaStreamSynchronize(st), "stream sync");
+  clk.mark("transform + downloads");
   const uint32_t rule_count = gram.next_id - gram.layer_start;
   out.layers.push_back(LayerRange{2, gram.layer_start, gram.next_id, 0, (uint64_t)rule_count * 2});
 
@@ -558,11 +560,22 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   std::vector<uint32_t> name_lens, ov_lens, seg_lens;
   join_strings(g.path_names, names_cat, name_lens);
   join_strings(g.path_overlaps, ov_cat, ov_lens);
-  // segments 1 .. min(S, next_id - 1) (compression_utils.cpp:81-101)
-  for (size_t i = 1; i < g.node_sequences.size() && i < gram.next_id; ++i) {
-    seg_cat += g.node_sequences[i];
-    seg_lens.push_back((uint32_t)g.node_sequences[i].size());
+  // segments 1 .. min(S, next_id - 1) (compression_utils.cpp:81-101),
+  // concatenated in parallel from their offsets
+  {
+    const size_t ns = g.node_sequences.empty() ? 0 : std::min<size_t>(g.node_sequences.size() - 1, gram.next_id - 1);
+    seg_lens.resize(ns);
+    std::vector<uint64_t> so(ns + 1, 0);
+    for (size_t i = 0; i < ns; ++i) {
+      seg_lens[i] = (uint32_t)g.node_sequences[i + 1].size();
+      so[i + 1] = so[i] + g.node_sequences[i + 1].size();
+    }
+    seg_cat.resize(so[ns]);
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int64_t i = 0; i < (int64_t)ns; ++i)
+      std::memcpy(&seg_cat[so[i]], g.node_sequences[i + 1].data(), g.node_sequences[i + 1].size());
   }
+  clk.mark("host columns");
 
 #pragma omp parallel sections num_threads(std::min(nth, 8))
   {
@@ -652,6 +665,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
       }
     }
   }
+  clk.mark("zstd of every column");
   if (show_stats) {
     std::cerr << "\n=== Compressed Data Breakdown ===\n"
               << "Rules (2-mer grammar): " << rule_count << " rules, " << gram.rounds_done << " rounds\n"

@@ -4,6 +4,8 @@
 // the device pipeline.
 #pragma once
 
+#include <chrono>
+#include <iostream>
 #include <string>
 #include <vector>
 
@@ -11,6 +13,24 @@
 #include "model.h"
 
 namespace gfz {
+
+// Wall-clock phases on stderr ("[label] phase: ms") when
+// GFA_COMPRESSION_DEBUG is set.
+struct PhaseClock {
+  explicit PhaseClock(const char *label) : label_(label) {}
+  void mark(const char *what) {
+    if (!on_) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::cerr << "[" << label_ << "] " << what << ": "
+              << std::chrono::duration<double, std::milli>(now - t_).count() << " ms" << std::endl;
+    t_ = now;
+  }
+
+ private:
+  const char *label_;
+  bool on_ = debug_enabled();
+  std::chrono::steady_clock::time_point t_ = std::chrono::steady_clock::now();
+};
 
 struct WalkKey {
   std::string sample_id;
