@@ -151,15 +151,15 @@ COPY_PIECE = 1 << 30
 
 
 def copy_bytes(ptr, n: int) -> bytes:
-    """n bytes at ptr.  ctypes.string_at takes its size as a C int, so 2 GiB
-    and more are copied in pieces of COPY_PIECE bytes."""
+    """n bytes at ptr.  ctypes.string_at takes its size as a C int, so
+    buffers above COPY_PIECE bytes are copied once through a memoryview of a
+    char array laid over them."""
     if not n:
         return b""
     addr = ptr.value if isinstance(ptr, ctypes.c_void_p) else int(ptr)
-    piece = COPY_PIECE
-    if n <= piece:
+    if n <= COPY_PIECE:
         return ctypes.string_at(addr, n)
-    return b"".join(ctypes.string_at(addr + o, min(piece, n - o)) for o in range(0, n, piece))
+    return memoryview((ctypes.c_char * n).from_address(addr)).tobytes()
 
 
 def take_bytes(ptr: ctypes.c_void_p, n: int) -> bytes:

@@ -317,9 +317,10 @@ gfz_status gfz_write_gfa(gfz_context *ctx, const gfz_compressed *c, const char *
 gfz_status gfz_gfa_text(gfz_context *ctx, const gfz_compressed *c, int threads, char **out, size_t *len) {
   return guard([&] {
     require(c && out && len, "NULL argument");
-    const std::string s = gfz::gfa_text(ctx_of(ctx), c->c, threads);
-    *out = dup_bytes(s.data(), s.size());
-    *len = s.size();
+    gfz::RawText t;
+    gfz::gfa_text_into(ctx_of(ctx), c->c, threads, t);
+    *len = t.size();
+    *out = t.release();
   });
 }
 

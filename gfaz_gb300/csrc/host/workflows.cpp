@@ -772,12 +772,75 @@ void download_text(Context &ctx, const DevVec<char> &text, uint64_t n, std::stri
 
 }  // namespace
 
-std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
-  set_zstd_threads(resolve_threads(threads));
+char *RawText::grow(size_t k) {
+  if (n_ + k + 1 > cap_) {
+    size_t c = std::max<size_t>(cap_ * 2, n_ + k + 1);
+    char *q = static_cast<char *>(std::realloc(p_, c));
+    if (!q) throw std::bad_alloc();
+    p_ = q;
+    cap_ = c;
+  }
+  char *at = p_ + n_;
+  n_ += k;
+  return at;
+}
+
+char *RawText::release() {
+  grow(0);
+  p_[n_] = '\0';
+  char *q = p_;
+  p_ = nullptr;
+  n_ = cap_ = 0;
+  return q;
+}
+
+namespace {
+
+// Device text -> host memory through two page-locked staging buffers: the
+// copy engine fills one while host threads copy the other out.
+void download_raw(Context &ctx, const char *dev, uint64_t n, char *dst, int nth) {
+  cudaStream_t st = ctx.stream();
+  const uint64_t piece = 128ull << 20;
+  cudaEvent_t ev[2];
+  cuda_check(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming), "event");
+  cuda_check(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming), "event");
+  char *stage[2] = {reinterpret_cast<char *>(ctx.host_buffer(0, piece / 4)),
+                    reinterpret_cast<char *>(ctx.host_buffer(1, piece / 4))};
+  auto issue = [&](uint64_t k) {
+    const uint64_t o = k * piece, m = std::min(piece, n - o);
+    cuda_check(cudaMemcpyAsync(stage[k & 1], dev + o, m, cudaMemcpyDeviceToHost, st), "text download");
+    cuda_check(cudaEventRecord(ev[k & 1], st), "event");
+  };
+  const uint64_t pieces = (n + piece - 1) / piece;
+  if (pieces) issue(0);
+  for (uint64_t k = 0; k < pieces; ++k) {
+    cuda_check(cudaEventSynchronize(ev[k & 1]), "event sync");
+    if (k + 1 < pieces) issue(k + 1);  // the other staging buffer is free
+    const uint64_t o = k * piece, m = std::min(piece, n - o);
+    const int T = std::max(1, std::min(nth, (int)(m >> 22) + 1));
+#pragma omp parallel for schedule(static) num_threads(T)
+    for (int t = 0; t < T; ++t) {
+      const uint64_t a = m * t / T, b = m * (t + 1) / T;
+      std::memcpy(dst + o + a, stage[k & 1] + a, b - a);
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+}
+
+}  // namespace
+
+void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out) {
+  const int nth = resolve_threads(threads);
+  set_zstd_threads(nth);
+  PhaseClock clk("gfa text");
   const StaticFields s = decode_static(c);
-  std::string out = ctx.static_text ? static_text_device(ctx, c, s, resolve_threads(threads)) : static_text(c, s);
+  clk.mark("static columns (zstd)");
+  out.append(ctx.static_text ? static_text_device(ctx, c, s, nth) : static_text(c, s));
+  clk.mark("H/S/L/J/C text");
   Grammar g(ctx.stream());
   const LoadedStreams ls = load_all(ctx, c, g, kWriterErr);
+  clk.mark("rules + encoded streams (zstd, upload)");
   DevVec<char> text(ctx.stream());
   if (ls.np) {
     const auto names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
@@ -785,7 +848,9 @@ std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
     const std::vector<uint64_t> off(g.h_off.begin(), g.h_off.begin() + (ptrdiff_t)ls.np + 1);
     const uint64_t n = decode_text(
         ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0, text);
-    download_text(ctx, text, n, out);
+    clk.mark("P text (device)");
+    download_raw(ctx, text.ptr, n, out.grow(n), nth);
+    clk.mark("P text download");
   }
   if (ls.nw) {
     const auto samples =
@@ -798,15 +863,21 @@ std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
         ctx, g, ls.np, ls.np + ls.nw,
         [&](const std::vector<uint64_t> &xoff) { return walk_pieces(samples, haps, seqids, starts, ends, xoff); }, 1,
         text);
-    download_text(ctx, text, n, out);
+    download_raw(ctx, text.ptr, n, out.grow(n), nth);
   }
-  return out;
+}
+
+std::string gfa_text(Context &ctx, const Compressed &c, int threads) {
+  RawText t;
+  gfa_text_into(ctx, c, threads, t);
+  return std::string(t.data() ? t.data() : "", t.size());
 }
 
 void write_gfa(Context &ctx, const Compressed &c, const std::string &out_path, int threads) {
   std::ofstream out(out_path, std::ios::binary);
   if (!out) throw std::runtime_error(std::string(kWriterErr) + "failed to open output file: " + out_path);
-  const std::string text = gfa_text(ctx, c, threads);
+  RawText text;
+  gfa_text_into(ctx, c, threads, text);
   out.write(text.data(), (std::streamsize)text.size());
   if (!out) throw std::runtime_error(std::string(kWriterErr) + "failed to write output file: " + out_path);
 }

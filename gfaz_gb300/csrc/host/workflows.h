@@ -5,6 +5,8 @@
 #pragma once
 
 #include <chrono>
+#include <cstdlib>
+#include <cstring>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -66,6 +68,31 @@ Compressed compress_gfa(Context &ctx, const std::string &gfa_path, int rounds, u
 // walks back to back, used in place of g's host steps.
 Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t threshold, int delta_round,
                           int threads, bool show_stats, const int32_t *d_steps = nullptr);
+
+// Growable text in malloc'd memory that is never zero-filled: the
+// full-file text is written into it and handed to C callers as is
+// (released with free).
+class RawText {
+ public:
+  RawText() = default;
+  RawText(const RawText &) = delete;
+  RawText &operator=(const RawText &) = delete;
+  ~RawText() { std::free(p_); }
+  // k more bytes at the end, uninitialized; returns where they start.
+  char *grow(size_t k);
+  void append(const char *s, size_t k) { if (k) std::memcpy(grow(k), s, k); }
+  void append(const std::string &s) { append(s.data(), s.size()); }
+  const char *data() const { return p_; }
+  size_t size() const { return n_; }
+  // The buffer (NUL-terminated) and its ownership.
+  char *release();
+
+ private:
+  char *p_ = nullptr;
+  size_t n_ = 0, cap_ = 0;
+};
+// The whole decompressed GFA (the bytes write_gfa writes) into out.
+void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out);
 
 // src/io/gfa_writer.cpp:376 write_gfa_from_compressed_data (H,S,L,J,C,P,W)
 void write_gfa(Context &ctx, const Compressed &c, const std::string &out_path, int threads);
