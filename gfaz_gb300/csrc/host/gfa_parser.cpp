@@ -398,36 +398,92 @@ void parse_segments(const char *d, const std::vector<Line> &S, Graph &g, Names &
   for (auto &c : g.segment_optional) pad_column(c, nseg);
 }
 
-void parse_links(const char *d, const std::vector<Line> &L, const Names &nm, Graph &g) {
+// L lines.  The fields are read in parallel; the order-dependent work runs
+// after, in line order: a line's name error is raised where the sequential
+// parser would raise it (before that line's optional fields, after the
+// optional fields of earlier lines), and optional-field columns are built
+// in line order.
+void parse_links(const char *d, const std::vector<Line> &L, const Names &nm, Graph &g, int threads) {
   OptSet link_opt{&g.link_optional, {}, "link "};
-  for (const Line &ln : L) {
-    const std::string_view line(d + ln.off, ln.len);
+  const int64_t nl = (int64_t)L.size();
+  struct Link {
+    uint32_t a = 0, b = 0, num = 0;
+    size_t rest = 0;  // offset of the optional fields in the line (0: none)
+    char fo = '+', to = '+', op = '\0';
+    bool err = false;
+  };
+  std::vector<Link> v(nl);
+  std::vector<std::string> errs;
+  std::vector<int64_t> err_at;
+#pragma omp parallel for schedule(static) num_threads(resolve_threads(threads))
+  for (int64_t i = 0; i < nl; ++i) {
+    const std::string_view line(d + L[i].off, L[i].len);
     size_t pos = 1;
     const std::string_view fn = next_field(line, pos), fo = next_field(line, pos);
     const std::string_view tn = next_field(line, pos), to = next_field(line, pos);
     const std::string_view ov = next_field(line, pos);
-    const uint32_t a = nm.resolve(fn), b = nm.resolve(tn);
-    if (a == 0 || b == 0) continue;
-    g.link_from.push_back(a);
-    g.link_to.push_back(b);
-    g.link_from_orients.push_back(fo.empty() ? '+' : fo[0]);
-    g.link_to_orients.push_back(to.empty() ? '+' : to[0]);
-    if (ov.empty() || ov == "*") {
-      g.link_overlap_nums.push_back(0);
-      g.link_overlap_ops.push_back('\0');
-    } else {
-      char op;
-      g.link_overlap_nums.push_back(overlap_number(ov, op));
-      g.link_overlap_ops.push_back(op);
+    Link &k = v[i];
+    try {
+      k.a = nm.resolve(fn);
+      k.b = nm.resolve(tn);
+    } catch (const std::exception &e) {
+      k.err = true;
+#pragma omp critical
+      {
+        errs.emplace_back(e.what());
+        err_at.push_back(i);
+      }
+      continue;
     }
-    const size_t li = g.link_from.size() - 1;
+    k.fo = fo.empty() ? '+' : fo[0];
+    k.to = to.empty() ? '+' : to[0];
+    if (!ov.empty() && ov != "*") k.num = overlap_number(ov, k.op);
+    while (pos < line.size() && (line[pos] == ' ' || line[pos] == '\t')) ++pos;
+    k.rest = pos < line.size() ? pos : 0;
+  }
+  int64_t first_err = nl;
+  std::string first_msg;
+  for (size_t e = 0; e < err_at.size(); ++e)
+    if (err_at[e] < first_err) {
+      first_err = err_at[e];
+      first_msg = errs[e];
+    }
+  // kept links (both ends resolved), in order
+  std::vector<uint64_t> at(nl + 1, 0);
+  for (int64_t i = 0; i < nl; ++i) at[i + 1] = at[i] + (!v[i].err && v[i].a && v[i].b);
+  // optional fields and the first error, in line order
+  for (int64_t i = 0; i < nl; ++i) {
+    if (i == first_err) throw std::runtime_error(first_msg);
+    const Link &k = v[i];
+    if (!k.a || !k.b || !k.rest) continue;
+    const std::string_view line(d + L[i].off, L[i].len);
+    size_t pos = k.rest;
     while (pos < line.size()) {
       const std::string_view f = next_field(line, pos);
       if (f.empty()) break;
-      link_opt.add(f, li);
+      link_opt.add(f, at[i]);
     }
   }
-  for (auto &c : g.link_optional) pad_column(c, g.link_from.size());
+  const uint64_t n = at[nl];
+  g.link_from.resize(n);
+  g.link_to.resize(n);
+  g.link_from_orients.resize(n);
+  g.link_to_orients.resize(n);
+  g.link_overlap_nums.resize(n);
+  g.link_overlap_ops.resize(n);
+#pragma omp parallel for schedule(static) num_threads(resolve_threads(threads))
+  for (int64_t i = 0; i < nl; ++i) {
+    const Link &k = v[i];
+    if (k.err || !k.a || !k.b) continue;
+    const uint64_t j = at[i];
+    g.link_from[j] = k.a;
+    g.link_to[j] = k.b;
+    g.link_from_orients[j] = k.fo;
+    g.link_to_orients[j] = k.to;
+    g.link_overlap_nums[j] = k.num;
+    g.link_overlap_ops[j] = k.op;
+  }
+  for (auto &c : g.link_optional) pad_column(c, n);
 }
 
 // P line header: the name and, from the end of the steps field, the
@@ -627,7 +683,7 @@ Graph parse_gfa(const std::string &path, int threads) {
   scan_lines(d, m.size, ls, g);
   Names nm;
   parse_segments(d, ls.S, g, nm, threads);
-  parse_links(d, ls.L, nm, g);
+  parse_links(d, ls.L, nm, g, threads);
   parse_traversals_host(d, ls, nm, threads, g);
   parse_jumps_containments(d, ls, nm, g);
   return g;
@@ -816,7 +872,7 @@ DeviceParse parse_gfa_device(Context &ctx, const std::string &path, int threads)
     ni = NameIndex{slots.ptr, cap - 1, noff.ptr, nlen.ptr};
     cuda_check(cudaStreamSynchronize(st), "stream sync");  // ho / hl leave scope
   }
-  parse_links(d, ls.L, nm, g);
+  parse_links(d, ls.L, nm, g, threads);
 
   // P / W steps
   DevVec<uint64_t> offP(st), offW(st);

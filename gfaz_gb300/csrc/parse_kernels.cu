@@ -329,7 +329,7 @@ __device__ __forceinline__ void lex_window(const uint4 &a, const uint4 &b, bool 
       if (active) {
         // the token [ts, j): P name = [ts, j - 1) with orientation prevc;
         // W name = (ts, j)
-        const bool empty = P ? j - ts < 2 : j - ts < 2;
+        const bool empty = j - ts < 2;  // P: one byte (the orientation); W: the marker alone
         const uint64_t nv = P && lastacc ? pv : v;
         const bool nany = P && lastacc ? pany : any;
         const uint64_t at = P ? p0 + ts : p0 + ts + 1;

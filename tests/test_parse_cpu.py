@@ -76,3 +76,28 @@ def test_host_parse_fuzz(seed, tmp_path):
             gz.parse_gfa(str(p), threads=1, device=False)
     else:
         same_as_oracle(gz.parse_gfa(str(p), threads=1, device=False), want)
+
+
+@pytest.mark.parametrize("order", ["field_first", "name_first"])
+def test_host_parse_link_error_order(order, tmp_path):
+    """L lines are read in parallel, but errors surface in line order as in
+    the sequential parser: an optional-field type clash on an earlier line
+    wins over a bad segment name on a later one, and the other way round."""
+    segs = "".join("S\t%d\tA\n" % i for i in range(1, 4))
+    clash = "L\t1\t+\t2\t-\t0M\tXX:i:5\nL\t2\t+\t3\t-\t0M\tXX:Z:a\n"
+    bad = "L\tx\t+\t3\t-\t0M\n"
+    text = segs + (clash + bad if order == "field_first" else bad + clash)
+    p = tmp_path / "in.gfa"
+    p.write_text(text)
+    msg = "Type mismatch for link tag 'XX'" if order == "field_first" else "parse_uint32: no digits"
+    with pytest.raises(gz.GfazError, match=msg):
+        gz.parse_gfa(str(p), device=False)
+
+
+def test_host_parse_links_kept_and_counted(tmp_path):
+    """Links with an unresolved end are dropped (named segments); the rest
+    keep their order."""
+    text = "S\ta\tA\nS\tb\tC\nL\ta\t+\tb\t-\t3M\nL\ta\t+\tzz\t-\t*\nL\tb\t-\ta\t+\t*\tRC:i:2\n"
+    p = tmp_path / "in.gfa"
+    p.write_text(text)
+    assert gz.parse_gfa(str(p), device=False).num_links == 2
