@@ -5,6 +5,7 @@
 #include "workflows.h"
 
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cstring>
@@ -196,18 +197,33 @@ struct StaticFields {
   std::vector<std::string> cov, crest;
 };
 
+// The columns are independent, so they decode in parallel (each zstd frame
+// itself decodes on one thread).
 StaticFields decode_static(const Compressed &d) {
   StaticFields s;
-  s.seg_seq = unzstd_str(d.segment_sequences);
-  s.seg_len = unzstd_u32(d.segment_seq_lengths);
-  for (const auto &c : d.segment_optional) s.seg_opt.push_back(decompress_opt(c));
-  for (const auto &c : d.link_optional) s.link_opt.push_back(decompress_opt(c));
-  s.lf = undelta_varint_u32(d.link_from_ids, d.num_links);
-  s.lt = undelta_varint_u32(d.link_to_ids, d.num_links);
-  s.lfo = unorientations(d.link_from_orients, d.num_links);
-  s.lto = unorientations(d.link_to_orients, d.num_links);
-  s.lnum = unzstd_u32(d.link_overlap_nums);
-  s.lop = unzstd_chars(d.link_overlap_ops);
+#pragma omp parallel sections num_threads(4)
+  {
+#pragma omp section
+    s.seg_seq = unzstd_str(d.segment_sequences);
+#pragma omp section
+    {
+      s.seg_len = unzstd_u32(d.segment_seq_lengths);
+      for (const auto &c : d.segment_optional) s.seg_opt.push_back(decompress_opt(c));
+      for (const auto &c : d.link_optional) s.link_opt.push_back(decompress_opt(c));
+    }
+#pragma omp section
+    {
+      s.lf = undelta_varint_u32(d.link_from_ids, d.num_links);
+      s.lt = undelta_varint_u32(d.link_to_ids, d.num_links);
+    }
+#pragma omp section
+    {
+      s.lfo = unorientations(d.link_from_orients, d.num_links);
+      s.lto = unorientations(d.link_to_orients, d.num_links);
+      s.lnum = unzstd_u32(d.link_overlap_nums);
+      s.lop = unzstd_chars(d.link_overlap_ops);
+    }
+  }
   if (d.num_jumps > 0) {
     s.jf = undelta_varint_u32(d.jump_from_ids, d.num_jumps);
     s.jt = undelta_varint_u32(d.jump_to_ids, d.num_jumps);
@@ -508,7 +524,12 @@ TextPieces walk_pieces(const std::vector<std::string> &samples, const std::vecto
 Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t threshold, int delta_round, int threads,
                           bool show_stats, const int32_t *d_steps) {
   const int nth = resolve_threads(threads);
-  set_zstd_threads(nth);
+  // zstd workers: the given thread count, or every host core when none is
+  // given.  The compressed bytes do not depend on the worker count (zstd's
+  // multithreaded mode cuts jobs by size; checked with the reference CLI
+  // at 1 to 16 workers), only the time does.
+  const int zw = threads > 0 ? nth : std::max<int>(nth, (int)std::max(1L, sysconf(_SC_NPROCESSORS_ONLN)));
+  set_zstd_threads(zw);
   Compressed out;
   out.header_line = g.header_line;
   if (delta_round < 0) {
@@ -581,13 +602,13 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   {
 #pragma omp section
     {
-      set_zstd_threads(nth);
+      set_zstd_threads(zw);
       out.rules_first = zstd_i32(first);
       out.rules_second = zstd_i32(second);
     }
 #pragma omp section
     {
-      set_zstd_threads(nth);
+      set_zstd_threads(zw);
       out.paths = zstd_i32(pflat);
       out.names = zstd_str(names_cat);
       out.name_lengths = zstd_u32(name_lens);
@@ -596,7 +617,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
     }
 #pragma omp section
     {
-      set_zstd_threads(nth);
+      set_zstd_threads(zw);
       if (nw) {
         std::vector<int32_t> wflat(enc.begin() + (ptrdiff_t)ep, enc.end());
         out.walk_lengths = lengths_of(gram.h_off, np, np + nw);
@@ -616,7 +637,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
     }
 #pragma omp section
     {
-      set_zstd_threads(nth);
+      set_zstd_threads(zw);
       out.segment_sequences = zstd_str(seg_cat);
       out.segment_seq_lengths = zstd_u32(seg_lens);
       out.num_links = g.link_from.size();
@@ -629,7 +650,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
     }
 #pragma omp section
     {
-      set_zstd_threads(nth);
+      set_zstd_threads(zw);
       for (const auto &c : g.segment_optional) out.segment_optional.push_back(compress_opt(c));
       for (const auto &c : g.link_optional) out.link_optional.push_back(compress_opt(c));
       if (!g.jump_from.empty()) {
@@ -733,10 +754,22 @@ struct LoadedStreams {
 };
 
 LoadedStreams load_all(Context &ctx, const Compressed &c, Grammar &g, const char *err_prefix) {
-  decode_rule_columns(ctx, c, g);
-  std::vector<int32_t> p, w;
-  if (!c.paths.payload.empty()) p = unzstd_i32(c.paths);
-  if (!c.walks.payload.empty()) w = unzstd_i32(c.walks);
+  // the four zstd frames decode in parallel
+  std::vector<int32_t> f, s, p, w;
+#pragma omp parallel sections num_threads(4)
+  {
+#pragma omp section
+    f = unzstd_i32(c.rules_first);
+#pragma omp section
+    s = unzstd_i32(c.rules_second);
+#pragma omp section
+    if (!c.paths.payload.empty()) p = unzstd_i32(c.paths);
+#pragma omp section
+    if (!c.walks.payload.empty()) w = unzstd_i32(c.walks);
+  }
+  if (f.size() != s.size()) throw std::runtime_error(std::string(kWriterErr) + "rule columns differ in length");
+  load_rules(ctx, g, f.data(), s.data(), f.size(), c.min_rule_id());
+  g.delta_round = c.delta_round;
   const std::vector<uint64_t> po = offsets_of(c.sequence_lengths), wo = offsets_of(c.walk_lengths);
   if (po.back() > p.size() || wo.back() > w.size())
     throw std::runtime_error(std::string(err_prefix) + "flattened sequence block is truncated");
