@@ -940,13 +940,17 @@ Graph decompress_graph(Context &ctx, const Compressed &c, int threads) {
   g.walk_seq_starts = unvarint_i64(c.walk_seq_starts, c.walk_lengths.size());
   g.walk_seq_ends = unvarint_i64(c.walk_seq_ends, c.walk_lengths.size());
   const StaticFields s = decode_static(c);
-  g.node_names.emplace_back();
-  g.node_sequences.emplace_back();
-  size_t sp = 0;
-  for (size_t i = 0; i < s.seg_len.size(); ++i) {
-    g.node_names.push_back(std::to_string(i + 1));
-    g.node_sequences.push_back(s.seg_seq.substr(sp, s.seg_len[i]));
-    sp += s.seg_len[i];
+  const size_t ns = s.seg_len.size();
+  std::vector<uint64_t> so(ns + 1, 0);
+  for (size_t i = 0; i < ns; ++i) so[i + 1] = so[i] + s.seg_len[i];
+  if (ns && so[ns - 1] > s.seg_seq.size())
+    throw std::runtime_error(std::string(kWriterErr) + "segment sequence column is truncated");
+  g.node_names.resize(ns + 1);
+  g.node_sequences.resize(ns + 1);
+#pragma omp parallel for schedule(static) num_threads(resolve_threads(threads))
+  for (int64_t i = 0; i < (int64_t)ns; ++i) {
+    g.node_names[i + 1] = std::to_string(i + 1);
+    g.node_sequences[i + 1] = s.seg_seq.substr(so[i], s.seg_len[i]);  // the last may run short
   }
   g.segment_optional = s.seg_opt;
   g.link_from = s.lf;
