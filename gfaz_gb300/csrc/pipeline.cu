@@ -56,7 +56,16 @@ uint64_t ceil_log2(uint64_t x) {
   return r;
 }
 
+
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
+
+// cap scaled down by 2^shift (up by 2^-shift when negative), kept within
+// [2^16, the table limit].
+uint64_t scale_cap(uint64_t cap, int shift) {
+  if (shift >= 0) return std::max<uint64_t>(shift < 63 ? cap >> shift : 0, 1u << 16);
+  const int up = std::min(-shift, 40);
+  return std::min<uint64_t>(cap << up, kMaxTableCap);
+}
 constexpr int kPassBatch = 4;  // level passes launched per status read (DevStatus::pass_open slots)
 static_assert(kPassBatch <= (int)(sizeof(DevStatus::pass_open) / sizeof(unsigned long long)), "pass slots");
 
@@ -419,15 +428,15 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     const int cls = (round == 0 ? 0 : 1) * 1000 + 4 * (int)ceil_log2(n) +
                     (round == 0 ? 0 : (int)std::min<uint64_t>(3, prev_distinct * 4 / std::max<uint64_t>(n, 1)));
     CountKernel kind = ctx.warp_dedup ? CountKernel::kTiledWarpDedup : CountKernel::kTiled;
-    // table size: the estimate's size shrunk by the factor the load-factor
-    // tuner kept for this class and round (tuned below, once the distinct
-    // pairs are known)
+    // table size: the estimate's size scaled by the power of two the
+    // load-factor tuner kept for this class and round (tuned below, once
+    // the distinct pairs are known; negative when the table had to grow)
     const int cap_cls = cls * 16 + std::min(round, 15);
     const uint64_t cap_default = cap;
     bool tune_cap = false;
     if (ctx.table_tuner && !forced_cap) {
       const auto it = ctx.tuned.find({Context::kTuneCap, cap_cls});
-      if (it != ctx.tuned.end()) cap = std::max<uint64_t>(cap >> it->second, 1u << 16);
+      if (it != ctx.tuned.end()) cap = scale_cap(cap, it->second);
       else tune_cap = true;
     }
     bool tune = false;
@@ -515,7 +524,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       if (debug_enabled())
         fprintf(stderr, "[gfaz gb300] load-factor tuner: class %d distinct=%llu table %llu -> %llu slots\n", cls,
                 (unsigned long long)distinct, (unsigned long long)cap, (unsigned long long)best);
-      ctx.record_tuned(Context::kTuneCap, cap_cls, (int)(ceil_log2(cap_default) - ceil_log2(best)));
+      ctx.record_tuned(Context::kTuneCap, cap_cls, (int)ceil_log2(cap_default) - (int)ceil_log2(best));
       cap = best;
       ctx.reset_status();
       if (last != best) {
@@ -785,11 +794,50 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
     est = std::min(est, n);
     uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
-    if (round == 0 && ctx.first_table_cap) cap = ctx.first_table_cap;
-    // the chunk with the step after it (pairs across chunk edges)
+    const bool forced_cap = round == 0 && ctx.first_table_cap;
+    if (forced_cap) cap = ctx.first_table_cap;
+    // the table size kept for this class and round (the resident rounds'
+    // tuner key), so that a table that had to grow does not refill again
+    const int cls = (round == 0 ? 0 : 1) * 1000 + 4 * (int)ceil_log2(n) +
+                    (round == 0 ? 0 : (int)std::min<uint64_t>(3, prev_distinct * 4 / std::max<uint64_t>(n, 1)));
+    const int cap_cls = cls * 16 + std::min(round, 15);
+    const uint64_t cap_default = cap;
+    bool keep_cap = false;
+    if (ctx.table_tuner && !forced_cap) {
+      const auto it = ctx.tuned.find({Context::kTuneCap, cap_cls});
+      if (it != ctx.tuned.end()) cap = scale_cap(cap, it->second);
+      else keep_cap = true;
+    }
+    // Input resident: when the round's input fits the budget beside the
+    // per-tile arrays and the table (with output chunks shrunk to the rest),
+    // it is uploaded once and the count, classification and emit passes
+    // read it in place instead of uploading every chunk three times.
+    uint64_t Cr = C;
+    // per-tile words and arrays, the table and its used bitmap, and a margin
+    const uint64_t fixed_n = n / 2 + n / 64 + 4 * n / 8 + (64ull << 20) + 17 * cap;
+    const bool in_res = budget && fixed_n + 4 * (n + 2) + 4 * 8 * TILE <= budget;
+    if (in_res) {
+      Cr = std::min(C, std::max<uint64_t>(TILE, (budget - fixed_n - 4 * (n + 2)) / 4 / TILE * TILE));
+      cin.release();
+      cout.release();
+      cout.resize(Cr);
+      A.resize(n + 1);
+      upload_range(cur, 0, n, A.ptr, st);
+    } else {
+      cin.resize(C + 2);
+      cout.resize(C);
+    }
+    // the chunk with the step after it (pairs across chunk edges); returns
+    // where it starts on the device and how many steps it holds
+    const int32_t *chunk_ptr = nullptr;
     auto load_chunk = [&](uint64_t c0, uint64_t c1) {
       const uint64_t e = std::min(c1 + 1, n);
-      upload_range(cur, c0, e, cin.ptr, st);
+      if (in_res) {
+        chunk_ptr = A.ptr + c0;
+      } else {
+        upload_range(cur, c0, e, cin.ptr, st);
+        chunk_ptr = cin.ptr;
+      }
       local_heads(offA.ptr, c0, c1 - c0);
       return e - c0;
     };
@@ -799,11 +847,11 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       tab.prepare(cap, st);
       ctx.reset_status();
-      for (uint64_t c0 = 0; c0 < n; c0 += C) {
-        const uint64_t c1 = std::min(c0 + C, n);
+      for (uint64_t c0 = 0; c0 < n; c0 += Cr) {
+        const uint64_t c1 = std::min(c0 + Cr, n);
         const uint64_t nd = load_chunk(c0, c1);
         GFZ_TIMED_B(ctx, "count_pairs", 4.0 * (c1 - c0),
-                    launch_count_pairs(cin.ptr, nd, hloc.ptr, tab.view(cap), ds, kind, st));
+                    launch_count_pairs(chunk_ptr, nd, hloc.ptr, tab.view(cap), ds, kind, st));
       }
       const DevStatus &s = ctx.read_status();
       distinct = s.u64[0];
@@ -815,6 +863,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       ctx.check_status("count_pairs");
       break;
     }
+    if (keep_cap) ctx.record_tuned(Context::kTuneCap, cap_cls, (int)ceil_log2(cap_default) - (int)ceil_log2(cap));
     prev_distinct = distinct;
     if (repeated == 0) break;
     if ((uint64_t)next_id + cap >= (1ULL << 31))
@@ -833,11 +882,11 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     uint32_t *counter;
     unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
     const ApplyScratch sc{rw.tword.ptr, rw.tile_agg.ptr, rw.tile_state.ptr, desc, counter};
-    for (uint64_t c0 = 0; c0 < n; c0 += C) {
-      const uint64_t c1 = std::min(c0 + C, n);
+    for (uint64_t c0 = 0; c0 < n; c0 += Cr) {
+      const uint64_t c1 = std::min(c0 + Cr, n);
       const uint64_t nd = load_chunk(c0, c1);
       GFZ_TIMED_B(ctx, "apply_classify", 4.0 * (c1 - c0),
-                  launch_classify_chunk(cin.ptr, c1 - c0, nd, hloc.ptr, tab.view(cap), c0 / TILE, sc, ds, st));
+                  launch_classify_chunk(chunk_ptr, c1 - c0, nd, hloc.ptr, tab.view(cap), c0 / TILE, sc, ds, st));
     }
     GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
     GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, rw.tile_trav.ptr, st));
@@ -854,12 +903,12 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       const unsigned long long stt = h_state[c0 / TILE];
       return c0 - (uint64_t)(stt >> 1) + (uint64_t)(stt & 1u);
     };
-    for (uint64_t c0 = 0; c0 < n; c0 += C) {
-      const uint64_t c1 = std::min(c0 + C, n);
+    for (uint64_t c0 = 0; c0 < n; c0 += Cr) {
+      const uint64_t c1 = std::min(c0 + Cr, n);
       load_chunk(c0, c1);
       const uint64_t o0 = out_start(c0);
       GFZ_TIMED_B(ctx, "apply_emit", 4.0 * (c1 - c0),
-                  launch_emit_chunk(cin.ptr, c0, c0 / TILE, apply_num_tiles(c1 - c0), n, offA.ptr, ntrav,
+                  launch_emit_chunk(chunk_ptr, c0, c0 / TILE, apply_num_tiles(c1 - c0), n, offA.ptr, ntrav,
                                     rw.tile_trav.ptr, tab.view(cap), temp_base, cout.ptr, o0, offB.ptr,
                                     used_bits.ptr, sc, ds, st));
       if (c1 < n) {
@@ -890,9 +939,10 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     for (int b = 0; b < 8; ++b)
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
     sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
+    if (in_res) A.release();
     // final ids into the round's output, chunk by chunk
-    for (uint64_t o0 = 0; o0 < n_out; o0 += C) {
-      const uint64_t o1 = std::min(o0 + C, n_out);
+    for (uint64_t o0 = 0; o0 < n_out; o0 += Cr) {
+      const uint64_t o1 = std::min(o0 + Cr, n_out);
       cuda_check(cudaMemcpyAsync(cout.ptr, nxt + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
                  "chunk upload");
       GFZ_TIMED_B(ctx, "remap", 8.0 * (o1 - o0), launch_remap(cout.ptr, o1 - o0, temp_base, tab.slots.ptr, st));
@@ -902,8 +952,9 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     ctx.read_status();
     ctx.check_status("rule sort");
     if (debug_enabled())
-      fprintf(stderr, "[gfaz gb300] chunked round %d: n=%llu chunk=%llu cap=%llu distinct=%llu used=%llu n_out=%llu\n",
-              round + 1, (unsigned long long)n, (unsigned long long)C, (unsigned long long)cap,
+      fprintf(stderr, "[gfaz gb300] chunked round %d%s: n=%llu chunk=%llu cap=%llu distinct=%llu used=%llu n_out=%llu\n",
+              round + 1, in_res ? " (input resident)" : "", (unsigned long long)n, (unsigned long long)Cr,
+              (unsigned long long)cap,
               (unsigned long long)distinct, (unsigned long long)U, (unsigned long long)n_out);
     g.nrules += U;
     next_id += (uint32_t)U;
@@ -957,9 +1008,11 @@ void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vec
   uint64_t chunk = ctx.encode_chunk;
   if (!chunk && ctx.hbm_budget) {
     if (!resident_fits(ctx, N)) {
-      // chunked: per-tile words and tile arrays of the whole stream, a pair
-      // table, the final stream; chunk buffers of 12 bytes per step
-      const uint64_t fixed = N / 2 + N / 64 + 4 * N / 8 + (64ull << 20) + 16 * std::min<uint64_t>(N, 1ull << 24);
+      // chunked: per-tile words and tile arrays of the whole stream, the
+      // first round's pair table and used bitmap, the final stream; chunk
+      // buffers of 12 bytes per step
+      const uint64_t cap0 = next_pow2(std::max<uint64_t>(std::min<uint64_t>(N / 8, 1u << 22) * 2, 1u << 16));
+      const uint64_t fixed = N / 2 + N / 64 + 4 * N / 8 + (64ull << 20) + 17 * cap0;
       if (ctx.hbm_budget <= fixed + 12 * kApplyTile)
         throw std::runtime_error("HBM budget too small for " + std::to_string(N) + " steps");
       chunk = (ctx.hbm_budget - fixed) / 12;
