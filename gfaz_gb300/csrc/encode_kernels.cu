@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restr
       return;
     }
     const uint32_t len = (uint32_t)min((uint64_t)TILE, n - tile * TILE);
-    count_tile<ITEMS, DEDUP>(P.sv[b], P.hb[b], len, tab, status, c);
+    // pairs start at positions with a successor inside the stream (the head
+    // bitmap marks position n too, but a caller may pass a shorter n)
+    const uint32_t plen = tile * TILE + len < n ? len : len - 1;
+    count_tile<ITEMS, DEDUP>(P.sv[b], P.hb[b], plen, tab, status, c);
     pipe_release();
     if (!has_next) break;
     tile = next;
@@ -619,12 +622,14 @@ __global__ void __launch_bounds__(BLOCK, 4) k_apply_classify(const int32_t *__re
       return;
     }
     const uint32_t len = (uint32_t)min((uint64_t)TILE, n - tile * TILE);
+    // positions with a successor inside the stream (as in the count)
+    const uint32_t plen = tile * TILE + len < n ? len : len - 1;
     int32_t v[ITEMS + 1];
     thread_steps<ITEMS>(P.sv[b], j0, v);
     const uint32_t hd = bits_from(P.hb[b], j0);
     uint32_t validb = 0;
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) validb |= (uint32_t)(j0 + k < len && !((hd >> (k + 1)) & 1u)) << k;
+    for (int k = 0; k < ITEMS; ++k) validb |= (uint32_t)(j0 + k < plen && !((hd >> (k + 1)) & 1u)) << k;
     uint32_t slot[ITEMS], fl[ITEMS], fwdb;
     lookup_pairs<ITEMS>(v, validb, tab, slot, fl, fwdb, status);
     uint32_t cbits = 0;

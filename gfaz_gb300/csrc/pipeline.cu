@@ -130,6 +130,10 @@ Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullp
   std::memset(h_status_, 0, sizeof(DevStatus));
   cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
   counter_.resize(1);
+  if (const char *e = std::getenv("GFAZ_TUNE_STEPS")) {
+    const long long v = std::atoll(e);
+    if (v > 0) tune_steps = (uint64_t)v;
+  }
   // earlier tuner decisions: lines "kernel class variant" of GFAZ_TUNE_FILE
   if (const char *f = std::getenv("GFAZ_TUNE_FILE")) {
     if (FILE *fp = std::fopen(f, "r")) {
@@ -373,8 +377,10 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
     if (it != ctx.tuned.end()) {
       flat = it->second == 1;
     } else {
-      const float t_tiled = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, false, ds, st); });
-      const float t_flat = ctx.time_launches([&] { launch_apply_classify(A, n, heads, tab, sc, true, ds, st); });
+      // timed on the stream's first steps; the full pass follows
+      const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);
+      const float t_tiled = ctx.time_launches([&] { launch_apply_classify(A, ns, heads, tab, sc, false, ds, st); });
+      const float t_flat = ctx.time_launches([&] { launch_apply_classify(A, ns, heads, tab, sc, true, ds, st); });
       flat = t_flat < t_tiled;
       ctx.record_tuned(Context::kTuneClassify, cls, flat ? 1 : 0);
       if (debug_enabled())
@@ -450,15 +456,17 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       if (tune) {
-        // every candidate kernel counts into a cleared table; the last run's
-        // table is kept (all fill it alike)
+        // every candidate kernel counts the stream's first ctx.tune_steps
+        // steps (GFAZ_TUNE_STEPS) into a cleared table; the full count with
+        // the fastest follows
         const CountKernel cand[] = {CountKernel::kTiled, CountKernel::kFlat, CountKernel::kFlat4};
         float best = 0, t[3] = {0, 0, 0};
         bool refill = false;
+        const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);
         for (int i = 0; i < 3; ++i) {
           tab.prepare(cap, st);
           ctx.reset_status();
-          t[i] = ctx.time_launches([&] { launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, cand[i], st); });
+          t[i] = ctx.time_launches([&] { launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(cap), ds, cand[i], st); });
           const DevStatus &s0 = ctx.read_status();
           if ((s0.err & kErrTableFull) || s0.u64[0] * 10 > cap * 8) {
             refill = true;
@@ -476,8 +484,9 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
         ctx.record_tuned(Context::kTuneCount, cls, (int)kind);
         if (debug_enabled())
           fprintf(stderr, "[gfaz gb300] count tuner: class %d n=%llu tiled %.3f, flat %.3f, flat4 %.3f ms\n", cls,
-                  (unsigned long long)n, t[0], t[1], t[2]);
+                  (unsigned long long)ns, t[0], t[1], t[2]);
         tune = false;
+        continue;  // the full count
       } else {
         tab.prepare(cap, st);
         ctx.reset_status();
@@ -504,15 +513,15 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
         const uint64_t c = cap_default >> sh;
         if (c >= 2 * distinct && c >= (1u << 16) && c < cap) caps.push_back(c);
       }
-      uint64_t best = cap, last = cap;
+      uint64_t best = cap;
       float tbest = -1;
+      const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);  // timed on the stream's first steps
       for (const uint64_t c : caps) {
         ctx.reset_status();
         const float t = ctx.time_launches([&] {
           tab.prepare(c, st);
-          launch_count_pairs(A.ptr, n, heads.ptr, tab.view(c), ds, kind, st);
+          launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(c), ds, kind, st);
         });
-        last = c;
         // a probe chain past its limit at this load: not a candidate (the
         // next reset clears the bit)
         if (ctx.read_status().err & kErrTableFull) continue;
@@ -526,14 +535,12 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
                 (unsigned long long)distinct, (unsigned long long)cap, (unsigned long long)best);
       ctx.record_tuned(Context::kTuneCap, cap_cls, (int)ceil_log2(cap_default) - (int)ceil_log2(best));
       cap = best;
+      // the timed runs cleared the table: the full count at the kept size
+      tab.prepare(cap, st);
       ctx.reset_status();
-      if (last != best) {
-        tab.prepare(cap, st);
-        GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
-                    launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
-        ctx.read_status();
-        ctx.check_status("count_pairs");
-      }
+      GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n, launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
+      ctx.read_status();
+      ctx.check_status("count_pairs");
     }
     prev_distinct = distinct;
     if (repeated == 0) break;  // no candidates: stop all rounds

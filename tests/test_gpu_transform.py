@@ -221,3 +221,20 @@ def test_tuner_decisions_file(tmp_path, monkeypatch, gpu_ctx):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
     assert f.read_text().count("\n") == len(rows)  # nothing new to decide
+
+
+def test_tuners_on_a_prefix(monkeypatch):
+    """The tuners time their candidates on the stream's first steps
+    (GFAZ_TUNE_STEPS); with a prefix far shorter than every round's stream
+    the grammar is unchanged (the timed runs must not read past the prefix
+    or leave their table or status behind)."""
+    steps, off, _ = synthetic.cfg2_stream(seed=6, n_segments=120_000, n_paths=5)
+    want = gz.encode(steps, off, ctx=gz.Context(0)).arrays()
+    monkeypatch.setenv("GFAZ_TUNE_STEPS", "5000")
+    for opt in (None, ("count_kernel", 0), ("classify_kernel", 0)):
+        ctx = gz.Context(0)
+        if opt:
+            ctx.set_option(*opt)
+        got = gz.encode(steps, off, ctx=ctx).arrays()
+        for x, y in zip(got, want):
+            np.testing.assert_array_equal(x, y)
