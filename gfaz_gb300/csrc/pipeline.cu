@@ -50,6 +50,14 @@ uint64_t next_pow2(uint64_t x) {
   return c;
 }
 
+// Steps the tuners time their candidates on: the whole stream up to 2^29
+// steps (short runs time unreliably), else its first 2^27 steps;
+// GFAZ_TUNE_STEPS sets the prefix for every length.
+uint64_t tune_len(const Context &ctx, uint64_t n) {
+  if (ctx.tune_steps) return std::min(n, ctx.tune_steps);
+  return n <= (1ull << 29) ? n : (1ull << 27);
+}
+
 uint64_t ceil_log2(uint64_t x) {
   uint64_t r = 0;
   while ((1ull << r) < x) ++r;
@@ -378,7 +386,7 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
       flat = it->second == 1;
     } else {
       // timed on the stream's first steps; the full pass follows
-      const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);
+      const uint64_t ns = tune_len(ctx, n);
       const float t_tiled = ctx.time_launches([&] { launch_apply_classify(A, ns, heads, tab, sc, false, ds, st); });
       const float t_flat = ctx.time_launches([&] { launch_apply_classify(A, ns, heads, tab, sc, true, ds, st); });
       flat = t_flat < t_tiled;
@@ -456,13 +464,12 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       if (tune) {
-        // every candidate kernel counts the stream's first ctx.tune_steps
-        // steps (GFAZ_TUNE_STEPS) into a cleared table; the full count with
-        // the fastest follows
+        // every candidate kernel counts the stream's first tune_len steps
+        // into a cleared table; the full count with the fastest follows
         const CountKernel cand[] = {CountKernel::kTiled, CountKernel::kFlat, CountKernel::kFlat4};
         float best = 0, t[3] = {0, 0, 0};
         bool refill = false;
-        const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);
+        const uint64_t ns = tune_len(ctx, n);
         for (int i = 0; i < 3; ++i) {
           tab.prepare(cap, st);
           ctx.reset_status();
@@ -515,7 +522,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       }
       uint64_t best = cap;
       float tbest = -1;
-      const uint64_t ns = std::min<uint64_t>(n, ctx.tune_steps);  // timed on the stream's first steps
+      const uint64_t ns = tune_len(ctx, n);  // timed on the stream's first steps
       for (const uint64_t c : caps) {
         ctx.reset_status();
         const float t = ctx.time_launches([&] {

@@ -143,7 +143,7 @@ class Context {
   // distinct-pair estimate gives, per class and round
   enum TunedKernel { kTuneCount = 0, kTuneClassify = 1, kTuneCap = 2 };
   bool table_tuner = true;  // pair-table size (hash load factor) tuned per stream class
-  uint64_t tune_steps = 1ull << 25;  // the tuners time candidates on this many leading steps
+  uint64_t tune_steps = 0;  // tuners' timing prefix (GFAZ_TUNE_STEPS); 0 = by stream length
   std::map<std::pair<int, int>, int> tuned;
   void record_tuned(int kernel, int cls, int variant);
   // Launches on this context's stream and returns their device time (ms).
