@@ -37,27 +37,43 @@ __global__ void __launch_bounds__(kGB) k_cover_bits(const int32_t *__restrict__ 
        p0 += (uint64_t)gridDim.x * blockDim.x * kGItems) {
     uint64_t t = trav_at(off, ntrav, p0), tend = off[t + 1];
     uint32_t g = gid[t];
-    uint64_t last = ~0ull;  // row word and group of the previous step
+    // row word and bit of every step (want: bit k = the step needs its bit);
+    // a step repeating the previous step's node and group is skipped
+    uint64_t idx[kGItems];
+    unsigned long long bit[kGItems];
+    uint32_t want = 0;
+    uint64_t last = ~0ull;
     uint32_t lastg = 0;
-    const uint64_t pe = p0 + kGItems < n ? p0 + kGItems : n;
-    for (uint64_t p = p0; p < pe; ++p) {
-      while (p >= tend) {
-        ++t;
-        tend = off[t + 1];
-        g = gid[t];
+#pragma unroll
+    for (int k = 0; k < kGItems; ++k) {
+      const uint64_t p = p0 + k;
+      idx[k] = 0;
+      bit[k] = 0;
+      if (p < n) {
+        while (p >= tend) {
+          ++t;
+          tend = off[t + 1];
+          g = gid[t];
+        }
+        const uint32_t w = g >> 6;
+        const int32_t v = x[p];
+        const uint32_t a = v < 0 ? 0u - (uint32_t)v : (uint32_t)v;
+        if (w >= w0 && w < w1 && a != 0 && a <= num_nodes) {
+          idx[k] = (uint64_t)a * stride + (w - w0);
+          bit[k] = 1ull << (g & 63);
+          if (!(idx[k] == last && g == lastg)) want |= 1u << k;
+          last = idx[k];
+          lastg = g;
+        }
       }
-      const uint32_t w = g >> 6;
-      if (w < w0 || w >= w1) continue;
-      const int32_t v = x[p];
-      const uint32_t a = v < 0 ? 0u - (uint32_t)v : (uint32_t)v;
-      if (a == 0 || a > num_nodes) continue;
-      const uint64_t idx = (uint64_t)a * stride + (w - w0);
-      const unsigned long long bit = 1ull << (g & 63);
-      if (idx == last && g == lastg) continue;  // the same node again in the same group
-      last = idx;
-      lastg = g;
-      if (!(bits[idx] & bit)) atomicOr(&bits[idx], bit);
     }
+    // all row loads in flight before any is resolved
+    unsigned long long cur[kGItems];
+#pragma unroll
+    for (int k = 0; k < kGItems; ++k) cur[k] = (want >> k) & 1u ? bits[idx[k]] : ~0ull;
+#pragma unroll
+    for (int k = 0; k < kGItems; ++k)
+      if (!(cur[k] & bit[k])) atomicOr(&bits[idx[k]], bit[k]);
   }
 }
 
