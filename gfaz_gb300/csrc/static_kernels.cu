@@ -8,11 +8,10 @@
 // float formatting) and passed as a blob.
 //
 // Work split: one thread per 16 output bytes, written with one 16-byte
-// store.  A block finds the lines of its first and last byte by binary
-// search over the line offsets; each thread then searches that short range
-// and walks forward through the lines its bytes touch, rebuilding the
-// line's head (the fields before the sequence / extra) in a small local
-// buffer.
+// store.  Each thread finds the line of its first byte by binary search
+// over the line offsets and walks forward through the lines its bytes
+// touch, rebuilding the line's head (the fields before the sequence /
+// extra) in a small local buffer.
 #include "common.cuh"
 #include "kernels.h"
 #include "text.cuh"
@@ -80,22 +79,11 @@ __global__ void k_static_len(StaticTextSource S, uint64_t *len) {
 
 __global__ void __launch_bounds__(kSB) k_static_write(StaticTextSource S, const uint64_t *__restrict__ loff,
                                                       uint64_t total, char *out) {
-  __shared__ uint64_t s_lo, s_hi;
-  const uint64_t b0 = (uint64_t)blockIdx.x * kSTile;
-  if (threadIdx.x == 0) {
-    s_lo = trav_of(loff, S.n, b0);
-    s_hi = trav_of(loff, S.n, (total < b0 + kSTile ? total : b0 + kSTile) - 1) + 1;
-  }
-  __syncthreads();
-  const uint64_t o = b0 + 16ull * threadIdx.x;
+  const uint64_t o = (uint64_t)blockIdx.x * kSTile + 16ull * threadIdx.x;
   if (o >= total) return;
-  // line of byte o within [s_lo, s_hi)
-  uint64_t lo = s_lo, hi = s_hi;
-  while (hi - lo > 1) {
-    const uint64_t mid = (lo + hi) >> 1;
-    if (loff[mid] <= o) lo = mid; else hi = mid;
-  }
-  uint64_t i = lo;
+  // line of byte o: every thread searches the offsets itself (the upper
+  // levels of the search are the same for the whole block and stay in L1)
+  uint64_t i = trav_of(loff, S.n, o);
   uint8_t h[48];
   uint32_t body, hl = line_head(S, i, h, body);
   uint64_t ls = loff[i], le = loff[i + 1];
