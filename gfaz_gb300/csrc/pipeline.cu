@@ -730,14 +730,60 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   // delta rounds (or the max |x| of the raw steps), chunk by chunk
   std::vector<HostSeg> cur = input;
   int32_t *nxt = X;
+  DevVec<int32_t> A(st), B(st);
+  // When round 1 will read its input in place (see the round loop; the
+  // same size rule), the last delta pass (or the max |x| pass) already
+  // leaves the stream in that buffer, so round 1 does not upload it again.
+  bool a_ready = false;
+  uint64_t Cr0 = C;
+  if (budget && dr <= 1 && resident_bytes(N, 0, 0) > budget) {
+    uint64_t cap0 = next_pow2(std::max<uint64_t>(std::min<uint64_t>(N / 8, 1u << 22) * 2, 1u << 16));
+    if (ctx.first_table_cap) {
+      cap0 = ctx.first_table_cap;
+    } else if (ctx.table_tuner) {
+      const auto it = ctx.tuned.find({Context::kTuneCap, (4 * (int)ceil_log2(N)) * 16});
+      if (it != ctx.tuned.end()) cap0 = scale_cap(cap0, it->second);
+    }
+    const uint64_t fixed0 = N / 2 + N / 64 + 4 * N / 8 + (64ull << 20) + 17 * cap0;
+    if (fixed0 + 4 * (N + 2) + 4 * 8 * TILE <= budget) {
+      Cr0 = std::min(C, std::max<uint64_t>(TILE, (budget - fixed0 - 4 * (N + 2)) / 4 / TILE * TILE));
+      a_ready = true;
+      cin.release();
+      cout.release();
+      cin.resize(Cr0 + 2);
+      A.resize(N + 1);
+    }
+  }
   if (dr == 0) {
-    for (uint64_t c0 = 0; c0 < N; c0 += C) {
-      const uint64_t c1 = std::min(c0 + C, N);
-      upload_range(cur, c0, c1, cin.ptr, st);
-      GFZ_TIMED_B(ctx, "max_abs", 4.0 * (c1 - c0), launch_max_abs(cin.ptr, c1 - c0, &ds->aux, st));
+    const uint64_t Cd = a_ready ? Cr0 : C;
+    for (uint64_t c0 = 0; c0 < N; c0 += Cd) {
+      const uint64_t c1 = std::min(c0 + Cd, N);
+      int32_t *dst = a_ready ? A.ptr + c0 : cin.ptr;
+      upload_range(cur, c0, c1, dst, st);
+      GFZ_TIMED_B(ctx, "max_abs", 4.0 * (c1 - c0), launch_max_abs(dst, c1 - c0, &ds->aux, st));
     }
   }
   for (int r = 0; r < dr; ++r) {
+    if (a_ready) {  // dr == 1: the output goes to the round-1 buffer and to host memory
+      for (uint64_t c0 = 0; c0 < N; c0 += Cr0) {
+        const uint64_t c1 = std::min(c0 + Cr0, N);
+        if (c0) {
+          upload_range(cur, c0 - 1, c1, cin.ptr, st);
+        } else {
+          cuda_check(cudaMemsetAsync(cin.ptr, 0, sizeof(int32_t), st), "chunk clear");
+          upload_range(cur, 0, c1, cin.ptr + 1, st);
+        }
+        local_heads(offA.ptr, c0, c1 - c0);
+        GFZ_TIMED_B(ctx, "delta_encode", 8.0 * (c1 - c0),
+                    launch_delta_chunk(cin.ptr, A.ptr + c0, c1 - c0, hloc.ptr, &ds->aux, st));
+        cuda_check(cudaMemcpyAsync(nxt + c0, A.ptr + c0, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                   "chunk download");
+      }
+      cuda_check(cudaStreamSynchronize(st), "stream sync");
+      cur = {HostSeg{nxt, N}};
+      nxt = nxt == X ? Y : X;
+      continue;
+    }
     for (uint64_t c0 = 0; c0 < N; c0 += C) {
       const uint64_t c1 = std::min(c0 + C, N);
       if (c0) {
@@ -781,7 +827,6 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   std::vector<unsigned long long> h_state;
   uint64_t n = N;
   uint64_t prev_distinct = 0;
-  DevVec<int32_t> A(st), B(st);
   bool resident = false;  // the remaining rounds ran on a device-resident stream
   for (int round = 0; round < p.rounds; ++round) {
     if (n < 2) break;
@@ -835,9 +880,12 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       cin.release();
       cout.release();
       cout.resize(Cr);
-      A.resize(n + 1);
-      upload_range(cur, 0, n, A.ptr, st);
+      if (!(a_ready && round == 0)) {
+        A.resize(n + 1);
+        upload_range(cur, 0, n, A.ptr, st);
+      }
     } else {
+      if (a_ready && round == 0) A.release();  // the host copy serves
       cin.resize(C + 2);
       cout.resize(C);
     }

@@ -66,22 +66,23 @@ def test_budget_selects_chunks(gpu_ctx):
         gz.encode(steps, off, ctx=ctx)
 
 
-@pytest.mark.parametrize("seed", [8, 9])
-def test_budget_input_resident(seed, gpu_ctx):
+@pytest.mark.parametrize("seed,delta_round", [(8, 1), (9, 1), (8, 0), (9, 2)])
+def test_budget_input_resident(seed, delta_round, gpu_ctx):
     """A budget with room for the round's input beside the per-tile arrays
-    and the table, but not for resident compression: round 1 reads its
-    input in place (output chunks to host memory), later rounds run
-    resident; the grammar is the resident one."""
+    and the table, but not for resident compression: the delta pass (or
+    the max |x| pass) leaves round 1's input on the device when it can,
+    round 1 reads it in place (output chunks to host memory), later rounds
+    run resident; the grammar is the resident one."""
     steps, off, _ = synthetic.cfg2_stream(seed=seed, n_segments=400_000, n_paths=6)
     n = len(steps)
     assert n < (1 << 24)
-    want = gz.encode(steps, off, ctx=gpu_ctx)
+    want = gz.encode(steps, off, delta_round=delta_round, ctx=gpu_ctx)
     ctx = gz.Context(0)
     # fixed part (per-tile words and arrays) ~1 B/step + the first round's
     # table + 64 MB; the input adds 4 B/step; resident rounds need ~12.7
     # B/step + 64 MB and more
     ctx.set_option("hbm_budget", 8 * n + (74 << 20))
-    _same(gz.encode(steps, off, ctx=ctx), want)
+    _same(gz.encode(steps, off, delta_round=delta_round, ctx=ctx), want)
 
 
 def test_chunked_container_bytes(tmp_path, gpu_ctx):
