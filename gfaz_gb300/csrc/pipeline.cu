@@ -735,6 +735,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   // same size rule), the last delta pass (or the max |x| pass) already
   // leaves the stream in that buffer, so round 1 does not upload it again.
   bool a_ready = false;
+  bool dev_next = false;  // the current stream is on the device in B (final ids)
   uint64_t Cr0 = C;
   if (budget && dr <= 1 && resident_bytes(N, 0, 0) > budget) {
     uint64_t cap0 = next_pow2(std::max<uint64_t>(std::min<uint64_t>(N / 8, 1u << 22) * 2, 1u << 16));
@@ -830,7 +831,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   bool resident = false;  // the remaining rounds ran on a device-resident stream
   for (int round = 0; round < p.rounds; ++round) {
     if (n < 2) break;
-    if (budget && resident_bytes(n, prev_distinct, g.nrules) <= budget) {
+    if (dev_next || (budget && resident_bytes(n, prev_distinct, g.nrules) <= budget)) {
       // the rest fits the budget: one upload, then the resident rounds
       cin.release();
       cout.release();
@@ -840,9 +841,15 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       rw.tile_agg.release();
       rw.tile_state.release();
       rw.tile_trav.release();
-      A.resize(std::max<uint64_t>(n, 1));
-      B.resize(std::max<uint64_t>(n, 1));
-      upload_range(cur, 0, n, A.ptr, st);
+      if (dev_next) {  // the previous round left the stream on the device
+        A.swap(B);
+        B.resize(std::max<uint64_t>(n, 1));
+      } else {
+        A.resize(std::max<uint64_t>(n, 1));
+        B.resize(std::max<uint64_t>(n, 1));
+        upload_range(cur, 0, n, A.ptr, st);
+      }
+      dev_next = false;
       phase("upload for the resident rounds");
       run_rounds(ctx, A, B, offA, offB, ntrav, n, next_id, prev_distinct, round, p.rounds, rules, g);
       cuda_check(cudaStreamSynchronize(st), "stream sync");
@@ -1002,14 +1009,27 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
     sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
     if (in_res) A.release();
-    // final ids into the round's output, chunk by chunk
-    for (uint64_t o0 = 0; o0 < n_out; o0 += Cr) {
-      const uint64_t o1 = std::min(o0 + Cr, n_out);
-      cuda_check(cudaMemcpyAsync(cout.ptr, nxt + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
-                 "chunk upload");
-      GFZ_TIMED_B(ctx, "remap", 8.0 * (o1 - o0), launch_remap(cout.ptr, o1 - o0, temp_base, tab.slots.ptr, st));
-      cuda_check(cudaMemcpyAsync(nxt + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
-                 "chunk download");
+    // final ids into the round's output: when the next round runs resident,
+    // the output goes up once and is remapped in place for it; otherwise
+    // chunk by chunk through host memory
+    dev_next = budget && resident_bytes(n_out, distinct, g.nrules + U) <= budget;
+    if (dev_next) {
+      cin.release();
+      cout.release();
+      used_bits.release();
+      B.resize(std::max<uint64_t>(n_out, 1));
+      if (n_out)
+        cuda_check(cudaMemcpyAsync(B.ptr, nxt, n_out * sizeof(int32_t), cudaMemcpyDefault, st), "stream upload");
+      GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
+    } else {
+      for (uint64_t o0 = 0; o0 < n_out; o0 += Cr) {
+        const uint64_t o1 = std::min(o0 + Cr, n_out);
+        cuda_check(cudaMemcpyAsync(cout.ptr, nxt + o0, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                   "chunk upload");
+        GFZ_TIMED_B(ctx, "remap", 8.0 * (o1 - o0), launch_remap(cout.ptr, o1 - o0, temp_base, tab.slots.ptr, st));
+        cuda_check(cudaMemcpyAsync(nxt + o0, cout.ptr, (o1 - o0) * sizeof(int32_t), cudaMemcpyDefault, st),
+                   "chunk download");
+      }
     }
     ctx.read_status();
     ctx.check_status("rule sort");
@@ -1031,6 +1051,9 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   if (resident) {
     A.size = n;
     g.enc = std::move(A);
+  } else if (dev_next) {  // the last round's output, remapped on the device
+    B.size = n;
+    g.enc = std::move(B);
   } else {
     g.enc.resize(std::max<uint64_t>(n, 1));
     g.enc.size = n;
