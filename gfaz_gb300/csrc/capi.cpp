@@ -410,8 +410,9 @@ gfz_status gfz_growth(gfz_context *ctx, const gfz_compressed *c, int threads, in
     *hist = nullptr;
     *growth = nullptr;
     if (r.num_haplotypes) {
-      *hist = reinterpret_cast<uint64_t *>(dup_bytes(r.hist.data(), r.hist.size() * 8));
+      std::unique_ptr<char, decltype(&std::free)> hb(dup_bytes(r.hist.data(), r.hist.size() * 8), &std::free);
       *growth = reinterpret_cast<double *>(dup_bytes(r.growth.data(), r.growth.size() * 8));
+      *hist = reinterpret_cast<uint64_t *>(hb.release());
     }
   });
 }
@@ -429,14 +430,20 @@ gfz_status gfz_pav(gfz_context *ctx, const gfz_compressed *c, const char *bed_pa
     for (const auto &q : r.ranges)
       rs += q.chrom + "\t" + std::to_string(q.start) + "\t" + std::to_string(q.end) + "\t" + q.name + "\n";
     for (const auto &n : r.group_names) gs += n + "\n";
-    *ranges = dup_bytes(rs.data(), rs.size());
+    // every buffer first, so that a failed allocation leaves no output set
+    std::unique_ptr<char, decltype(&std::free)> rb(dup_bytes(rs.data(), rs.size()), &std::free);
+    std::unique_ptr<char, decltype(&std::free)> gb(dup_bytes(gs.data(), gs.size()), &std::free);
+    std::unique_ptr<char, decltype(&std::free)> db(dup_bytes(r.denominators.data(), r.denominators.size() * 8),
+                                                   &std::free);
+    char *nb = dup_bytes(r.numerators.data(), r.numerators.size() * 8);
+    *ranges = rb.release();
     *ranges_len = rs.size();
-    *groups = dup_bytes(gs.data(), gs.size());
+    *groups = gb.release();
     *groups_len = gs.size();
     *nranges = r.ranges.size();
     *ngroups = r.group_names.size();
-    *denominators = reinterpret_cast<uint64_t *>(dup_bytes(r.denominators.data(), r.denominators.size() * 8));
-    *numerators = reinterpret_cast<uint64_t *>(dup_bytes(r.numerators.data(), r.numerators.size() * 8));
+    *denominators = reinterpret_cast<uint64_t *>(db.release());
+    *numerators = reinterpret_cast<uint64_t *>(nb);
   });
 }
 
