@@ -732,9 +732,11 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   int32_t *nxt = X;
   DevVec<int32_t> A(st), B(st);
   // When round 1 will read its input in place (see the round loop; the
-  // same size rule), the last delta pass (or the max |x| pass) already
-  // leaves the stream in that buffer, so round 1 does not upload it again.
+  // same size rule, so it always does), the last delta pass (or the max
+  // |x| pass) already leaves the stream in that buffer: round 1 does not
+  // upload it again, and the stream never goes back to host memory.
   bool a_ready = false;
+  bool a_holds = false;  // A holds the current stream (round 1's input)
   bool dev_next = false;  // the current stream is on the device in B (final ids)
   uint64_t Cr0 = C;
   if (budget && dr <= 1 && resident_bytes(N, 0, 0) > budget) {
@@ -765,7 +767,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     }
   }
   for (int r = 0; r < dr; ++r) {
-    if (a_ready) {  // dr == 1: the output goes to the round-1 buffer and to host memory
+    if (a_ready) {  // dr == 1: the output goes to the round-1 buffer only
       for (uint64_t c0 = 0; c0 < N; c0 += Cr0) {
         const uint64_t c1 = std::min(c0 + Cr0, N);
         if (c0) {
@@ -777,12 +779,9 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
         local_heads(offA.ptr, c0, c1 - c0);
         GFZ_TIMED_B(ctx, "delta_encode", 8.0 * (c1 - c0),
                     launch_delta_chunk(cin.ptr, A.ptr + c0, c1 - c0, hloc.ptr, &ds->aux, st));
-        cuda_check(cudaMemcpyAsync(nxt + c0, A.ptr + c0, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
-                   "chunk download");
       }
       cuda_check(cudaStreamSynchronize(st), "stream sync");
-      cur = {HostSeg{nxt, N}};
-      nxt = nxt == X ? Y : X;
+      cur.clear();  // the stream is in A only
       continue;
     }
     for (uint64_t c0 = 0; c0 < N; c0 += C) {
@@ -803,6 +802,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     cur = {HostSeg{nxt, N}};
     nxt = nxt == X ? Y : X;
   }
+  a_holds = a_ready;
   const DevStatus &s0 = ctx.read_status();
   const uint32_t max_abs = s0.aux;
   if (max_abs == UINT32_MAX)
@@ -881,7 +881,8 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     uint64_t Cr = C;
     // per-tile words and arrays, the table and its used bitmap, and a margin
     const uint64_t fixed_n = n / 2 + n / 64 + 4 * n / 8 + (64ull << 20) + 17 * cap;
-    const bool in_res = budget && fixed_n + 4 * (n + 2) + 4 * 8 * TILE <= budget;
+    // (with a_ready, round 1 meets this rule: the same table size and sizes)
+    const bool in_res = (a_ready && round == 0) || (budget && fixed_n + 4 * (n + 2) + 4 * 8 * TILE <= budget);
     if (in_res) {
       Cr = std::min(C, std::max<uint64_t>(TILE, (budget - fixed_n - 4 * (n + 2)) / 4 / TILE * TILE));
       cin.release();
@@ -892,7 +893,6 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
         upload_range(cur, 0, n, A.ptr, st);
       }
     } else {
-      if (a_ready && round == 0) A.release();  // the host copy serves
       cin.resize(C + 2);
       cout.resize(C);
     }
@@ -1009,6 +1009,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       if ((diff >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
     sort_used_rules(ctx, tab.view(cap), U, byte_mask, next_id, su, rules, g.nrules);
     if (in_res) A.release();
+    a_holds = false;
     // final ids into the round's output: when the next round runs resident,
     // the output goes up once and is remapped in place for it; otherwise
     // chunk by chunk through host memory
@@ -1054,6 +1055,9 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   } else if (dev_next) {  // the last round's output, remapped on the device
     B.size = n;
     g.enc = std::move(B);
+  } else if (a_holds) {  // round 1 stopped before any output: its input
+    A.size = n;
+    g.enc = std::move(A);
   } else {
     g.enc.resize(std::max<uint64_t>(n, 1));
     g.enc.size = n;

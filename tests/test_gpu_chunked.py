@@ -85,6 +85,29 @@ def test_budget_input_resident(seed, delta_round, gpu_ctx):
     _same(gz.encode(steps, off, delta_round=delta_round, ctx=ctx), want)
 
 
+@pytest.mark.parametrize("delta_round", [0, 1])
+def test_budget_input_resident_no_repeats(delta_round, gpu_ctx):
+    """Round 1 reads its input in place and finds no repeated pair (every
+    traversal is [t+1, 2t+3], so no pair repeats raw or delta-coded): the
+    grammar has no rules and the stream is round 1's input, taken from the
+    device."""
+    T = 2_000_000
+    t = np.arange(T, dtype=np.int64)
+    steps = np.empty(2 * T, dtype=np.int32)
+    steps[0::2] = t + 1
+    steps[1::2] = 2 * t + 3
+    off = np.arange(0, 2 * T + 1, 2, dtype=np.uint64)
+    n = len(steps)
+    want = gz.encode(steps, off, delta_round=delta_round, ctx=gpu_ctx)
+    ctx = gz.Context(0)
+    ctx.set_option("hbm_budget", 8 * n + (74 << 20))
+    got = gz.encode(steps, off, delta_round=delta_round, ctx=ctx)
+    _same(got, want)
+    assert got.info()["num_rules"] == 0
+    x, _ = got.decode()
+    np.testing.assert_array_equal(x, steps)
+
+
 def test_chunked_container_bytes(tmp_path, gpu_ctx):
     src = os.path.join(GOLDEN, "cfg1_mini.gfa")
     a = gz.compress_file(src, ctx=gpu_ctx)
