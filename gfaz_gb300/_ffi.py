@@ -148,18 +148,39 @@ def check(status: int):
 
 
 COPY_PIECE = 1 << 30
+# Buffers of at least this many bytes are copied by several threads.
+PARALLEL_COPY = 64 << 20
+
+_new_bytes = ctypes.pythonapi.PyBytes_FromStringAndSize
+_new_bytes.restype = ctypes.py_object
+_new_bytes.argtypes = [ctypes.c_void_p, ctypes.c_ssize_t]
 
 
-def copy_bytes(ptr, n: int) -> bytes:
-    """n bytes at ptr.  ctypes.string_at takes its size as a C int, so
-    buffers above COPY_PIECE bytes are copied once through a memoryview of a
-    char array laid over them."""
+def copy_bytes(ptr, n: int, threads: int = 0) -> bytes:
+    """n bytes at ptr.  Small buffers go through ctypes.string_at (which
+    takes its size as a C int, hence COPY_PIECE).  Larger ones are copied
+    into a new, not yet initialised bytes object (PyBytes_FromStringAndSize
+    with no source), in pieces by `threads` threads (0: one per core, at
+    most 16); ctypes releases the GIL around each memmove, so the pieces
+    and the first touch of the new pages run in parallel."""
     if not n:
         return b""
     addr = ptr.value if isinstance(ptr, ctypes.c_void_p) else int(ptr)
-    if n <= COPY_PIECE:
+    if n <= COPY_PIECE and n < PARALLEL_COPY:
         return ctypes.string_at(addr, n)
-    return memoryview((ctypes.c_char * n).from_address(addr)).tobytes()
+    out = _new_bytes(None, n)
+    dst = ctypes.cast(ctypes.c_char_p(out), ctypes.c_void_p).value
+    nth = threads if threads > 0 else min(16, os.cpu_count() or 1)
+    piece = max(1 << 20, -(-n // max(nth, 1)))
+    piece = -(-piece // 4096) * 4096
+    spans = [(o, min(piece, n - o)) for o in range(0, n, piece)]
+    if len(spans) == 1:
+        ctypes.memmove(dst, addr, n)
+        return out
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=len(spans)) as pool:
+        list(pool.map(lambda sp: ctypes.memmove(dst + sp[0], addr + sp[0], sp[1]), spans))
+    return out
 
 
 def take_bytes(ptr: ctypes.c_void_p, n: int) -> bytes:

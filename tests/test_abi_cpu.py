@@ -100,3 +100,18 @@ def test_copy_bytes_in_pieces(monkeypatch):
     assert _ffi.copy_bytes(ctypes.addressof(buf), len(data)) == data
     assert _ffi.copy_bytes(ctypes.c_void_p(ctypes.addressof(buf)), 5) == data[:5]
     assert _ffi.copy_bytes(None, 0) == b""
+
+
+def test_copy_bytes_parallel():
+    """Large library buffers are copied by several threads into a fresh bytes
+    object; every piece split gives the same bytes, and the source is not
+    touched."""
+    import ctypes
+    from gfaz_gb300 import _ffi
+    rng = np.random.default_rng(5)
+    data = rng.integers(0, 256, (5 << 20) + 12345, dtype=np.uint8).tobytes()
+    buf = ctypes.create_string_buffer(data, len(data))
+    for threads in (1, 2, 3, 4, 7):
+        got = _ffi.copy_bytes(ctypes.addressof(buf), len(data), threads=threads)
+        assert type(got) is bytes and got == data
+    assert buf.raw == data
