@@ -9,7 +9,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <exception>
 #include <fstream>
+#include <future>
 #include <iomanip>
 #include <iostream>
 #include <limits>
@@ -867,22 +869,36 @@ void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out)
   const int nth = resolve_threads(threads);
   set_zstd_threads(nth);
   PhaseClock clk("gfa text");
-  const StaticFields s = decode_static(c);
-  clk.mark("static columns (zstd)");
+  // The static columns' zstd runs on its own host thread while the grammar
+  // loads and the P text is written on the device; that text waits in HBM
+  // until the H/S/L/J/C text before it is in place.  An error in the static
+  // columns is reported first, as when the steps ran one after the other.
+  std::future<StaticFields> fs = std::async(std::launch::async, [&c] { return decode_static(c); });
+  Grammar g(ctx.stream());
+  DevVec<char> text(ctx.stream());
+  LoadedStreams ls{};
+  uint64_t pn = 0;
+  std::exception_ptr dev_err;
+  try {
+    ls = load_all(ctx, c, g, kWriterErr);
+    clk.mark("rules + encoded streams (zstd, upload)");
+    if (ls.np) {
+      const auto names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
+      const auto ovs = split_strings(unzstd_str(c.overlaps), unzstd_u32(c.overlap_lengths), true, kWriterErr);
+      pn = decode_text(
+          ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0, text);
+      clk.mark("P text (device)");
+    }
+  } catch (...) {
+    dev_err = std::current_exception();
+  }
+  const StaticFields s = fs.get();
+  if (dev_err) std::rethrow_exception(dev_err);
+  clk.mark("static columns (zstd, overlapped)");
   out.append(ctx.static_text ? static_text_device(ctx, c, s, nth) : static_text(c, s));
   clk.mark("H/S/L/J/C text");
-  Grammar g(ctx.stream());
-  const LoadedStreams ls = load_all(ctx, c, g, kWriterErr);
-  clk.mark("rules + encoded streams (zstd, upload)");
-  DevVec<char> text(ctx.stream());
   if (ls.np) {
-    const auto names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
-    const auto ovs = split_strings(unzstd_str(c.overlaps), unzstd_u32(c.overlap_lengths), true, kWriterErr);
-    const std::vector<uint64_t> off(g.h_off.begin(), g.h_off.begin() + (ptrdiff_t)ls.np + 1);
-    const uint64_t n = decode_text(
-        ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0, text);
-    clk.mark("P text (device)");
-    download_raw(ctx, text.ptr, n, out.grow(n), nth);
+    download_raw(ctx, text.ptr, pn, out.grow(pn), nth);
     clk.mark("P text download");
   }
   if (ls.nw) {
