@@ -553,6 +553,35 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   for (uint64_t t = 0; t < nw; ++t) off[np + t + 1] = NP + g.walks.offsets[t + 1];
   cudaStream_t st = ctx.stream();
   PhaseClock clk("compress");
+  // The segment columns hold segments 1 .. min(S, next_id - 1)
+  // (compression_utils.cpp:81-101), where next_id is known only after the
+  // transform; it is S unless the stream's ids stay below S.  Their zstd
+  // (the largest column) starts for S on a host thread while the transform
+  // runs, and is redone for the smaller count in the other case.
+  struct SegColumns {
+    Block seq, lens;
+    size_t ns = 0;
+  };
+  auto seg_columns = [&g, nth, zw](size_t ns) {
+    set_zstd_threads(zw);
+    SegColumns r;
+    r.ns = ns;
+    std::vector<uint32_t> lens(ns);
+    std::vector<uint64_t> so(ns + 1, 0);
+    for (size_t i = 0; i < ns; ++i) {
+      lens[i] = (uint32_t)g.node_sequences[i + 1].size();
+      so[i + 1] = so[i] + g.node_sequences[i + 1].size();
+    }
+    std::string cat(so[ns], '\0');
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int64_t i = 0; i < (int64_t)ns; ++i)
+      std::memcpy(&cat[so[i]], g.node_sequences[i + 1].data(), g.node_sequences[i + 1].size());
+    r.seq = zstd_str(cat);
+    r.lens = zstd_u32(lens);
+    return r;
+  };
+  const size_t S = g.node_sequences.empty() ? 0 : g.node_sequences.size() - 1;
+  std::future<SegColumns> fseg = std::async(std::launch::async, seg_columns, S);
   Grammar gram(st);
   if (d_steps)
     encode_traversals(ctx, d_steps, off, EncodeParams{rounds, delta_round}, gram);
@@ -579,25 +608,11 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
   const uint64_t ep = gram.h_off[np];
   out.sequence_lengths = lengths_of(gram.h_off, 0, np);
   std::vector<int32_t> pflat(enc.begin(), enc.begin() + (ptrdiff_t)ep);
-  std::string names_cat, ov_cat, seg_cat;
-  std::vector<uint32_t> name_lens, ov_lens, seg_lens;
+  std::string names_cat, ov_cat;
+  std::vector<uint32_t> name_lens, ov_lens;
   join_strings(g.path_names, names_cat, name_lens);
   join_strings(g.path_overlaps, ov_cat, ov_lens);
-  // segments 1 .. min(S, next_id - 1) (compression_utils.cpp:81-101),
-  // concatenated in parallel from their offsets
-  {
-    const size_t ns = g.node_sequences.empty() ? 0 : std::min<size_t>(g.node_sequences.size() - 1, gram.next_id - 1);
-    seg_lens.resize(ns);
-    std::vector<uint64_t> so(ns + 1, 0);
-    for (size_t i = 0; i < ns; ++i) {
-      seg_lens[i] = (uint32_t)g.node_sequences[i + 1].size();
-      so[i + 1] = so[i] + g.node_sequences[i + 1].size();
-    }
-    seg_cat.resize(so[ns]);
-#pragma omp parallel for schedule(static) num_threads(nth)
-    for (int64_t i = 0; i < (int64_t)ns; ++i)
-      std::memcpy(&seg_cat[so[i]], g.node_sequences[i + 1].data(), g.node_sequences[i + 1].size());
-  }
+  const size_t ns = std::min<size_t>(S, gram.next_id - 1);
   clk.mark("host columns");
 
 #pragma omp parallel sections num_threads(std::min(nth, 8))
@@ -640,8 +655,6 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
 #pragma omp section
     {
       set_zstd_threads(zw);
-      out.segment_sequences = zstd_str(seg_cat);
-      out.segment_seq_lengths = zstd_u32(seg_lens);
       out.num_links = g.link_from.size();
       out.link_from_ids = delta_varint_u32(g.link_from);
       out.link_to_ids = delta_varint_u32(g.link_to);
@@ -688,6 +701,10 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
       }
     }
   }
+  SegColumns sc = fseg.get();
+  if (sc.ns != ns) sc = seg_columns(ns);
+  out.segment_sequences = std::move(sc.seq);
+  out.segment_seq_lengths = std::move(sc.lens);
   clk.mark("zstd of every column");
   if (show_stats) {
     std::cerr << "\n=== Compressed Data Breakdown ===\n"
@@ -695,7 +712,7 @@ Compressed compress_graph(Context &ctx, const Graph &g, int rounds, uint64_t thr
               << "  rules_first_zstd:       " << out.rules_first.payload.size() << " B\n"
               << "  rules_second_zstd:      " << out.rules_second.payload.size() << " B\n"
               << "Paths (P-lines): " << np << "\n  paths_zstd:             " << out.paths.payload.size() << " B\n"
-              << "Segments (S-lines): " << seg_lens.size() << "\nLinks (L-lines): " << out.num_links << "\n";
+              << "Segments (S-lines): " << ns << "\nLinks (L-lines): " << out.num_links << "\n";
     if (nw) std::cerr << "Walks (W-lines): " << nw << "\n  walks_zstd:             " << out.walks.payload.size() << " B\n";
   }
   return out;
