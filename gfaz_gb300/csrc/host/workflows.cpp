@@ -952,6 +952,9 @@ Graph decompress_graph(Context &ctx, const Compressed &c, int threads) {
   set_zstd_threads(resolve_threads(threads));
   Graph g;
   g.header_line = c.header_line;
+  // the static columns' zstd runs on its own host thread while the
+  // traversals decode; its errors are raised at the same point as before
+  std::future<StaticFields> fs = std::async(std::launch::async, [&c] { return decode_static(c); });
   Grammar gram(ctx.stream());
   const LoadedStreams ls = load_all(ctx, c, gram, kWriterErr);
   auto fetch = [&](uint64_t t0, uint64_t t1, Traversals &tv) {
@@ -972,7 +975,7 @@ Graph decompress_graph(Context &ctx, const Compressed &c, int threads) {
   g.walk_seq_ids = split_strings(unzstd_str(c.walk_seq_ids), unzstd_u32(c.walk_seq_id_lengths), false, "");
   g.walk_seq_starts = unvarint_i64(c.walk_seq_starts, c.walk_lengths.size());
   g.walk_seq_ends = unvarint_i64(c.walk_seq_ends, c.walk_lengths.size());
-  const StaticFields s = decode_static(c);
+  StaticFields s = fs.get();
   const size_t ns = s.seg_len.size();
   std::vector<uint64_t> so(ns + 1, 0);
   for (size_t i = 0; i < ns; ++i) so[i + 1] = so[i] + s.seg_len[i];
@@ -985,27 +988,27 @@ Graph decompress_graph(Context &ctx, const Compressed &c, int threads) {
     g.node_names[i + 1] = std::to_string(i + 1);
     g.node_sequences[i + 1] = s.seg_seq.substr(so[i], s.seg_len[i]);  // the last may run short
   }
-  g.segment_optional = s.seg_opt;
-  g.link_from = s.lf;
-  g.link_to = s.lt;
-  g.link_from_orients = s.lfo;
-  g.link_to_orients = s.lto;
-  g.link_overlap_nums = s.lnum;
-  g.link_overlap_ops = s.lop;
-  g.link_optional = s.link_opt;
-  g.jump_from = s.jf;
-  g.jump_to = s.jt;
-  g.jump_from_orients = s.jfo;
-  g.jump_to_orients = s.jto;
-  g.jump_distances = s.jdist;
-  g.jump_rest = s.jrest;
-  g.cont_container = s.cc;
-  g.cont_contained = s.cd;
-  g.cont_container_orients = s.cco;
-  g.cont_contained_orients = s.cdo;
-  g.cont_positions = s.cpos;
-  g.cont_overlaps = s.cov;
-  g.cont_rest = s.crest;
+  g.segment_optional = std::move(s.seg_opt);
+  g.link_from = std::move(s.lf);
+  g.link_to = std::move(s.lt);
+  g.link_from_orients = std::move(s.lfo);
+  g.link_to_orients = std::move(s.lto);
+  g.link_overlap_nums = std::move(s.lnum);
+  g.link_overlap_ops = std::move(s.lop);
+  g.link_optional = std::move(s.link_opt);
+  g.jump_from = std::move(s.jf);
+  g.jump_to = std::move(s.jt);
+  g.jump_from_orients = std::move(s.jfo);
+  g.jump_to_orients = std::move(s.jto);
+  g.jump_distances = std::move(s.jdist);
+  g.jump_rest = std::move(s.jrest);
+  g.cont_container = std::move(s.cc);
+  g.cont_contained = std::move(s.cd);
+  g.cont_container_orients = std::move(s.cco);
+  g.cont_contained_orients = std::move(s.cdo);
+  g.cont_positions = std::move(s.cpos);
+  g.cont_overlaps = std::move(s.cov);
+  g.cont_rest = std::move(s.crest);
   return g;
 }
 
