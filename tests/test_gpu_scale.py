@@ -1,6 +1,7 @@
 """Config-4 scale (3.6B steps, 4,320 W-lines): compression under a 24 GB
 HBM budget (chunked, the stream in host memory) gives the same grammar as
-the resident compression, and decoding it gives the input back exactly, so
+the resident compression, and both equal the oracle's (encoded stream,
+offsets, rulebook, id seeds), and decoding gives the input back exactly, so
 positions, offsets and tile indices hold past 2^31 steps (byte offsets past
 2^33).  The W text of the first and last lines equals the oracle's
 formatting."""
@@ -36,9 +37,17 @@ def test_cfg4_chunked_roundtrip(gpu_ctx):
     ctx.set_option("hbm_budget", 24 << 30)
     g = gz.encode(steps, off, ctx=ctx)
     ref = gz.encode(steps, off, ctx=gpu_ctx)
-    for x, y in zip(g.arrays(), ref.arrays()):
+    got = g.arrays()
+    for x, y in zip(got, ref.arrays()):
         np.testing.assert_array_equal(x, y)
     del ref
+    want = oracle.compress(steps, off, rounds=8, delta_round=1)
+    info = g.info()
+    assert (info["layer_start"], info["next_id"]) == (want["layer_start"], want["next_id"])
+    np.testing.assert_array_equal(got[1], want["enc_offsets"])
+    assert np.array_equal(got[0], want["encoded"]), "encoded stream differs from the oracle"
+    assert np.array_equal(got[2], want["rules"]), "rulebook differs from the oracle"
+    del got, want
     x, xoff = g.decode()
     np.testing.assert_array_equal(xoff, off)
     assert np.array_equal(x, steps)
