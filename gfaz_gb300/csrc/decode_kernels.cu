@@ -367,11 +367,14 @@ void launch_expand(const int32_t *enc, uint64_t m, const uint64_t *pos, const in
                                                                status);
 }
 
+static_assert((uint64_t)kBlock * kDeltaItems == kInverseDeltaTile, "inverse delta tile size");
+
+uint64_t inverse_delta_num_tiles(uint64_t n) { return (n + kInverseDeltaTile - 1) / kInverseDeltaTile; }
+
 void launch_inverse_delta(int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav, unsigned long long *desc,
                           uint32_t *tile_counter, DevStatus *status, cudaStream_t st) {
   if (!n) return;
-  constexpr uint64_t TILE = kBlock * kDeltaItems;
-  k_inverse_delta<kBlock, kDeltaItems><<<(unsigned)((n + TILE - 1) / TILE), kBlock, 0, st>>>(
+  k_inverse_delta<kBlock, kDeltaItems><<<(unsigned)inverse_delta_num_tiles(n), kBlock, 0, st>>>(
       x, n, off, ntrav, desc, tile_counter, status);
 }
 

@@ -176,6 +176,10 @@ void launch_expand(const int32_t *enc, uint64_t m, const uint64_t *pos, const in
                    const int32_t *second, uint64_t nrules, uint32_t min_id, int32_t *out, DevStatus *status,
                    cudaStream_t st);
 // In-place inclusive prefix sum inside every traversal (inverse delta).
+// It tiles the stream by kInverseDeltaTile steps and needs one look-back
+// descriptor per tile: inverse_delta_num_tiles(n) of them.
+constexpr uint64_t kInverseDeltaTile = 4096;
+uint64_t inverse_delta_num_tiles(uint64_t n);
 void launch_inverse_delta(int32_t *x, uint64_t n, const uint64_t *off, uint64_t ntrav,
                           unsigned long long *desc, uint32_t *tile_counter, DevStatus *status,
                           cudaStream_t st);

@@ -11,12 +11,12 @@
 // want the decode step to touch nothing else.
 //
 // The scratch (status word, tile counter, one look-back descriptor per
-// 4096-step tile) is a file-scope __device__ array of kScratchBytes.  Every
-// GPU that loads this library holds it until the process exits.  All calls on
-// a device share it and it keeps the last call's contents, so each call
-// clears what must start at zero; two calls whose GPU work overlaps (calls
-// from different host threads, on any streams of the same device) race on it
-// and must be serialised by the caller.
+// 4096-step tile of the inverse-delta kernel) is a file-scope __device__
+// array of kScratchBytes.  Every GPU that loads this library holds it until
+// the process exits.  All calls on a device share it and it keeps the last
+// call's contents, so each call clears what must start at zero; two calls
+// whose GPU work overlaps (calls from different host threads, on any streams
+// of the same device) race on it and must be serialised by the caller.
 #include "noalloc.h"
 
 #include <mutex>
@@ -31,10 +31,13 @@ namespace gfz {
 
 namespace {
 
-constexpr uint64_t kMaxTiles = 16384;          // look-back descriptors
+// One look-back descriptor per inverse-delta tile of the largest stream.
+constexpr uint64_t kMaxTiles = kNoAllocMaxSteps / kInverseDeltaTile;
+static_assert(kMaxTiles * kInverseDeltaTile == kNoAllocMaxSteps, "the step limit is a whole number of tiles");
 constexpr size_t kCounterOffset = 128;         // tile counter, after DevStatus
 constexpr size_t kDescOffset = 256;            // descriptors, 256-byte aligned
 constexpr size_t kScratchBytes = kDescOffset + kMaxTiles * sizeof(unsigned long long);
+static_assert(kScratchBytes == 131328, "the documented scratch size");
 static_assert(sizeof(DevStatus) <= kCounterOffset, "status must fit before the counter");
 constexpr int kMaxDevices = 64;
 
@@ -63,18 +66,19 @@ unsigned char *scratch_for(int dev) {
   return g_scratch_addr[dev];
 }
 
-// The buffers are the caller's: make sure the kernel can reach them from
-// device `dev` before it dereferences them.
-void require_reachable(const void *p, int dev, const char *what) {
+// The buffers are the caller's and the kernel dereferences them as given:
+// only device memory of device `dev` is accepted (managed and mapped host
+// memory are refused, since a mapped pointer's device address can differ
+// from its host address).
+void require_device_memory(const void *p, int dev, const char *what) {
   cudaPointerAttributes a{};
   const cudaError_t e = cudaPointerGetAttributes(&a, p);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     throw std::invalid_argument(std::string(what) + ": not a CUDA-visible pointer");
   }
-  const bool ok = (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged ||
-                  (a.type == cudaMemoryTypeHost && a.devicePointer != nullptr);
-  if (!ok) throw std::invalid_argument(std::string(what) + ": not device memory of the current device");
+  if (a.type != cudaMemoryTypeDevice || a.device != dev)
+    throw std::invalid_argument(std::string(what) + ": not device memory of the current device");
 }
 
 // Offsets must run from 0 to n without decreasing; the inverse-delta kernel
@@ -111,16 +115,16 @@ void inverse_delta_noalloc(const int32_t *in, int32_t *out, uint64_t n, const ui
     const uintptr_t a = reinterpret_cast<uintptr_t>(in), b = reinterpret_cast<uintptr_t>(out), bytes = n * 4;
     if (a < b + bytes && b < a + bytes) throw std::invalid_argument("input and output overlap without being equal");
   }
-  const uint64_t tiles = scan_num_tiles(n);
+  const uint64_t tiles = inverse_delta_num_tiles(n);
   if (tiles > kMaxTiles) throw std::logic_error("static scratch smaller than the tile count");
 
   int dev = -1;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   unsigned char *base = scratch_for(dev);
-  require_reachable(offsets, dev, "offsets");
+  require_device_memory(offsets, dev, "offsets");
   if (n) {
-    require_reachable(in, dev, "input steps");
-    require_reachable(out, dev, "output steps");
+    require_device_memory(in, dev, "input steps");
+    require_device_memory(out, dev, "output steps");
   }
   DevStatus *status = reinterpret_cast<DevStatus *>(base);
   uint32_t *counter = reinterpret_cast<uint32_t *>(base + kCounterOffset);
@@ -143,7 +147,7 @@ void inverse_delta_noalloc(const int32_t *in, int32_t *out, uint64_t n, const ui
     launch_inverse_delta(out, n, offsets, ntrav, desc, counter, status, st);
     cuda_check(cudaGetLastError(), "inverse delta launch");
   }
-  if (read_err(status, st)) throw std::runtime_error("device error in allocation-free inverse delta: look-back wait timed out;");
+  if (const uint32_t e = read_err(status, st)) throw std::runtime_error(describe_device_error("allocation-free inverse delta", e));
 }
 
 }  // namespace gfz

@@ -17,6 +17,18 @@
 
 namespace gfz {
 
+std::string describe_device_error(const char *stage, uint32_t e) {
+  std::string msg = std::string("device error in ") + stage + ":";
+  if (e & kErrTableFull) msg += " pair table full;";
+  if (e & kErrLookupMiss) msg += " counted pair missing from table;";
+  if (e & kErrTimeout) msg += " look-back wait timed out;";
+  if (e & kErrDepth) msg += " rule nesting deeper than 64;";
+  if (e & kErrLength) msg += " length overflow or mismatch;";
+  if (e & kErrRuleCycle) msg += " rule lengths do not resolve (cyclic rulebook);";
+  if (e & kErrBadSymbol) msg += " invalid rule key;";
+  return msg;
+}
+
 void cuda_check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaError(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
 }
@@ -217,15 +229,7 @@ void Context::check_status(const char *stage) {
     h_status_->sticky_err = 0;
     cudaMemsetAsync(&d_status_->sticky_err, 0, sizeof(uint32_t), stream_);
   }
-  std::string msg = std::string("device error in ") + stage + ":";
-  if (e & kErrTableFull) msg += " pair table full;";
-  if (e & kErrLookupMiss) msg += " counted pair missing from table;";
-  if (e & kErrTimeout) msg += " look-back wait timed out;";
-  if (e & kErrDepth) msg += " rule nesting deeper than 64;";
-  if (e & kErrLength) msg += " length overflow or mismatch;";
-  if (e & kErrRuleCycle) msg += " rule lengths do not resolve (cyclic rulebook);";
-  if (e & kErrBadSymbol) msg += " invalid rule key;";
-  throw std::runtime_error(msg);
+  throw std::runtime_error(describe_device_error(stage, e));
 }
 
 unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) {
@@ -1169,10 +1173,10 @@ void load_rules(Context &ctx, Grammar &g, const int32_t *first, const int32_t *s
   cuda_check(cudaMemcpyAsync(off.ptr, h, sizeof(h), cudaMemcpyHostToDevice, st), "upload");
   ctx.reset_status();
   uint32_t *counter;
-  unsigned long long *desc = ctx.lookback(scan_num_tiles(nrules), &counter);
+  unsigned long long *desc = ctx.lookback(inverse_delta_num_tiles(nrules), &counter);
   GFZ_TIMED(ctx, "inverse_delta",
             launch_inverse_delta(g.first.ptr, nrules, off.ptr, 1, desc, counter, ctx.dstatus(), st));
-  desc = ctx.lookback(scan_num_tiles(nrules), &counter);
+  desc = ctx.lookback(inverse_delta_num_tiles(nrules), &counter);
   GFZ_TIMED(ctx, "inverse_delta",
             launch_inverse_delta(g.second.ptr, nrules, off.ptr, 1, desc, counter, ctx.dstatus(), st));
   ctx.read_status();
@@ -1334,7 +1338,7 @@ static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, E
     cuda_check(cudaMemcpyAsync(loc.ptr, h_loc.data(), (nt + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
                "offsets upload");
     GFZ_TIMED_B(ctx, "symbol_sums", 24.0 * m, launch_symbol_records(g.enc.ptr + e0, m, rv, P.rec.ptr, sums.ptr, st));
-    desc = ctx.lookback(scan_num_tiles(m), &counter);
+    desc = ctx.lookback(inverse_delta_num_tiles(m), &counter);
     GFZ_TIMED_B(ctx, "symbol_sums", 8.0 * m,
                 launch_inverse_delta(sums.ptr, m, loc.ptr, nt, desc, counter, ctx.dstatus(), st));
     GFZ_TIMED_B(ctx, "symbol_sums", 36.0 * m, launch_symbol_exclusive(P.rec.ptr, sums.ptr, m, st));
@@ -1400,7 +1404,7 @@ void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVe
   }
   for (int r = 0; r < g.delta_round && total; ++r) {
     uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(scan_num_tiles(total), &counter);
+    unsigned long long *desc = ctx.lookback(inverse_delta_num_tiles(total), &counter);
     GFZ_TIMED_B(ctx, "inverse_delta", 8.0 * total,
               launch_inverse_delta(out.ptr, total, d_out_off.ptr, nt, desc, counter, ctx.dstatus(), st));
   }

@@ -24,6 +24,8 @@ struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
 void cuda_check(cudaError_t e, const char *what);
+// "device error in <stage>:" followed by one phrase per kErr* bit set in e.
+std::string describe_device_error(const char *stage, uint32_t e);
 
 // Growable device array allocated from the stream-ordered pool.
 template <typename T>
@@ -130,6 +132,7 @@ class Context {
   uint64_t append_chunk = 0;     // steps per chunk of the chunked stack pass (0 = the automatic ladder)
   uint64_t hbm_budget = 0;       // device bytes host-input compression may use (0 = no limit)
   uint64_t encode_chunk = 0;     // steps per chunk of host-input compression (0 = from the budget)
+  uint64_t decode_chunk = 0;     // expanded steps per device text pass of the full-file writer (0 = all)
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
