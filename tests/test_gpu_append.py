@@ -1,52 +1,36 @@
-"""Append encoding (add-haplotypes) against the oracle's stack encoder
-(path_encoder.cpp:31-79 applied per stored layer): the encoded streams of
-the appended traversals are identical for copies of stored paths, mutated
-and reversed copies, random steps, long paths spanning many chunks of the
-chunked pass, single-step paths, and repetitive paths whose pairings
-cascade over long stretches."""
+"""Append encoding (add-haplotypes).
+
+Against the reference CLI's own add-haplotypes output
+(tests/golden/append.*, made by tests/golden/make_append_golden.py;
+add_haplotypes_workflow.cpp:336-379, 447-465, 579-592): the updated .gfaz
+bytes, through the Python API, the `gfaz add-haplotypes` binary and the
+server's concurrent append, and the decompressed GFA of the updated file.
+
+Against the oracle's stack encoder (path_encoder.cpp:31-79 applied per
+stored layer; the oracle is pinned to the same reference output): the
+encoded streams of the appended traversals are identical for copies of
+stored paths, mutated and reversed copies, random steps, long paths
+spanning many chunks of the chunked pass, single-step paths, and
+repetitive paths whose pairings cascade over long stretches, with every
+chunk size of the chunked pass."""
+import hashlib
+import json
 import os
+import subprocess
 
 import numpy as np
 import pytest
 
 import gfaz_format as fmt
 import gfaz_gb300 as gz
+import append_cases
 from conftest import GOLDEN, golden_raw
 from oracle import oracle
+from test_gpu_golden import _same_zstd
 
 pytestmark = pytest.mark.gpu
 
 CASES = ["cfg1", "cfg1_mini_d2_r3", "cfg1_mini_d0", "cfg1_mini_r1"]
-
-
-def _p_line(name, steps):
-    return "P\t%s\t%s\t*\n" % (name, ",".join("%d%s" % (abs(int(v)), "+" if v > 0 else "-") for v in steps))
-
-
-def _appended(raw, off, rng):
-    paths = [raw[int(off[i]):int(off[i + 1])] for i in range(len(off) - 1)]
-    hi = int(np.abs(raw).max())
-    out = [paths[0].copy()]
-    m = paths[1 % len(paths)].copy()
-    idx = rng.integers(0, len(m), max(1, len(m) // 100))
-    m[idx] = rng.integers(1, hi // 2 + 1, len(idx))
-    out.append(m)
-    out.append(-paths[2 % len(paths)][::-1])
-    out.append(np.concatenate(paths[:6]))
-    out.append((rng.integers(1, hi // 2 + 1, 5000) * rng.choice([-1, 1], 5000)).astype(np.int32))
-    out.append(np.array([7], np.int32))
-    out.append(np.tile(paths[3 % len(paths)][:2], 6000))
-    out.append(np.tile(paths[4 % len(paths)][:7], 3000))
-    out.append(np.tile(np.array([5, 6], np.int32), 9000))
-    return [np.asarray(p, np.int32) for p in out]
-
-
-def _fits(p, delta_round, min_id):
-    """Whether the delta-coded path stays below the rule id region."""
-    x = p.astype(np.int64)
-    for _ in range(delta_round):
-        x = np.concatenate([x[:1], np.diff(x)])
-    return int(np.abs(x).max()) < min_id
 
 
 @pytest.mark.parametrize("case,chunk", [(c, 0) for c in CASES] + [("cfg1", 8), ("cfg1_mini_r1", 8), ("cfg1", 1)])
@@ -62,12 +46,13 @@ def test_append_encoding_matches_oracle(case, chunk, manifest, tmp_path, gpu_ctx
     raw, off, _ = golden_raw(case, meta)
     src = os.path.join(GOLDEN, case + ".gfaz")
     before = fmt.pre_entropy(fmt.read(src))
-    rng = np.random.default_rng(11)
     dr = int(before["delta_round"][0])
-    new = [p for p in _appended(raw, np.asarray(off, np.uint64), rng) if _fits(p, dr, int(before["layers"][0][1]))]
+    npaths = len(before["sequence_lengths"])
+    new = [p for p in append_cases.path_set(raw, off, npaths, seed=21)
+           if append_cases.fits(p, dr, int(before["layers"][0][1]))]
     assert len(new) >= 6
     ap = tmp_path / "append.gfa"
-    ap.write_text("".join(_p_line("app%d" % i, p) for i, p in enumerate(new)))
+    ap.write_text("".join(append_cases.p_line("app%d" % i, p) for i, p in enumerate(new)))
     c2 = gz.add_haplotypes(gz.deserialize(src), str(ap), ctx=ctx)
     out = tmp_path / "out.gfaz"
     gz.serialize(c2, str(out))
@@ -85,16 +70,17 @@ def test_append_encoding_matches_oracle(case, chunk, manifest, tmp_path, gpu_ctx
     assert np.array_equal(after["paths"][base:], np.concatenate(want))
     # and the appended paths read back as written
     lines = gz.extract_path_lines(c2, ["app%d" % i for i in range(len(new))], ctx=gpu_ctx)
-    assert "".join(lines) == "".join(_p_line("app%d" % i, p) for i, p in enumerate(new))
+    assert "".join(lines) == "".join(append_cases.p_line("app%d" % i, p) for i, p in enumerate(new))
 
 
 def test_server_append_matches_add_haplotypes(manifest, tmp_path, gpu_ctx):
     """The server's concurrent append encodes exactly like add_haplotypes."""
     case = "cfg1"
     src = os.path.join(GOLDEN, case + ".gfaz")
-    raw, off, _ = golden_raw(case, manifest["cases"][case])
-    new = _appended(raw, np.asarray(off, np.uint64), np.random.default_rng(12))
-    text = "".join(_p_line("srv%d" % i, p) for i, p in enumerate(new))
+    raw, off, z = golden_raw(case, manifest["cases"][case])
+    new = [p for p in append_cases.path_set(raw, off, int(z["n_paths"][0]), seed=12)
+           if append_cases.fits(p, int(z["delta_round"][0]), int(z["layers"][0, 1]))]
+    text = "".join(append_cases.p_line("srv%d" % i, p) for i, p in enumerate(new))
     ap = tmp_path / "append.gfa"
     ap.write_text(text)
     c2 = gz.add_haplotypes(gz.deserialize(src), str(ap), ctx=gpu_ctx)
@@ -104,3 +90,69 @@ def test_server_append_matches_add_haplotypes(manifest, tmp_path, gpu_ctx):
         srv.wait(srv.submit_append(text))
         got = [srv.wait(srv.submit_path(n))[0] for n in names]
     assert got == want
+
+
+@pytest.fixture(scope="module")
+def append_golden():
+    with open(os.path.join(GOLDEN, "append.json")) as fh:
+        meta = json.load(fh)
+    return meta, np.load(os.path.join(GOLDEN, "append.npz"))
+
+
+def _check_updated(mine: bytes, case, manifest, append_golden, ctx):
+    meta, z = append_golden
+    m = meta["cases"][case]
+    if _same_zstd(manifest):
+        assert hashlib.sha256(mine).hexdigest() == m["updated_gfaz_sha256"]
+    else:
+        pe = fmt.pre_entropy(fmt.read(mine))
+        for k, v in pe.items():
+            np.testing.assert_array_equal(v, z[case + ":" + k], err_msg=k)
+    text = gz.gfa_text(gz.CompressedData.from_bytes(mine), ctx=ctx)
+    assert hashlib.sha256(text).hexdigest() == m["updated_gfa_out_sha256"]
+
+
+@pytest.mark.parametrize("case,kind", append_cases.GOLDEN_CASES)
+def test_append_matches_reference_gfaz(case, kind, manifest, append_golden, tmp_path, gpu_ctx):
+    """add_haplotypes on the GPU writes the reference CLI's updated .gfaz."""
+    text, _, _ = append_cases.golden_append(case, kind, manifest)
+    ap = tmp_path / "append.gfa"
+    ap.write_text(text)
+    c2 = gz.add_haplotypes(gz.deserialize(os.path.join(GOLDEN, case + ".gfaz")), str(ap), ctx=gpu_ctx)
+    _check_updated(c2.to_bytes(), case, manifest, append_golden, gpu_ctx)
+
+
+@pytest.mark.parametrize("case,kind", [("cfg1", "P"), ("rich", "W")])
+def test_append_cli_matches_reference_gfaz(case, kind, manifest, append_golden, tmp_path, gpu_ctx):
+    """The same through the `gfaz add-haplotypes` binary."""
+    from gfaz_gb300.build import CLI
+    text, _, _ = append_cases.golden_append(case, kind, manifest)
+    ap = tmp_path / "append.gfa"
+    ap.write_text(text)
+    out = tmp_path / "updated.gfaz"
+    r = subprocess.run([CLI, "add-haplotypes", os.path.join(GOLDEN, case + ".gfaz"), str(ap), str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _check_updated(out.read_bytes(), case, manifest, append_golden, gpu_ctx)
+
+
+@pytest.mark.parametrize("case,kind", [("cfg1", "P"), ("rich", "W")])
+def test_server_append_matches_reference(case, kind, manifest, append_golden, gpu_ctx):
+    """The server's concurrent append of the golden set answers with the
+    lines of the reference's updated container."""
+    text, steps, _ = append_cases.golden_append(case, kind, manifest)
+    ap_lines = text.splitlines(keepends=True)
+    with gz.Server(gz.deserialize(os.path.join(GOLDEN, case + ".gfaz")), workers=2) as srv:
+        srv.wait(srv.submit_append(text))
+        if kind == "P":
+            got = [srv.wait(srv.submit_path("app%d" % i))[0] for i in range(len(steps))]
+        else:
+            got = []
+            for ln in ap_lines:
+                f = ln.rstrip("\n").split("\t")
+                key = gz.WalkLookupKey(f[1], int(f[2]), f[3], -1 if f[4] == "*" else int(f[4]),
+                                       -1 if f[5] == "*" else int(f[5]))
+                got.append(srv.wait(srv.submit_walk(key))[0])
+    # the appended lines read back as written (the reference's decompressed
+    # updated file ends with them: its digest is checked above)
+    assert got == ap_lines

@@ -81,3 +81,45 @@ def test_oracle_append_encoding_cascades():
     parts = oracle.append_encode(np.array([1, 2, 3], np.int32), np.array([0, 3], np.uint64), 1, first, second,
                                  layers)
     assert parts[0].tolist() == [11]
+
+
+@pytest.fixture(scope="module")
+def append_golden():
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "append.json")) as fh:
+        meta = json.load(fh)
+    return meta, np.load(os.path.join(GOLDEN, "append.npz"))
+
+
+@pytest.mark.parametrize("case,kind", __import__("append_cases").GOLDEN_CASES)
+def test_oracle_append_matches_reference(case, kind, manifest, append_golden):
+    """The oracle's append encoder against the reference CLI's
+    add-haplotypes output (tests/golden/make_append_golden.py): the
+    appended encoded traversals and their lengths, and everything the
+    append leaves alone."""
+    import append_cases
+    meta, z = append_golden
+    text, steps, before = append_cases.golden_append(case, kind, manifest)
+    m = meta["cases"][case]
+    assert hashlib.sha256(text.encode()).hexdigest() == m["append_sha256"]
+    after = {k.split(":", 1)[1]: z[k] for k in z.files if k.startswith(case + ":")}
+    for k in ("rules_first", "rules_second", "layers", "delta_round"):
+        np.testing.assert_array_equal(after[k], before[k], err_msg=k)
+    off = np.zeros(len(steps) + 1, np.uint64)
+    np.cumsum([len(s) for s in steps], out=off[1:])
+    parts = oracle.append_encode(np.concatenate(steps), off, int(before["delta_round"][0]), before["rules_first"],
+                                 before["rules_second"], before["layers"])
+    col, lens, orig = ("paths", "sequence_lengths", "original_path_lengths") if kind == "P" else \
+        ("walks", "walk_lengths", "original_walk_lengths")
+    old = len(before[lens])
+    base = int(np.sum(before[lens]))
+    np.testing.assert_array_equal(after[col][:base], before[col])
+    np.testing.assert_array_equal(after[col][base:], np.concatenate(parts))
+    np.testing.assert_array_equal(after[lens][:old], before[lens])
+    assert [int(x) for x in after[lens][old:]] == [len(p) for p in parts]
+    assert [int(x) for x in after[orig][old:]] == [len(s) for s in steps]
+    other = ("walks", "walk_lengths") if kind == "P" else ("paths", "sequence_lengths")
+    for k in other:
+        np.testing.assert_array_equal(after[k], before[k], err_msg=k)
