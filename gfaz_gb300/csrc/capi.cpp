@@ -229,6 +229,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "encode_chunk") {
       require(value >= 0, "encode_chunk must be >= 0");
       c.encode_chunk = (uint64_t)value;
+    } else if (std::string(name) == "decode_chunk") {
+      require(value >= 0, "decode_chunk must be >= 0");
+      c.decode_chunk = (uint64_t)value;
     } else if (std::string(name) == "front_end") {
       require(value == 0 || value == 1, "front_end must be 0 (host parser) or 1 (device)");
       c.front_end = (int)value;

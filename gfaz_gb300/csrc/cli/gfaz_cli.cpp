@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cerrno>
 #include <cstring>
 #include <iomanip>
 #include <iostream>
@@ -39,9 +40,13 @@ void usage() {
                "    gfaz add-haplotypes [OPTIONS] <input.gfaz> <paths_or_walks.gfa> [output.gfaz]\n"
                "    gfaz growth [-j N] [-G path|sample-hap-seq|sample-hap|sample] <input.gfaz>\n"
                "    gfaz pav -i <input.gfaz> -b <ranges.bed> [-S|-H] [-M] [-B T] [-t N]\n\n"
-               "compress options: -r/--rounds N (8)  -d/--delta N (1)  -t/--threshold N (2)\n"
-               "                  -j/--threads N (0 = auto)  -g/--gpu  -s/--stats\n"
-               "other commands:   -j/--threads N\n";
+               "compress options:   -r/--rounds N (8)  -d/--delta N (1)  -t/--threshold N (2)\n"
+               "                    -j/--threads N (0 = auto)  -g/--gpu  -s/--stats  --debug\n"
+               "                    --gpu-rolling-input-chunk-mb N (alias --gpu-chunk-mb)  --gpu-legacy\n"
+               "decompress options: -j/--threads N  -l/--legacy  -g/--gpu  -s/--stats  --debug\n"
+               "                    --gpu-rolling-output-chunk-mb N (alias --gpu-max-expanded-chunk-mb)\n"
+               "                    --gpu-legacy\n"
+               "other commands:     -j/--threads N\n";
 }
 
 long file_size(const std::string &p) {
@@ -53,13 +58,69 @@ long file_size(const std::string &p) {
   return n;
 }
 
+// Long-only options of the reference CLI (src/cli/common.hpp values).
+constexpr int kOptInputChunkMb = 1000;
+constexpr int kOptGpuLegacy = 1001;
+constexpr int kOptDebug = 1003;
+constexpr int kOptOutputChunkMb = 1004;
+// The reference's default rolling output chunk of the GPU decompressor, MiB.
+constexpr unsigned long long kDefaultOutputChunkMb = 1024;
+
+// A positive decimal integer, as the reference's parse_ull_arg takes it.
+bool positive_ull(const char *name, const char *value, unsigned long long &out) {
+  errno = 0;
+  char *end = nullptr;
+  out = std::strtoull(value, &end, 10);
+  if (errno != 0 || end == value || *end != '\0' || out == 0) {
+    std::cerr << "Error: Invalid value for " << name << ": " << value << std::endl;
+    return false;
+  }
+  return true;
+}
+
+// --debug: the library's phase timers (GFA_COMPRESSION_DEBUG, read once, on
+// the first library call that looks at it).
+void enable_debug() { setenv("GFA_COMPRESSION_DEBUG", "1", 1); }
+
+// A context carrying one option, or none (the library's default context).
+struct CliContext {
+  gfz_context *ctx = nullptr;
+  ~CliContext() {
+    if (ctx) gfz_context_destroy(ctx);
+  }
+  bool set(const char *name, int64_t value) {
+    if (!ctx && gfz_context_create(0, nullptr, &ctx) != GFZ_OK) return false;
+    return gfz_context_set_option(ctx, name, value) == GFZ_OK;
+  }
+};
+
+const char *threads_line(int threads, std::string &buf) {
+  buf = threads == 0 ? std::string("auto") : threads < 0 ? std::string("inherit OpenMP") : std::to_string(threads);
+  return buf.c_str();
+}
+
+// compress_command.cpp:21-271.  The transform always runs on the GPU and is
+// bit-exact with the reference's CPU compressor, so --delta and --threshold
+// are honoured with or without --gpu.  --gpu-rolling-input-chunk-mb N
+// streams host-resident steps through HBM in chunks of N MiB (same bytes);
+// --gpu-legacy selects the whole-device path, which is this build's default
+// (it changes nothing); both require --gpu, as in the reference.
 int do_compress(int argc, char **argv) {
   int rounds = 8, delta = 1, threshold = 2, threads = 0;
-  bool stats = false;
-  static struct option lo[] = {{"rounds", required_argument, 0, 'r'},    {"delta", required_argument, 0, 'd'},
-                               {"threshold", required_argument, 0, 't'}, {"threads", required_argument, 0, 'j'},
-                               {"gpu", no_argument, 0, 'g'},             {"stats", no_argument, 0, 's'},
-                               {"help", no_argument, 0, 'h'},            {0, 0, 0, 0}};
+  bool stats = false, use_gpu = false, gpu_legacy = false, debug = false;
+  unsigned long long chunk_mb = 0;
+  static struct option lo[] = {{"rounds", required_argument, 0, 'r'},
+                               {"delta", required_argument, 0, 'd'},
+                               {"threshold", required_argument, 0, 't'},
+                               {"threads", required_argument, 0, 'j'},
+                               {"gpu", no_argument, 0, 'g'},
+                               {"gpu-rolling-input-chunk-mb", required_argument, 0, kOptInputChunkMb},
+                               {"gpu-chunk-mb", required_argument, 0, kOptInputChunkMb},
+                               {"gpu-legacy", no_argument, 0, kOptGpuLegacy},
+                               {"stats", no_argument, 0, 's'},
+                               {"debug", no_argument, 0, kOptDebug},
+                               {"help", no_argument, 0, 'h'},
+                               {0, 0, 0, 0}};
   int opt;
   optind = 1;
   while ((opt = getopt_long(argc, argv, "r:d:t:j:gsh", lo, nullptr)) != -1) {
@@ -74,8 +135,13 @@ int do_compress(int argc, char **argv) {
         break;
       case 't': threshold = std::atoi(optarg); break;
       case 'j': threads = std::atoi(optarg); break;
-      case 'g': break;
+      case 'g': use_gpu = true; break;
+      case kOptInputChunkMb:
+        if (!positive_ull("--gpu-rolling-input-chunk-mb", optarg, chunk_mb)) return 1;
+        break;
+      case kOptGpuLegacy: gpu_legacy = true; break;
       case 's': stats = true; break;
+      case kOptDebug: debug = true; break;
       case 'h': usage(); return 0;
       default: usage(); return 1;
     }
@@ -86,11 +152,26 @@ int do_compress(int argc, char **argv) {
   }
   const std::string in = argv[optind];
   const std::string out = optind + 1 < argc ? argv[optind + 1] : in + ".gfaz";
-  std::cout << "=== GFAZ Compress ===\nInput:  " << in << "\nOutput: " << out << "\nBackend: GPU\nRounds: " << rounds
-            << "\nDelta:  " << delta << "\nThreshold: " << threshold << "\n\n";
+  if (!use_gpu && (chunk_mb > 0 || gpu_legacy)) {
+    std::cerr << "Error: --gpu-rolling-input-chunk-mb and --gpu-legacy require --gpu\n";
+    return 1;
+  }
+  if (gpu_legacy && chunk_mb > 0) {
+    std::cerr << "Note: --gpu-rolling-input-chunk-mb is ignored with --gpu-legacy." << std::endl;
+    chunk_mb = 0;
+  }
+  std::string tb;
+  std::cout << "=== GFAZ Compress ===\nInput:  " << in << "\nOutput: " << out << "\nBackend: GPU\nStats: "
+            << (stats ? "on" : "off") << "\nDebug: " << (debug ? "on" : "off") << "\nRounds: " << rounds
+            << "\nDelta:  " << delta << "\nThreshold: " << threshold;
+  if (chunk_mb) std::cout << "\nGPU Rolling Input Chunk: " << chunk_mb << " MiB";
+  std::cout << "\nThreads: " << threads_line(threads, tb) << "\n\n";
+  if (debug) enable_debug();
+  CliContext cc;
+  if (chunk_mb && !cc.set("encode_chunk", (int64_t)(chunk_mb * 1024ull * 1024ull / 4))) return fail();
   const auto t0 = Clock::now();
   gfz_compressed *c = nullptr;
-  if (gfz_compress_file(nullptr, in.c_str(), rounds, (uint64_t)threshold, delta, threads, stats ? 1 : 0, &c) != GFZ_OK)
+  if (gfz_compress_file(cc.ctx, in.c_str(), rounds, (uint64_t)threshold, delta, threads, stats ? 1 : 0, &c) != GFZ_OK)
     return fail();
   const gfz_status st = gfz_serialize(c, out.c_str());
   gfz_compressed_free(c);
@@ -105,16 +186,19 @@ int do_compress(int argc, char **argv) {
   return 0;
 }
 
+// extract-path, extract-walk, add-haplotypes: -j/--threads and -h as in the
+// reference; --gpu is accepted as well (these always run on the GPU).
 int simple_opts(int argc, char **argv, int &threads, const char *shortopts) {
-  static struct option lo[] = {{"threads", required_argument, 0, 'j'}, {"gpu", no_argument, 0, 'g'},
-                               {"stats", no_argument, 0, 's'},         {"legacy", no_argument, 0, 'l'},
-                               {"help", no_argument, 0, 'h'},          {0, 0, 0, 0}};
+  static struct option lo[] = {{"threads", required_argument, 0, 'j'},
+                               {"gpu", no_argument, 0, 'g'},
+                               {"help", no_argument, 0, 'h'},
+                               {0, 0, 0, 0}};
   int opt;
   optind = 1;
   while ((opt = getopt_long(argc, argv, shortopts, lo, nullptr)) != -1) {
     switch (opt) {
       case 'j': threads = std::atoi(optarg); break;
-      case 'g': case 's': case 'l': break;
+      case 'g': break;
       case 'h': usage(); return 0;
       default: usage(); return 1;
     }
@@ -122,25 +206,88 @@ int simple_opts(int argc, char **argv, int &threads, const char *shortopts) {
   return -1;
 }
 
+// decompress_command.cpp:23-274.  --gpu-rolling-output-chunk-mb N (alias
+// --gpu-max-expanded-chunk-mb) writes the P and W text in traversal groups
+// of at most N MiB of expanded int32 steps, one group on the device at a
+// time; without it the whole graph decodes in one pass.  --legacy (the
+// reference's in-memory CPU mode) and --gpu-legacy write the same bytes as
+// the default; the reference's checks on combining them are kept.
 int do_decompress(int argc, char **argv) {
   int threads = 0;
-  if (int r = simple_opts(argc, argv, threads, "j:glsh"); r >= 0) return r;
+  bool use_gpu = false, legacy = false, gpu_legacy = false, stats = false, debug = false;
+  unsigned long long chunk_mb = kDefaultOutputChunkMb;
+  bool chunk_given = false;
+  static struct option lo[] = {{"threads", required_argument, 0, 'j'},
+                               {"legacy", no_argument, 0, 'l'},
+                               {"gpu", no_argument, 0, 'g'},
+                               {"gpu-rolling-output-chunk-mb", required_argument, 0, kOptOutputChunkMb},
+                               {"gpu-max-expanded-chunk-mb", required_argument, 0, kOptOutputChunkMb},
+                               {"gpu-legacy", no_argument, 0, kOptGpuLegacy},
+                               {"stats", no_argument, 0, 's'},
+                               {"debug", no_argument, 0, kOptDebug},
+                               {"help", no_argument, 0, 'h'},
+                               {0, 0, 0, 0}};
+  int opt;
+  optind = 1;
+  while ((opt = getopt_long(argc, argv, "j:lgsh", lo, nullptr)) != -1) {
+    switch (opt) {
+      case 'j': threads = std::atoi(optarg); break;
+      case 'l': legacy = true; break;
+      case 'g': use_gpu = true; break;
+      case kOptOutputChunkMb:
+        if (!positive_ull("--gpu-rolling-output-chunk-mb", optarg, chunk_mb)) return 1;
+        chunk_given = true;
+        break;
+      case kOptGpuLegacy: gpu_legacy = true; break;
+      case 's': stats = true; break;
+      case kOptDebug: debug = true; break;
+      case 'h': usage(); return 0;
+      default: usage(); return 1;
+    }
+  }
   if (optind >= argc) {
     std::cerr << "Error: No input file specified\n";
     return 1;
   }
   const std::string in = argv[optind];
+  if (!use_gpu && (chunk_mb != kDefaultOutputChunkMb || gpu_legacy)) {
+    std::cerr << "Error: --gpu-rolling-output-chunk-mb and --gpu-legacy require --gpu\n";
+    return 1;
+  }
+  if (use_gpu && legacy) {
+    std::cerr << "Error: --legacy is the CPU legacy mode. Use --gpu-legacy for the old whole-graph GPU "
+                 "decompression path.\n";
+    return 1;
+  }
   std::string out;
   if (optind + 1 < argc) out = argv[optind + 1];
   else if (in.size() > 5 && in.substr(in.size() - 5) == ".gfaz") out = in.substr(0, in.size() - 5);
   else out = in + ".decompressed";
-  std::cout << "=== GFAZ Decompress ===\nInput:  " << in << "\nOutput: " << out << "\n\n";
+  if (gpu_legacy && chunk_given) {
+    std::cerr << "Note: --gpu-rolling-output-chunk-mb is ignored with --gpu-legacy." << std::endl;
+    chunk_given = false;
+  }
+  std::string tb;
+  std::cout << "=== GFAZ Decompress ===\nInput:  " << in << "\nOutput: " << out << "\nBackend: GPU\nStats: "
+            << (stats ? "on" : "off") << "\nDebug: " << (debug ? "on" : "off");
+  if (chunk_given) std::cout << "\nGPU Rolling Output Chunk: " << chunk_mb << " MiB";
+  std::cout << "\nThreads: " << threads_line(threads, tb) << "\n\n";
+  if (debug) enable_debug();
+  CliContext cc;
+  if (chunk_given && !cc.set("decode_chunk", (int64_t)(chunk_mb * 1024ull * 1024ull / 4))) return fail();
+  const auto t0 = Clock::now();
   gfz_compressed *c = nullptr;
   if (gfz_deserialize(in.c_str(), &c) != GFZ_OK) return fail();
-  const gfz_status st = gfz_write_gfa(nullptr, c, out.c_str(), threads);
+  const gfz_status st = gfz_write_gfa(cc.ctx, c, out.c_str(), threads);
   gfz_compressed_free(c);
   if (st != GFZ_OK) return fail();
+  const double s = std::chrono::duration<double>(Clock::now() - t0).count();
   std::cout << "\nDecompression complete!" << std::endl;
+  if (stats) {
+    const long a = file_size(in), b = file_size(out);
+    std::printf("Stats:\n  Time: %.3f s\n  Input: %ld B\n  Output: %ld B\n  Throughput: %.2f MB/s\n", s, a, b,
+                b / 1048576.0 / (s > 0 ? s : 1));
+  }
   return 0;
 }
 
@@ -153,7 +300,7 @@ int print_and_free(gfz_status st, char *text, size_t len) {
 
 int do_extract_path(int argc, char **argv) {
   int threads = 0;
-  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (int r = simple_opts(argc, argv, threads, "j:gh"); r >= 0) return r;
   if (optind + 1 >= argc) {
     std::cerr << "Error: Expected <input.gfaz> and at least one <path_name>\n";
     return 1;
@@ -170,7 +317,7 @@ int do_extract_path(int argc, char **argv) {
 
 int do_extract_walk(int argc, char **argv) {
   int threads = 0;
-  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (int r = simple_opts(argc, argv, threads, "j:gh"); r >= 0) return r;
   if (optind + 5 >= argc) {
     std::cerr << "Error: Expected <input.gfaz> and at least one walk identifier tuple\n";
     return 1;
@@ -205,7 +352,7 @@ int do_extract_walk(int argc, char **argv) {
 
 int do_add_haplotypes(int argc, char **argv) {
   int threads = 0;
-  if (int r = simple_opts(argc, argv, threads, "j:h"); r >= 0) return r;
+  if (int r = simple_opts(argc, argv, threads, "j:gh"); r >= 0) return r;
   if (optind + 1 >= argc) {
     std::cerr << "Error: Expected <input.gfaz> and <paths_or_walks.gfa>\n";
     return 1;

@@ -490,30 +490,32 @@ TextPieces make_pieces(const std::vector<std::string> &pre, const std::vector<st
 }
 
 TextPieces path_pieces(const std::vector<std::string> &names, const std::vector<std::string> &overlaps,
-                       const std::vector<uint64_t> &off) {
+                       const std::vector<uint64_t> &off, size_t base) {
   const size_t n = off.size() - 1;
   std::vector<std::string> pre(n), suf(n);
-  for (size_t t = 0; t < n; ++t) {
+  for (size_t i = 0; i < n; ++i) {
+    const size_t t = base + i;
     const std::string &name = t < names.size() ? names[t] : std::to_string(t);
     const std::string ov = t < overlaps.size() ? overlaps[t] : std::string();
-    pre[t] = "P\t" + name + "\t";
-    suf[t] = "\t" + (ov.empty() ? std::string("*") : ov) + "\n";
+    pre[i] = "P\t" + name + "\t";
+    suf[i] = "\t" + (ov.empty() ? std::string("*") : ov) + "\n";
   }
   return make_pieces(pre, suf, off);
 }
 
 TextPieces walk_pieces(const std::vector<std::string> &samples, const std::vector<uint32_t> &haps,
                        const std::vector<std::string> &seqids, const std::vector<int64_t> &starts,
-                       const std::vector<int64_t> &ends, const std::vector<uint64_t> &off) {
+                       const std::vector<int64_t> &ends, const std::vector<uint64_t> &off, size_t base) {
   const size_t n = off.size() - 1;
   std::vector<std::string> pre(n), suf(n, "\n");
-  for (size_t t = 0; t < n; ++t) {
+  for (size_t i = 0; i < n; ++i) {
+    const size_t t = base + i;
     const std::string sample = t < samples.size() ? samples[t] : "sample";
     const uint32_t hap = t < haps.size() ? haps[t] : 0;
     const std::string seqid = t < seqids.size() ? seqids[t] : "unknown";
     const int64_t st = t < starts.size() ? starts[t] : -1;
     const int64_t en = t < ends.size() ? ends[t] : -1;
-    pre[t] = "W\t" + sample + "\t" + std::to_string(hap) + "\t" + seqid + "\t" +
+    pre[i] = "W\t" + sample + "\t" + std::to_string(hap) + "\t" + seqid + "\t" +
              (st >= 0 ? std::to_string(st) : std::string("*")) + "\t" +
              (en >= 0 ? std::to_string(en) : std::string("*")) + "\t";
   }
@@ -882,6 +884,32 @@ void download_raw(Context &ctx, const char *dev, uint64_t n, char *dst, int nth)
 
 }  // namespace
 
+namespace {
+
+// Boundaries [b[i], b[i+1]) of consecutive groups of the n traversals whose
+// expanded steps (lens) stay within `chunk` (a longer traversal is a group
+// of its own); chunk 0 gives one group.
+std::vector<uint64_t> traversal_groups(uint64_t n, const std::vector<uint32_t> &lens, uint64_t chunk) {
+  std::vector<uint64_t> b{0};
+  if (!chunk) {
+    if (n) b.push_back(n);
+    return b;
+  }
+  uint64_t acc = 0;
+  for (uint64_t t = 0; t < n; ++t) {
+    const uint64_t len = t < lens.size() ? lens[t] : 0;
+    if (t > b.back() && acc + len > chunk) {
+      b.push_back(t);
+      acc = 0;
+    }
+    acc += len;
+  }
+  if (n) b.push_back(n);
+  return b;
+}
+
+}  // namespace
+
 void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out) {
   const int nth = resolve_threads(threads);
   set_zstd_threads(nth);
@@ -890,21 +918,28 @@ void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out)
   // loads and the P text is written on the device; that text waits in HBM
   // until the H/S/L/J/C text before it is in place.  An error in the static
   // columns is reported first, as when the steps ran one after the other.
+  // With ctx.decode_chunk set, P and W text are written in traversal groups
+  // of at most that many expanded steps, each downloaded before the next is
+  // decoded, so the device holds one group's output at a time.
   std::future<StaticFields> fs = std::async(std::launch::async, [&c] { return decode_static(c); });
   Grammar g(ctx.stream());
   DevVec<char> text(ctx.stream());
   LoadedStreams ls{};
   uint64_t pn = 0;
+  std::vector<std::string> names, ovs;
   std::exception_ptr dev_err;
   try {
     ls = load_all(ctx, c, g, kWriterErr);
     clk.mark("rules + encoded streams (zstd, upload)");
     if (ls.np) {
-      const auto names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
-      const auto ovs = split_strings(unzstd_str(c.overlaps), unzstd_u32(c.overlap_lengths), true, kWriterErr);
-      pn = decode_text(
-          ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0, text);
-      clk.mark("P text (device)");
+      names = split_strings(unzstd_str(c.names), unzstd_u32(c.name_lengths), true, kWriterErr);
+      ovs = split_strings(unzstd_str(c.overlaps), unzstd_u32(c.overlap_lengths), true, kWriterErr);
+      if (!ctx.decode_chunk) {
+        pn = decode_text(
+            ctx, g, 0, ls.np, [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff); }, 0,
+            text);
+        clk.mark("P text (device)");
+      }
     }
   } catch (...) {
     dev_err = std::current_exception();
@@ -915,7 +950,17 @@ void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out)
   out.append(ctx.static_text ? static_text_device(ctx, c, s, nth) : static_text(c, s));
   clk.mark("H/S/L/J/C text");
   if (ls.np) {
-    download_raw(ctx, text.ptr, pn, out.grow(pn), nth);
+    if (!ctx.decode_chunk) {
+      download_raw(ctx, text.ptr, pn, out.grow(pn), nth);
+    } else {
+      const std::vector<uint64_t> b = traversal_groups(ls.np, c.original_path_lengths, ctx.decode_chunk);
+      for (size_t i = 0; i + 1 < b.size(); ++i) {
+        const uint64_t n = decode_text(
+            ctx, g, b[i], b[i + 1],
+            [&](const std::vector<uint64_t> &xoff) { return path_pieces(names, ovs, xoff, b[i]); }, 0, text);
+        download_raw(ctx, text.ptr, n, out.grow(n), nth);
+      }
+    }
     clk.mark("P text download");
   }
   if (ls.nw) {
@@ -925,11 +970,16 @@ void gfa_text_into(Context &ctx, const Compressed &c, int threads, RawText &out)
     const auto seqids = split_strings(unzstd_str(c.walk_seq_ids), unzstd_u32(c.walk_seq_id_lengths), true, kWriterErr);
     const auto starts = unvarint_i64(c.walk_seq_starts, c.walk_lengths.size());
     const auto ends = unvarint_i64(c.walk_seq_ends, c.walk_lengths.size());
-    const uint64_t n = decode_text(
-        ctx, g, ls.np, ls.np + ls.nw,
-        [&](const std::vector<uint64_t> &xoff) { return walk_pieces(samples, haps, seqids, starts, ends, xoff); }, 1,
-        text);
-    download_raw(ctx, text.ptr, n, out.grow(n), nth);
+    const std::vector<uint64_t> b = traversal_groups(ls.nw, c.original_walk_lengths, ctx.decode_chunk);
+    for (size_t i = 0; i + 1 < b.size(); ++i) {
+      const uint64_t n = decode_text(
+          ctx, g, ls.np + b[i], ls.np + b[i + 1],
+          [&](const std::vector<uint64_t> &xoff) {
+            return walk_pieces(samples, haps, seqids, starts, ends, xoff, b[i]);
+          },
+          1, text);
+      download_raw(ctx, text.ptr, n, out.grow(n), nth);
+    }
   }
 }
 

@@ -173,10 +173,11 @@ TextPieces make_pieces(const std::vector<std::string> &pre, const std::vector<st
 
 // Decoded rule columns (zstd + delta decode on the device) and text pieces.
 void decode_rule_columns(Context &ctx, const Compressed &c, Grammar &g);
+// Traversal t of `off` takes its fields from entry base + t of the columns.
 TextPieces path_pieces(const std::vector<std::string> &names, const std::vector<std::string> &overlaps,
-                       const std::vector<uint64_t> &off);
+                       const std::vector<uint64_t> &off, size_t base = 0);
 TextPieces walk_pieces(const std::vector<std::string> &samples, const std::vector<uint32_t> &haps,
                        const std::vector<std::string> &seqids, const std::vector<int64_t> &starts,
-                       const std::vector<int64_t> &ends, const std::vector<uint64_t> &off);
+                       const std::vector<int64_t> &ends, const std::vector<uint64_t> &off, size_t base = 0);
 
 }  // namespace gfz

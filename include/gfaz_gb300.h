@@ -88,6 +88,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * use (default 0 = no limit): above it the stream stays in host memory and
  * passes through HBM in chunks, with identical output; "encode_chunk" =
  * steps per such chunk, forcing chunked compression (default 0);
+ * "decode_chunk" = expanded steps per device pass of the full-file writer
+ * (gfz_write_gfa, gfz_gfa_text): P and W lines are written in traversal
+ * groups of at most that many steps (a longer traversal alone), each group
+ * downloaded before the next decodes (default 0 = one pass; the same
+ * bytes; the CLI's --gpu-rolling-output-chunk-mb sets it);
  * "front_end" = the GFA parse of file compression: 1 (default) = the
  * device front end (line index and P/W steps on the GPU), 0 = the host
  * parser; both give the same graph, and the host parser also runs when the
@@ -301,7 +306,8 @@ void gfz_server_destroy(gfz_server *s);
  * gfz_decode) of `n` steps from `steps_in` into `steps_out` on `cuda_stream`
  * (NULL = legacy default stream), with `offsets` (ntrav + 1 entries, from 0
  * to n) marking the traversals.  All three buffers are the caller's device
- * memory on the current device; steps_in == steps_out decodes in place.
+ * memory on the current device (managed and mapped host memory are refused
+ * with GFZ_ERR_INVALID); steps_in == steps_out decodes in place.
  * The call allocates nothing: its scratch is a fixed 131,328-byte device
  * array that every GPU loading this library holds until exit, so n is
  * limited to GFZ_NOALLOC_MAX_STEPS (67,108,864); larger n fails with
