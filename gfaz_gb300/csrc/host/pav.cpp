@@ -10,7 +10,6 @@
 #include <algorithm>
 #include <cctype>
 #include <fstream>
-#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -24,19 +23,55 @@ namespace gfz {
 
 namespace {
 
+// Whitespace-separated fields of one BED line, read left to right the way
+// formatted stream extraction reads them: a word is a run of non-blank
+// bytes; a number is an optional sign and decimal digits directly at the
+// cursor (a '-' wraps, as strtoull does), and whatever follows the digits is
+// left for the next field.
+struct BedFields {
+  const std::string &s;
+  size_t i = 0;
+  explicit BedFields(const std::string &line) : s(line) {}
+  void skip_blanks() {
+    while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
+  }
+  bool word(std::string &out) {
+    skip_blanks();
+    const size_t b = i;
+    while (i < s.size() && !std::isspace((unsigned char)s[i])) ++i;
+    out.assign(s, b, i - b);
+    return i > b;
+  }
+  bool number(uint64_t &out) {
+    skip_blanks();
+    bool neg = false;
+    if (i < s.size() && (s[i] == '+' || s[i] == '-')) neg = s[i++] == '-';
+    uint64_t v = 0;
+    const size_t b = i;
+    for (; i < s.size() && s[i] >= '0' && s[i] <= '9'; ++i) {
+      const uint64_t d = (uint64_t)(s[i] - '0');
+      if (v > (UINT64_MAX - d) / 10) return false;
+      v = v * 10 + d;
+    }
+    if (i == b) return false;
+    out = neg ? 0 - v : v;
+    return true;
+  }
+};
+
+// BED ranges (chrom start end [name]); '#' lines and empty lines are
+// skipped.  The messages are the reference CLI's (pav_workflow.cpp:225-251).
 std::vector<PavRange> read_bed(const std::string &path) {
   std::ifstream in(path);
   if (!in) throw std::runtime_error("pav: failed to open BED file: " + path);
   std::vector<PavRange> ranges;
-  std::string line;
-  while (std::getline(in, line)) {
+  for (std::string line; std::getline(in, line);) {
     if (line.empty() || line[0] == '#') continue;
-    std::stringstream ss(line);
+    BedFields f(line);
     PavRange r;
-    ss >> r.chrom >> r.start >> r.end;
-    if (!ss || r.chrom.empty()) throw std::runtime_error("pav: malformed BED line: " + line);
-    ss >> r.name;
-    if (r.name.empty()) r.name = r.chrom + ":" + std::to_string(r.start) + "-" + std::to_string(r.end);
+    if (!f.word(r.chrom) || !f.number(r.start) || !f.number(r.end))
+      throw std::runtime_error("pav: malformed BED line: " + line);
+    if (!f.word(r.name)) r.name = r.chrom + ":" + std::to_string(r.start) + "-" + std::to_string(r.end);
     if (r.end < r.start) throw std::runtime_error("pav: BED end before start: " + line);
     ranges.push_back(std::move(r));
   }

@@ -4,7 +4,11 @@
 # for the oracle restatement and the generator of the golden fixtures under
 # tests/golden/.  Nothing in the product links or runs it.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $GFAZ_REFERENCE_ROOT.  Without either, the
+#   script looks in the one place the reference checkout is mounted on the
+#   build container (below); when no sources are found it builds nothing and
+#   exits 3, which callers treat as "skipped".
 #
 # The reference normally builds with CMake against a zstd submodule; here the
 # 18 CPU core sources (CMakeLists.txt:128-147) and the CLI sources are
@@ -15,7 +19,7 @@
 #   * cli_fix.hpp - force-included into decompress_command.cpp, which names a
 #                   GPU-only constant outside its ENABLE_CUDA guard.
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${GFAZ_REFERENCE_ROOT:-/root/reference}}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 OBJ="$OUT/obj"
@@ -23,7 +27,7 @@ mkdir -p "$OBJ"
 
 if [ ! -d "$REF/src" ]; then
   echo "reference sources not found at $REF" >&2
-  exit 1
+  exit 3
 fi
 
 ZSTD_LIB=""
