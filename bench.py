@@ -13,11 +13,15 @@ delta + P-line text emission).
   e2e    the same through the C ABI with host buffers: pinned host steps in,
          encoded stream + rulebook out to the host (what the entropy stage
          consumes), loaded back from the host and decoded to pinned host
-         text; every copy inside the timed region.
+         text; every copy inside the timed region; two such jobs in flight
+         at once (--e2e-jobs), each on its own context and stream.
 
 `--impl reference` times the reference algorithm's CPU implementation on
 the host cores (the oracle port: the reference is not built on the GPU
-host), on a bounded sample of the same workload.
+host) on the whole workload, every timed step all 90 P-lines; the port's
+speed relative to the reference CLI's own code is recorded in
+oracle/calibration.json (made by oracle/calibrate_ref.py) and reported
+beside it.
 
 Multi-GPU (torchrun): independent replicas, one per rank (the transform has
 no cross-rank exchange); a barrier and the max over ranks bracket the timed
@@ -51,9 +55,11 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the cfg2 workload (testing)")
-    ap.add_argument("--cpu-sample-paths", type=int, default=12)
+    ap.add_argument("--cpu-sample-paths", type=int, default=90,
+                    help="P-lines of the CPU port's timed pass (all 90 by default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-jobs", type=int, default=2, help="end-to-end jobs in flight at once")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-traversal-per-launch GPU baseline")
     ap.add_argument("--serve-rate", type=float, default=5000.0, help="extract requests per second")
@@ -153,18 +159,37 @@ def dist_init():
     return ws, rank, local
 
 
-def run_cpu_port(steps, off, sample_paths, threads):
+def run_cpu_port(steps, off, sample_paths, threads, grammar=False):
     """Times the oracle port (reference algorithm on the CPU) on the first
-    `sample_paths` traversals; returns (GB/s, seconds, text bytes, sample)."""
+    `sample_paths` traversals; returns (GB/s, seconds, text bytes, sample,
+    grammar or None).  With grammar set, the port's encoded stream, offsets
+    and rulebook come back too (copied out after its timed phases)."""
     from oracle import oracle
     k = min(sample_paths, len(off) - 1)
     s = steps[:int(off[k])]
     o = off[:k + 1].copy()
     oracle.lib()
     t0 = time.perf_counter()
-    nbytes, _, _ = oracle.roundtrip_p(s, o, 8, 1, threads)
+    r = oracle.roundtrip_p(s, o, 8, 1, threads, grammar=grammar)
     dt = time.perf_counter() - t0
-    return nbytes / dt / 1e9, dt, nbytes, f"{k} of {len(off) - 1} P-lines ({int(o[-1])} steps)"
+    nbytes = r[0]
+    return (nbytes / dt / 1e9, dt, nbytes, f"{k} of {len(off) - 1} P-lines ({int(o[-1])} steps)",
+            r[3] if grammar else None)
+
+
+def calibration():
+    """The port's time relative to the reference CLI's on the same input
+    (oracle/calibration.json), or None."""
+    p = os.path.join(ROOT, "oracle", "calibration.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        c = json.load(fh)
+    return {"port_over_reference_time": c["ratio_port_over_reference_time"]["total"],
+            "compress": c["ratio_port_over_reference_time"]["compress"],
+            "decompress": c["ratio_port_over_reference_time"]["decompress"],
+            "measured_on": f"{c['input']}, {c['threads']} threads of the build host "
+                           "(oracle/calibrate_ref.py against the reference CLI built from its sources)"}
 
 
 def serving_setup(ctx, seed: int = 5):
@@ -306,12 +331,14 @@ def reference_arm(args):
         return 0
     steps, off, _ = workload(args.scale)
     threads = os.cpu_count() or 1
+    # warm-up steps page the port's code and buffers in on a 12-line sample
+    # (untimed); every timed step is the whole workload
     for _ in range(args.warmup):
-        run_cpu_port(steps, off, args.cpu_sample_paths, threads)
+        run_cpu_port(steps, off, min(12, args.cpu_sample_paths), threads)
     vals, secs = [], []
     nbytes, sample = 0, ""
     for _ in range(args.steps):
-        v, dt, nbytes, sample = run_cpu_port(steps, off, args.cpu_sample_paths, threads)
+        v, dt, nbytes, sample, _ = run_cpu_port(steps, off, args.cpu_sample_paths, threads)
         vals.append(v)
         secs.append(dt)
     value = nbytes * len(secs) / sum(secs) / 1e9
@@ -319,14 +346,110 @@ def reference_arm(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded cfg2-shape generator)",
-           "config": {"workload": "chromosome-scale cfg2: 90 P-lines x ~5.7M steps; CPU sample per step",
+           "config": {"workload": "chromosome-scale cfg2: 90 P-lines, %d steps; the whole workload per timed step"
+                                   % len(steps),
                       "rounds": 8, "delta_round": 1, "threshold": 2},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": sample + " per step; oracle/gfaz_oracle.c (OpenMP), reference CLI "
-                                               "not buildable on the GPU host"},
+                                               "not buildable on the GPU host",
+                            "calibration": calibration()},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return 0
+
+
+def e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, device, ws):
+    """End to end through the C ABI with host buffers.  One job = pinned host
+    steps uploaded and compressed (gfz_encode), the encoded stream and rule
+    columns copied to pinned host memory (what the entropy stage consumes),
+    loaded back from there (gfz_grammar_load) and decoded to P-line text in a
+    pinned host buffer (gfz_decode_text).  args.e2e_jobs jobs are in flight
+    at once, each on its own context, CUDA stream and host buffers (host
+    threads; the library calls release the interpreter lock), so one job's
+    uploads and kernels overlap another's text download over the
+    chip-to-chip link.  Every step is one whole job with all of its copies;
+    the time is the wall clock from the first job's start to the last one's
+    end, with the device synchronised on both sides."""
+    import ctypes
+    import torch
+    import gfaz_gb300 as gz
+    from gfaz_gb300._ffi import lib as L, check
+    ntrav = len(off) - 1
+    offa = np.ascontiguousarray(off, np.uint64)
+    h_steps = torch.from_numpy(steps).pin_memory()
+    rules_cap = max(1, ginfo["num_rules"] * 2 + 1024)
+    jobs = max(1, args.e2e_jobs)
+
+    class Slot:
+        def __init__(self):
+            # above the lowest priority, which the library gives the text
+            # it writes into host memory
+            self.stream = torch.cuda.Stream(device=device, priority=-1)
+            self.ctx = gz.Context(device, self.stream.cuda_stream)
+            self.enc = torch.empty(max(1, int(ginfo["encoded_len"] * 1.5) + 1024), dtype=torch.int32).pin_memory()
+            self.f = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
+            self.s = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
+            self.text = torch.empty(int(text_bytes * 1.1) + 4096, dtype=torch.uint8).pin_memory()
+
+        def run(self):
+            ctx = self.ctx
+            h = ctypes.c_void_p()
+            check(L().gfz_encode(ctx.handle, ctypes.c_void_p(h_steps.data_ptr()), offa.ctypes.data, ntrav, 8, 2, 1,
+                                 gz.WHERE_HOST, ctypes.byref(h)))
+            g = gz.Grammar(h, ctx)
+            info = g.info()
+            eoff = np.zeros(ntrav + 1, np.uint64)
+            check(L().gfz_grammar_copy(ctx.handle, g.handle, ctypes.c_void_p(self.enc.data_ptr()), eoff.ctypes.data,
+                                       None, gz.WHERE_HOST))
+            check(L().gfz_grammar_rule_columns(ctx.handle, g.handle, ctypes.c_void_p(self.f.data_ptr()),
+                                               ctypes.c_void_p(self.s.data_ptr()), gz.WHERE_HOST))
+            del g
+            h2 = ctypes.c_void_p()
+            check(L().gfz_grammar_load(ctx.handle, ctypes.c_void_p(self.enc.data_ptr()), eoff.ctypes.data, ntrav,
+                                       ctypes.c_void_p(self.f.data_ptr()), ctypes.c_void_p(self.s.data_ptr()),
+                                       info["num_rules"], info["layer_start"], 1, gz.WHERE_HOST, ctypes.byref(h2)))
+            g2 = gz.Grammar(h2, ctx)
+            n = g2.decode_text(0, ntrav, names=names, overlaps=overlaps, out_ptr=self.text.data_ptr(),
+                               cap=self.text.numel(), where=gz.WHERE_HOST)
+            del g2
+            return info, n
+
+    slots = [Slot() for _ in range(jobs)]
+    for sl in slots:  # warm-up one after the other: each context tunes alone
+        for _ in range(max(1, args.warmup // 2)):
+            sl.run()
+    k2 = max(jobs, min(args.steps, 3 * jobs))
+    results = [None] * k2
+    errors = []
+
+    def worker(j):
+        try:
+            for i in range(j, k2, jobs):
+                results[i] = slots[j].run()
+        except Exception as e:  # reported after the join
+            errors.append(e)
+
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    ths = [threading.Thread(target=worker, args=(j,)) for j in range(jobs)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    if errors:
+        raise errors[0]
+    e2e_ms = wall * 1e3 / k2
+    info, n = results[-1]
+    heads_ok = all(bytes(sl.text[:64].numpy().tobytes()).startswith(b"P\thap0\t") for sl in slots)
+    h2d = 4 * len(steps) + 4 * info["encoded_len"] + 8 * info["num_rules"] + 8 * (ntrav + 1) * 2
+    d2h = 4 * info["encoded_len"] + 8 * info["num_rules"] + n
+    out = {"value": ws * n / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms, "jobs_in_flight": jobs, "steps": k2,
+           "text_head_ok": heads_ok}
+    del slots
+    return out
 
 
 def main():
@@ -367,6 +490,7 @@ def main():
     x, xoff = g.decode()
     parity_ok = bool(np.array_equal(xoff, off) and np.array_equal(x, steps))
     ginfo = g.info()
+    gpu_grammar = g.arrays() if not args.no_cpu_baseline and rank == 0 else None
     del g, x
 
     def barrier():
@@ -430,67 +554,21 @@ def main():
     # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        h_steps = torch.from_numpy(steps).pin_memory()
-        rules_cap = max(1, ginfo["num_rules"] * 2 + 1024)
-        h_enc = torch.empty(max(1, int(ginfo["encoded_len"] * 1.5) + 1024), dtype=torch.int32).pin_memory()
-        h_f = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
-        h_s = torch.empty(rules_cap, dtype=torch.int32).pin_memory()
-        h_text = torch.empty(int(text_bytes * 1.1) + 4096, dtype=torch.uint8).pin_memory()
-
-        import ctypes
-        from gfaz_gb300._ffi import lib as L, check
-
-        def e2e_step():
-            h = ctypes.c_void_p()
-            offa = np.ascontiguousarray(off, np.uint64)
-            check(L().gfz_encode(ctx.handle, ctypes.c_void_p(h_steps.data_ptr()), offa.ctypes.data, ntrav, 8, 2, 1,
-                                 gz.WHERE_HOST, ctypes.byref(h)))
-            g = gz.Grammar(h, ctx)
-            info = g.info()
-            eoff = np.zeros(ntrav + 1, np.uint64)
-            check(L().gfz_grammar_copy(ctx.handle, g.handle, ctypes.c_void_p(h_enc.data_ptr()), eoff.ctypes.data,
-                                       None, gz.WHERE_HOST))
-            check(L().gfz_grammar_rule_columns(ctx.handle, g.handle, ctypes.c_void_p(h_f.data_ptr()),
-                                               ctypes.c_void_p(h_s.data_ptr()), gz.WHERE_HOST))
-            del g
-            h2 = ctypes.c_void_p()
-            check(L().gfz_grammar_load(ctx.handle, ctypes.c_void_p(h_enc.data_ptr()), eoff.ctypes.data, ntrav,
-                                       ctypes.c_void_p(h_f.data_ptr()), ctypes.c_void_p(h_s.data_ptr()),
-                                       info["num_rules"], info["layer_start"], 1, gz.WHERE_HOST, ctypes.byref(h2)))
-            g2 = gz.Grammar(h2, ctx)
-            n = g2.decode_text(0, ntrav, names=names, overlaps=overlaps, out_ptr=h_text.data_ptr(),
-                               cap=h_text.numel(), where=gz.WHERE_HOST)
-            del g2
-            return info, n
-
-        for _ in range(max(1, args.warmup // 2)):
-            info, n = e2e_step()
-        k2 = max(1, min(args.steps, 3))
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        w0 = time.perf_counter()
-        for _ in range(k2):
-            info, n = e2e_step()
-        b.record(stream)
-        torch.cuda.synchronize()
-        wall = (time.perf_counter() - w0) / k2
-        ev_ms = a.elapsed_time(b) / k2
-        e2e_ms = max(ev_ms, wall * 1e3)
-        e2e_text = bytes(h_text[:min(n, 64)].numpy().tobytes())
-        h2d = 4 * len(steps) + 4 * info["encoded_len"] + 8 * info["num_rules"] + 8 * (ntrav + 1) * 2
-        d2h = 4 * info["encoded_len"] + 8 * info["num_rules"] + n
-        e2e = {"value": ws * n / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-               "text_head_ok": e2e_text.startswith(b"P\thap0\t")}
+        e2e = e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, local, ws)
 
     cpu = None
+    grammar_parity = "not compared"
+    grammar_ok = True
     if not args.no_cpu_baseline and rank == 0:
-        v, dt, nb, sample = run_cpu_port(steps, off, args.cpu_sample_paths, os.cpu_count() or 1)
+        v, dt, nb, sample, cpu_grammar = run_cpu_port(steps, off, args.cpu_sample_paths, os.cpu_count() or 1,
+                                                      grammar=True)
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s "
-                         "(oracle/gfaz_oracle.c, OpenMP)"}
+                         "(oracle/gfaz_oracle.c, OpenMP)", "calibration": calibration()}
+        if args.cpu_sample_paths >= ntrav:
+            # the GPU grammar of the parity step against the port's, element by element
+            grammar_ok = all(np.array_equal(a, b) for a, b in zip(gpu_grammar, cpu_grammar))
+            grammar_parity = "identical to the CPU port's" if grammar_ok else "MISMATCH with the CPU port's"
 
     # plain GPU form: the same kernels with one traversal per launch sequence
     # (compression encodes each P-line as its own stream, so its rulebooks
@@ -541,7 +619,8 @@ def main():
         "compress_gbps": ws * text_bytes / (comp_ms / 1e3) / 1e9,
         "decompress_gbps": ws * text_bytes / (dec_ms / 1e3) / 1e9,
         "compress_ms": comp_ms, "decompress_ms": dec_ms,
-        "parity": "decode(encode(x)) == x: %s" % ("exact" if parity_ok else "MISMATCH"),
+        "parity": {"roundtrip": "decode(encode(x)) == x: %s" % ("exact" if parity_ok else "MISMATCH"),
+                   "grammar": "encoded stream, offsets and rulebook of the whole workload " + grammar_parity},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic},
         "kernels": kernels,
@@ -557,7 +636,7 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
-    return 0 if parity_ok else 1
+    return 0 if parity_ok and grammar_ok else 1
 
 
 if __name__ == "__main__":

@@ -509,10 +509,24 @@ uint64_t orc_format_w_lines(const int32_t *steps, const uint64_t *off, uint64_t 
  * columns, then expansion + inverse delta + P-line text, on one batch of
  * traversals.  Returns the text size, or 0 on failure.  Scratch is
  * allocated here and released before returning. */
+static double wall_ms(void) {
+#ifdef _OPENMP
+  return omp_get_wtime() * 1e3;
+#else
+  return 0.0;
+#endif
+}
+
 uint64_t orc_roundtrip_p(const int32_t *raw, const uint64_t *off, uint64_t ntrav, int rounds,
                          int delta_round, char *text_out, uint64_t text_cap, int threads,
-                         uint64_t *enc_len_out, uint64_t *nrules_out) {
+                         uint64_t *enc_len_out, uint64_t *nrules_out, double *phase_ms,
+                         int32_t *enc_out, uint64_t *enc_off_out, int64_t *rules_out) {
+  /* phase_ms (optional): [0] delta + grammar + rule columns, [1] expansion +
+   * inverse delta + P text, wall-clock milliseconds.  enc_out (n entries),
+   * enc_off_out (ntrav + 1) and rules_out (n entries), when given, receive
+   * the grammar: encoded stream, its offsets and the packed rulebook. */
   threads = resolve_threads(threads);
+  const double t_start = wall_ms();
   uint64_t n = off[ntrav];
   int32_t *s = (int32_t *)malloc((n ? n : 1) * sizeof(int32_t));
   memcpy(s, raw, n * sizeof(int32_t));
@@ -528,6 +542,7 @@ uint64_t orc_roundtrip_p(const int32_t *raw, const uint64_t *off, uint64_t ntrav
   int32_t *f = (int32_t *)malloc((nr ? nr : 1) * sizeof(int32_t));
   int32_t *g = (int32_t *)malloc((nr ? nr : 1) * sizeof(int32_t));
   orc_rule_columns(rules, (uint64_t)nr, f, g);
+  const double t_mid = wall_ms();
   /* decode side: undo the column deltas, expand, inverse delta, text */
   for (int64_t i = 1; i < nr; ++i) {
     f[i] = (int32_t)((uint32_t)f[i] + (uint32_t)f[i - 1]);
@@ -568,8 +583,15 @@ uint64_t orc_roundtrip_p(const int32_t *raw, const uint64_t *off, uint64_t ntrav
     size = acc;
     free(tsz);
   }
+  if (phase_ms) {
+    phase_ms[0] = t_mid - t_start;
+    phase_ms[1] = wall_ms() - t_mid;
+  }
   if (enc_len_out) *enc_len_out = eoff[ntrav];
   if (nrules_out) *nrules_out = (uint64_t)nr;
+  if (enc_out) memcpy(enc_out, s, eoff[ntrav] * sizeof(int32_t));
+  if (enc_off_out) memcpy(enc_off_out, eoff, (ntrav + 1) * sizeof(uint64_t));
+  if (rules_out) memcpy(rules_out, rules, (uint64_t)nr * sizeof(int64_t));
   free(s); free(eoff); free(rules); free(f); free(g); free(x);
   return size;
 }

@@ -56,7 +56,7 @@ def lib():
         L.orc_append_encode.argtypes = [_P, _P, _U64, _P, _P, _P, _U64, _P, _P, _P, _P, ctypes.c_int]
         L.orc_roundtrip_p.restype = _U64
         L.orc_roundtrip_p.argtypes = [_P, _P, _U64, ctypes.c_int, ctypes.c_int, _P, _U64, ctypes.c_int,
-                                      _P, _P]
+                                      _P, _P, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -168,13 +168,26 @@ def append_encode(raw, offsets, delta_round, rules_first, rules_second, layers):
     return parts
 
 
-def roundtrip_p(raw, offsets, rounds=8, delta_round=1, threads=0):
+def roundtrip_p(raw, offsets, rounds=8, delta_round=1, threads=0, phases=False, grammar=False):
     """CPU transform round trip (delta + grammar + expansion + P text);
-    returns (text_bytes, encoded_len, nrules)."""
+    returns (text_bytes, encoded_len, nrules), plus (compress_ms,
+    decompress_ms) wall-clock phase times when phases is set, plus the
+    grammar (encoded stream, its offsets, packed rulebook) when grammar is
+    set."""
     s = np.ascontiguousarray(raw, dtype=np.int32)
     off = np.ascontiguousarray(offsets, dtype=np.uint64)
     el = np.zeros(1, np.uint64)
     nr = np.zeros(1, np.uint64)
+    ph = np.zeros(2, np.float64)
+    gram = None
+    if grammar:
+        gram = (np.empty(max(1, len(s)), np.int32), np.empty(len(off), np.uint64), np.empty(max(1, len(s)), np.int64))
+    g_ptrs = [_p(x) for x in gram] if gram else [None, None, None]
     n = lib().orc_roundtrip_p(_p(s), _p(off), len(off) - 1, rounds, delta_round, None, 0, threads,
-                              _p(el), _p(nr))
-    return int(n), int(el[0]), int(nr[0])
+                              _p(el), _p(nr), _p(ph), *g_ptrs)
+    out = (int(n), int(el[0]), int(nr[0]))
+    if phases:
+        out += ((float(ph[0]), float(ph[1])),)
+    if grammar:
+        out += ((gram[0][:int(el[0])], gram[1], gram[2][:int(nr[0])]),)
+    return out
