@@ -232,6 +232,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "decode_chunk") {
       require(value >= 0, "decode_chunk must be >= 0");
       c.decode_chunk = (uint64_t)value;
+    } else if (std::string(name) == "slot_refs") {
+      require(value == 0 || value == 1, "slot_refs must be 0 or 1");
+      c.slot_refs = value != 0;
     } else if (std::string(name) == "front_end") {
       require(value == 0 || value == 1, "front_end must be 0 (host parser) or 1 (device)");
       c.front_end = (int)value;

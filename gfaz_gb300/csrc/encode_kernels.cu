@@ -113,25 +113,31 @@ struct InsertCounts {
   uint32_t fresh = 0, repeated = 0;
 };
 
-// Sets the repeated flag; counts the key if this call set it.
-__device__ __forceinline__ void mark_repeated(PairSlot *slot, InsertCounts &c) {
-  const uint32_t old = atomicOr(&slot->flags, kFlagRepeated);
-  if (!(old & kFlagRepeated)) c.repeated++;
+// Sets the repeated flag of slot h; counts the key if this call set it, and
+// then also sets bit h of rep_bits (when given: the repeated slots as a
+// bitmap, cap bits, read by the slot-reference classification).
+__device__ __forceinline__ void mark_repeated(const PairTable &tab, uint32_t h, uint32_t *rep_bits,
+                                              InsertCounts &c) {
+  const uint32_t old = atomicOr(&tab.slots[h].flags, kFlagRepeated);
+  if (!(old & kFlagRepeated)) {
+    c.repeated++;
+    if (rep_bits) atomicOr(&rep_bits[h >> 5], 1u << (h & 31));
+  }
 }
 
 // Inserts one occurrence of canonical `key` starting at slot h, whose
 // contents (cur, fl) were already loaded.  `more` = the caller folded a
-// second occurrence into this call.  Returns false when the probe bound is
-// exceeded.
-__device__ __forceinline__ bool insert_at(const PairTable &tab, unsigned long long key, bool more, uint32_t h,
-                                          unsigned long long cur, uint32_t fl, InsertCounts &c) {
+// second occurrence into this call.  On return h is the key's slot.
+// Returns false when the probe bound is exceeded.
+__device__ __forceinline__ bool insert_at(const PairTable &tab, unsigned long long key, bool more, uint32_t &h,
+                                          unsigned long long cur, uint32_t fl, uint32_t *rep_bits, InsertCounts &c) {
   const uint32_t mask = (uint32_t)(tab.cap - 1);
   for (uint32_t p = 0; p < kMaxProbe; ++p) {
     if (cur == kEmptyKey) {
       const unsigned long long old = atomicCAS(&tab.slots[h].key, kEmptyKey, key);
       if (old == kEmptyKey) {
         c.fresh++;
-        if (more) mark_repeated(&tab.slots[h], c);
+        if (more) mark_repeated(tab, h, rep_bits, c);
         return true;
       }
       cur = old;
@@ -139,7 +145,7 @@ __device__ __forceinline__ bool insert_at(const PairTable &tab, unsigned long lo
     }
     if (cur == key) {
       // a stale flag word can only miss bits, so a set bit needs no atomic
-      if (!(fl & kFlagRepeated)) mark_repeated(&tab.slots[h], c);
+      if (!(fl & kFlagRepeated)) mark_repeated(tab, h, rep_bits, c);
       return true;
     }
     h = (h + 1) & mask;
@@ -147,6 +153,13 @@ __device__ __forceinline__ bool insert_at(const PairTable &tab, unsigned long lo
   }
   return false;
 }
+
+// Slot references (one u32 per stream position, written by the counts when
+// asked): the slot of the pair starting at the position, with bit 31 set
+// when the pair is the reverse of its canonical key; kNoPair where no pair
+// starts (a traversal's last step).  Tables up to 2^30 slots.
+constexpr uint32_t kNoPair = 0xFFFFFFFFu;
+constexpr uint32_t kRevBit = 0x80000000u;
 
 // The ITEMS + 1 steps a thread looks at: positions j0 .. j0 + ITEMS of the
 // staged tile (two 16-byte shared loads plus one element).
@@ -164,19 +177,51 @@ __device__ __forceinline__ void thread_steps(const int32_t *sv, uint32_t j0, int
 // j0 = t * ITEMS .. j0 + ITEMS - 1.  A run of equal keys inside a thread is
 // inserted once (flagged repeated when longer than one); with DEDUP the
 // lanes of a warp also fold equal keys of the same item index.
+// The slot references of K consecutive positions (see kNoPair): h = the
+// slots of the inserted positions, whose runs' dropped positions take their
+// predecessor's; cnt of them are stored at dst (16-byte stores when whole
+// and aligned).
+template <int K>
+__device__ __forceinline__ void store_srefs(uint32_t *dst, uint32_t cnt, uint32_t validb, uint32_t dropped,
+                                            uint32_t revb, const uint32_t (&h)[K]) {
+  uint32_t r[K];
+  uint32_t prev = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const uint32_t slot = ((dropped >> k) & 1u) ? prev : h[k];
+    prev = slot;
+    r[k] = ((validb >> k) & 1u) ? (slot | (((revb >> k) & 1u) ? kRevBit : 0u)) : kNoPair;
+  }
+  if (cnt == (uint32_t)K && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k += 4) *reinterpret_cast<uint4 *>(dst + k) = make_uint4(r[k], r[k + 1], r[k + 2], r[k + 3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if ((uint32_t)k < cnt) dst[k] = r[k];
+  }
+}
+
+// len = positions of the tile with a successor in the stream, tlen = all
+// its positions.  With sref (not with DEDUP: a lane whose key another lane
+// inserted does not learn the slot) the tile's slot references are stored
+// at sref[j] for tile position j; rep_bits as in mark_repeated.
 template <int ITEMS, bool DEDUP>
-__device__ __forceinline__ void count_tile(const int32_t *sv, const uint32_t *hb, uint32_t len, const PairTable &tab,
-                                           DevStatus *status, InsertCounts &c) {
+__device__ __forceinline__ void count_tile(const int32_t *sv, const uint32_t *hb, uint32_t len, uint32_t tlen,
+                                           const PairTable &tab, DevStatus *status, InsertCounts &c,
+                                           uint32_t *sref, uint32_t *rep_bits) {
   const uint32_t j0 = threadIdx.x * ITEMS;
   int32_t v[ITEMS + 1];
   thread_steps<ITEMS>(sv, j0, v);
   const uint32_t hd = bits_from(hb, j0);  // bit k: position j0 + k starts a traversal
   unsigned long long key[ITEMS];
-  uint32_t validb = 0, sameb = 0;
+  uint32_t validb = 0, sameb = 0, revb = 0;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
     const bool valid = j0 + k < len && !((hd >> (k + 1)) & 1u);
-    key[k] = canon2(pack2(v[k], v[k + 1]));
+    const unsigned long long f = pack2(v[k], v[k + 1]);
+    key[k] = canon2(f);
+    revb |= (uint32_t)(key[k] != f) << k;
     validb |= (uint32_t)valid << k;
     if (k > 0) sameb |= (uint32_t)(key[k] == key[k - 1]) << k;
   }
@@ -210,12 +255,13 @@ __device__ __forceinline__ void count_tile(const int32_t *sv, const uint32_t *hb
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
     if (((insb >> k) & 1u) && !abort) {
-      if (!insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], c)) {
+      if (!insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], rep_bits, c)) {
         atomicOr(&status->err, kErrTableFull);
         abort = true;
       }
     }
   }
+  if (!DEDUP && sref && j0 < tlen) store_srefs<ITEMS>(sref + j0, min((uint32_t)ITEMS, tlen - j0), validb, dropped, revb, h);
 }
 
 // Persistent: block b counts tiles b, b + gridDim.x, ..., the next tile
@@ -223,7 +269,8 @@ __device__ __forceinline__ void count_tile(const int32_t *sv, const uint32_t *hb
 template <int BLOCK, int ITEMS, bool DEDUP>
 __global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restrict__ s, uint64_t n,
                                                           const uint32_t *__restrict__ heads, uint64_t head_words,
-                                                          PairTable tab, DevStatus *status) {
+                                                          PairTable tab, DevStatus *status, uint32_t *sref,
+                                                          uint32_t *rep_bits) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   __shared__ __align__(128) TilePipe<TILE> P;
   __shared__ uint32_t s_fresh, s_rep;
@@ -255,7 +302,8 @@ __global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restr
     // pairs start at positions with a successor inside the stream (the head
     // bitmap marks position n too, but a caller may pass a shorter n)
     const uint32_t plen = tile * TILE + len < n ? len : len - 1;
-    count_tile<ITEMS, DEDUP>(P.sv[b], P.hb[b], plen, tab, status, c);
+    count_tile<ITEMS, DEDUP>(P.sv[b], P.hb[b], plen, len, tab, status, c, sref ? sref + tile * TILE : nullptr,
+                             rep_bits);
     pipe_release();
     if (!has_next) break;
     tile = next;
@@ -280,7 +328,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_count_pairs(const int32_t *__restr
 // system sees as many of them at once as threads are resident.
 __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict__ s, uint64_t n,
                                                        const uint32_t *__restrict__ heads, PairTable tab,
-                                                       DevStatus *status) {
+                                                       DevStatus *status, uint32_t *sref, uint32_t *rep_bits) {
   __shared__ uint32_t s_fresh, s_rep;
   if (threadIdx.x == 0) {
     s_fresh = 0;
@@ -290,22 +338,27 @@ __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict
   InsertCounts c;
   const uint32_t mask = (uint32_t)(tab.cap - 1);
   uint32_t it = 0;
-  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p + 1 < n;
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
        p += (uint64_t)gridDim.x * blockDim.x) {
     // a full table (some chain ran past the probe limit) ends every thread
     // within 16 of its pairs
     if ((++it & 15u) == 0 && (*(volatile uint32_t *)&status->err & kErrTableFull)) break;
     const uint64_t q = p + 1;
-    if ((heads[q >> 5] >> (q & 31)) & 1u) continue;  // q opens a traversal
-    const unsigned long long key = canon2(pack2(s[p], s[q]));
-    const uint32_t h = hash_pair(key) & mask;
+    if (q >= n || ((heads[q >> 5] >> (q & 31)) & 1u)) {  // no pair: q ends the stream or opens a traversal
+      if (sref) sref[p] = kNoPair;
+      continue;
+    }
+    const unsigned long long f = pack2(s[p], s[q]);
+    const unsigned long long key = canon2(f);
+    uint32_t h = hash_pair(key) & mask;
     unsigned long long cur;
     uint32_t fl;
     load_slot(&tab.slots[h], cur, fl);
-    if (!insert_at(tab, key, false, h, cur, fl, c)) {
+    if (!insert_at(tab, key, false, h, cur, fl, rep_bits, c)) {
       atomicOr(&status->err, kErrTableFull);
       break;
     }
+    if (sref) sref[p] = h | (key != f ? kRevBit : 0u);
   }
   const uint32_t f = __reduce_add_sync(0xffffffffu, c.fresh);
   const uint32_t r = __reduce_add_sync(0xffffffffu, c.repeated);
@@ -325,7 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict
 // when longer than one), as in the tiled kernel, but with no barrier.
 __global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restrict__ s, uint64_t n,
                                                         const uint32_t *__restrict__ heads, PairTable tab,
-                                                        DevStatus *status) {
+                                                        DevStatus *status, uint32_t *sref, uint32_t *rep_bits) {
   constexpr int K = 4;
   __shared__ uint32_t s_fresh, s_rep;
   if (threadIdx.x == 0) {
@@ -338,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restric
   const bool aligned = (reinterpret_cast<uintptr_t>(s) & 15u) == 0;
   bool full = false;
   uint32_t it = 0;
-  for (uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * K; p0 + 1 < n && !full;
+  for (uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * K; p0 < n && !full;
        p0 += (uint64_t)gridDim.x * blockDim.x * K) {
     if ((++it & 3u) == 0 && (*(volatile uint32_t *)&status->err & kErrTableFull)) break;  // as in k_count_flat
     int32_t v[K + 1];
@@ -353,10 +406,12 @@ __global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restric
     const uint32_t w = (uint32_t)(p0 >> 5);
     const uint32_t hd = (uint32_t)((((unsigned long long)heads[w + 1] << 32) | heads[w]) >> (p0 & 31));
     unsigned long long key[K];
-    uint32_t validb = 0, sameb = 0;
+    uint32_t validb = 0, sameb = 0, revb = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      key[k] = canon2(pack2(v[k], v[k + 1]));
+      const unsigned long long f = pack2(v[k], v[k + 1]);
+      key[k] = canon2(f);
+      revb |= (uint32_t)(key[k] != f) << k;
       validb |= (uint32_t)(p0 + k + 1 < n && !((hd >> (k + 1)) & 1u)) << k;
       if (k > 0) sameb |= (uint32_t)(key[k] == key[k - 1]) << k;
     }
@@ -375,11 +430,13 @@ __global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restric
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      if (((insb >> k) & 1u) && !full && !insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], c)) {
+      if (((insb >> k) & 1u) && !full &&
+          !insert_at(tab, key[k], (moreb >> k) & 1u, h[k], cur[k], fl[k], rep_bits, c)) {
         atomicOr(&status->err, kErrTableFull);
         full = true;
       }
     }
+    if (sref && !full) store_srefs<K>(sref + p0, (uint32_t)min((uint64_t)K, n - p0), validb, dropped, revb, h);
   }
   const uint32_t f = __reduce_add_sync(0xffffffffu, c.fresh);
   const uint32_t r = __reduce_add_sync(0xffffffffu, c.repeated);
@@ -694,6 +751,42 @@ __global__ void __launch_bounds__(BLOCK) k_apply_classify_flat(const int32_t *__
   if (threadIdx.x == 0) tile_agg[tile] = par_encode(total);
 }
 
+// Classification from slot references: the candidate bit of a position is
+// the repeated bit of its slot (rep_bits, set by the count), so no key is
+// formed and no table probed.  One tile per block, as k_apply_classify_flat.
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_apply_classify_sref(const uint32_t *__restrict__ sref, uint64_t n,
+                                                               const uint32_t *__restrict__ rep_bits,
+                                                               uint32_t *__restrict__ tword,
+                                                               unsigned long long *__restrict__ tile_agg) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(ITEMS == 8 && TILE <= 2048, "a thread word holds 8 candidate bits and 11-bit counts");
+  __shared__ ParAgg s_warp[BLOCK / 32];
+  const uint64_t tile = blockIdx.x;
+  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  uint32_t ref[ITEMS];
+  if (p0 + ITEMS <= n && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(sref + p0);
+    const uint4 b = *reinterpret_cast<const uint4 *>(sref + p0 + 4);
+    ref[0] = a.x; ref[1] = a.y; ref[2] = a.z; ref[3] = a.w;
+    ref[4] = b.x; ref[5] = b.y; ref[6] = b.z; ref[7] = b.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) ref[k] = p0 + k < n ? sref[p0 + k] : kNoPair;
+  }
+  uint32_t word[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) word[k] = ref[k] != kNoPair ? rep_bits[(ref[k] & ~kRevBit) >> 5] : 0u;
+  uint32_t cbits = 0;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k)
+    cbits |= (uint32_t)(ref[k] != kNoPair && ((word[k] >> (ref[k] & 31)) & 1u)) << k;
+  ParAgg total;
+  const ParAgg excl = block_par_scan<BLOCK>(par_of_bits(cbits, ITEMS), total, s_warp);
+  tword[tile * BLOCK + threadIdx.x] = cbits | ((excl.xo & 3u) << 8) | (excl.c0 << 10) | (excl.c1 << 21);
+  if (threadIdx.x == 0) tile_agg[tile] = par_encode(total);
+}
+
 // state[t] = the state (x, replaced count) before tile t, encoded x | c << 1.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_tile_states(const unsigned long long *__restrict__ tile_agg,
@@ -736,13 +829,16 @@ __global__ void __launch_bounds__(BLOCK) k_tile_states(const unsigned long long 
 // their output positions.  v = the thread's ITEMS steps and the next one;
 // tw / st / ag = the thread's word, the tile's carried-in state and its
 // aggregate; tlo = the tile's first traversal; so / lidx = shared scratch.
-template <int BLOCK, int ITEMS>
+// With SREF the rules of the replaced positions come from their slot
+// references ref[] (written by the count) instead of a second table lookup,
+// and a slot already set in used_bits takes no atomic.
+template <int BLOCK, int ITEMS, bool SREF = false>
 __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_t tile, uint64_t n, uint32_t tw,
                                           unsigned long long st, unsigned long long ag, const uint64_t *s_tlo,
                                           const uint64_t *__restrict__ off, uint64_t ntrav, const PairTable &tab,
                                           int32_t temp_base, int32_t *__restrict__ out, uint64_t out_shift,
                                           uint64_t *__restrict__ new_off, uint32_t *used_bits, DevStatus *status,
-                                          int32_t *so, uint16_t *lidx) {
+                                          int32_t *so, uint16_t *lidx, const uint32_t (&ref)[ITEMS]) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   const uint32_t j0 = threadIdx.x * ITEMS;
   const uint64_t base = tile * TILE;
@@ -770,7 +866,20 @@ __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_
   }
   // the rules of the replaced positions
   uint32_t slot[ITEMS], fl[ITEMS], fwdb;
-  lookup_pairs<ITEMS>(v, xbits, tab, slot, fl, fwdb, status);
+  if (SREF) {
+    fwdb = 0;
+    uint32_t uw[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      slot[k] = ref[k] & ~kRevBit;
+      fwdb |= (uint32_t)((ref[k] & kRevBit) == 0) << k;
+      uw[k] = ((xbits >> k) & 1u) ? used_bits[slot[k] >> 5] : 0u;  // all gathers in flight together
+    }
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) fl[k] = ((uw[k] >> (slot[k] & 31)) & 1u) ? kFlagUsed : 0u;
+  } else {
+    lookup_pairs<ITEMS>(v, xbits, tab, slot, fl, fwdb, status);
+  }
   // kept positions of the tile before j0: j0 minus the consumed ones (the
   // carried-in position and the partner of every replaced position before
   // j0, except a replaced j0 - 1 whose partner is j0 itself)
@@ -806,7 +915,7 @@ __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_
       if (__any_sync(0xffffffffu, nk)) {
         const uint32_t peers = __match_any_sync(0xffffffffu, nk ? slot[k] : 0xFFFFFFFFu);
         if (nk && (peers & lanemask_lt()) == 0) {
-          atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
+          if (!SREF) atomicOr(&tab.slots[slot[k]].flags, kFlagUsed);
           atomicOr(&used_bits[slot[k] >> 5], 1u << (slot[k] & 31));
         }
       }
@@ -876,8 +985,9 @@ __global__ void __launch_bounds__(BLOCK, 3) k_apply_emit(const int32_t *__restri
     }
     int32_t v[ITEMS + 1];
     thread_steps<ITEMS>(P.sv[b], j0, v);
+    const uint32_t no_ref[ITEMS] = {};
     emit_tile<BLOCK, ITEMS>(v, tile, n, tw_cur, st_cur, ag_cur, &s_tlo, off, ntrav, tab, temp_base, out, 0,
-                            new_off, used_bits, status, so, lidx);
+                            new_off, used_bits, status, so, lidx, no_ref);
     pipe_release();
     if (!has_next) break;
     tile = next;
@@ -928,8 +1038,55 @@ __global__ void __launch_bounds__(BLOCK) k_apply_emit_flat(const int32_t *__rest
 #pragma unroll
     for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? sl[k] : 0;
   }
+  const uint32_t no_ref[ITEMS] = {};
   emit_tile<BLOCK, ITEMS>(v, tile, n, tw, st, ag, &s_tlo, off, ntrav, tab, temp_base, out, out_shift, new_off,
-                          used_bits, status, so, lidx);
+                          used_bits, status, so, lidx, no_ref);
+}
+
+// Emit from slot references: one tile per block (as k_apply_emit_flat on a
+// whole resident stream), the replaced positions' rules read from sref.
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_apply_emit_sref(const int32_t *__restrict__ s,
+                                                           const uint32_t *__restrict__ sref, uint64_t n,
+                                                           const uint32_t *__restrict__ tword,
+                                                           const unsigned long long *__restrict__ tile_agg,
+                                                           const unsigned long long *__restrict__ state,
+                                                           const uint64_t *__restrict__ off, uint64_t ntrav,
+                                                           const uint64_t *__restrict__ tile_trav, PairTable tab,
+                                                           int32_t temp_base, int32_t *__restrict__ out,
+                                                           uint64_t *__restrict__ new_off, uint32_t *used_bits,
+                                                           DevStatus *status) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  static_assert(TILE < (1u << 16), "tile must fit 16-bit local indices");
+  static_assert(ITEMS == 8, "lidx packs eight 16-bit indices per thread");
+  __shared__ __align__(16) int32_t so[TILE + 4];
+  __shared__ __align__(16) uint16_t lidx[TILE];
+  __shared__ uint64_t s_tlo;
+  const uint64_t tile = blockIdx.x;
+  if (threadIdx.x == 0) s_tlo = tile_trav[tile];
+  const uint32_t tw = tword[tile * BLOCK + threadIdx.x];
+  const unsigned long long st = state[tile], ag = tile_agg[tile];
+  const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
+  int32_t v[ITEMS + 1];
+  uint32_t ref[ITEMS];
+  if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0 && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
+    const int4 a = *reinterpret_cast<const int4 *>(s + p0);
+    const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
+    const uint4 ra = *reinterpret_cast<const uint4 *>(sref + p0);
+    const uint4 rb = *reinterpret_cast<const uint4 *>(sref + p0 + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    v[8] = s[p0 + ITEMS];
+    ref[0] = ra.x; ref[1] = ra.y; ref[2] = ra.z; ref[3] = ra.w;
+    ref[4] = rb.x; ref[5] = rb.y; ref[6] = rb.z; ref[7] = rb.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k <= ITEMS; ++k) v[k] = p0 + k < n ? s[p0 + k] : 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) ref[k] = p0 + k < n ? sref[p0 + k] : kNoPair;
+  }
+  emit_tile<BLOCK, ITEMS, true>(v, tile, n, tw, st, ag, &s_tlo, off, ntrav, tab, temp_base, out, 0, new_off,
+                                used_bits, status, so, lidx, ref);
 }
 
 // ---------------------------------------------------------------------------
@@ -1373,14 +1530,15 @@ void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaS
 }
 
 void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
-                        CountKernel kind, cudaStream_t st) {
+                        CountKernel kind, cudaStream_t st, uint32_t *sref, uint32_t *rep_bits) {
   if (!n) return;
   if (kind == CountKernel::kFlat) {
-    k_count_flat<<<grid_for(n, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status);
+    k_count_flat<<<grid_for(n, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status, sref, rep_bits);
     return;
   }
   if (kind == CountKernel::kFlat4) {
-    k_count_flat4<<<grid_for((n + 3) / 4, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status);
+    k_count_flat4<<<grid_for((n + 3) / 4, kBlock, 152u * 8u * 16u), kBlock, 0, st>>>(s, n, heads, tab, status, sref,
+                                                                                        rep_bits);
     return;
   }
   constexpr uint64_t TILE = kBlock * kCountItems;
@@ -1388,10 +1546,10 @@ void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, Pai
   const uint64_t hw = head_words(n);
   if (kind == CountKernel::kTiledWarpDedup) {
     auto k = k_count_pairs<kBlock, kCountItems, true>;
-    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status);
+    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status, nullptr, rep_bits);
   } else {
     auto k = k_count_pairs<kBlock, kCountItems, false>;
-    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status);
+    k<<<persistent_grid(k, kBlock, tiles), kBlock, 0, st>>>(s, n, heads, hw, tab, status, sref, rep_bits);
   }
 }
 
@@ -1452,6 +1610,23 @@ void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, 
   auto k = k_apply_classify<kBlock, kApplyItems>;
   k<<<persistent_grid(k, kBlock, apply_num_tiles(n)), kBlock, 0, st>>>(s, n, heads, head_words(n), tab, w.tword,
                                                                        w.tile_agg, status);
+}
+
+void launch_apply_classify_sref(const uint32_t *sref, uint64_t n, const uint32_t *rep_bits, const ApplyScratch &w,
+                                cudaStream_t st) {
+  if (!n) return;
+  k_apply_classify_sref<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(sref, n, rep_bits,
+                                                                                               w.tword, w.tile_agg);
+}
+
+void launch_apply_emit_sref(const int32_t *s, const uint32_t *sref, uint64_t n, const uint64_t *off, uint64_t ntrav,
+                            const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out,
+                            uint64_t *new_off, uint32_t *used_bits, const ApplyScratch &w, DevStatus *status,
+                            cudaStream_t st) {
+  if (!n) return;
+  k_apply_emit_sref<kBlock, kApplyItems><<<(unsigned)apply_num_tiles(n), kBlock, 0, st>>>(
+      s, sref, n, w.tword, w.tile_agg, w.state, off, ntrav, tile_trav, tab, temp_base, out, new_off, used_bits,
+      status);
 }
 
 void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st) {

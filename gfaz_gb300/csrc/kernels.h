@@ -53,9 +53,14 @@ void launch_head_bits(const uint64_t *off, uint64_t ntrav, uint32_t *bits, cudaS
 // also folds equal keys across a warp; kFlat takes one pair per thread
 // without staging or barriers (streams of mostly new pairs); kFlat4 takes
 // four and folds their runs, still without barriers.
+// With sref (n entries; not with kTiledWarpDedup; tables of at most 2^30
+// slots) every position p gets its slot reference: the slot of the pair
+// starting at p, bit 31 set when the pair is the reverse of its canonical
+// key, 0xFFFFFFFF where no pair starts; with rep_bits (cap bits, zeroed with
+// the table) the slot of every key that becomes repeated is set in it.
 enum class CountKernel { kTiled = 0, kTiledWarpDedup = 1, kFlat = 2, kFlat4 = 3 };
 void launch_count_pairs(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, DevStatus *status,
-                        CountKernel kind, cudaStream_t st);
+                        CountKernel kind, cudaStream_t st, uint32_t *sref = nullptr, uint32_t *rep_bits = nullptr);
 
 // Greedy left-to-right replacement of candidate pairs; writes the compacted
 // stream with temporary symbols +-(temp_base + slot), the new traversal
@@ -75,6 +80,15 @@ struct ApplyScratch {
 // and compacted output.
 void launch_apply_classify(const int32_t *s, uint64_t n, const uint32_t *heads, PairTable tab, const ApplyScratch &w,
                            bool flat, DevStatus *status, cudaStream_t st);
+// The classification and emit passes from the count's slot references and
+// repeated-slot bitmap (a resident stream; no table probes).  The same
+// output as the probing passes.
+void launch_apply_classify_sref(const uint32_t *sref, uint64_t n, const uint32_t *rep_bits, const ApplyScratch &w,
+                                cudaStream_t st);
+void launch_apply_emit_sref(const int32_t *s, const uint32_t *sref, uint64_t n, const uint64_t *off, uint64_t ntrav,
+                            const uint64_t *tile_trav, PairTable tab, int32_t temp_base, int32_t *out,
+                            uint64_t *new_off, uint32_t *used_bits, const ApplyScratch &w, DevStatus *status,
+                            cudaStream_t st);
 void launch_apply_states(uint64_t n, const ApplyScratch &w, DevStatus *status, cudaStream_t st);
 // Emit also sets bit `slot` of used_bits (cap bits, zeroed) for every slot
 // it flags used; flat = one tile per block, read from global memory.

@@ -78,6 +78,7 @@ uint64_t ceil_log2(uint64_t x) {
 
 
 constexpr uint64_t kMaxTableCap = 1ULL << 31;
+constexpr uint64_t kSrefMaxCap = 1ULL << 30;  // largest table whose slots fit a slot reference
 
 // cap scaled down by 2^shift (up by 2^-shift when negative), kept within
 // [2^16, the table limit].
@@ -134,7 +135,12 @@ Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullp
   if (stream) {
     stream_ = stream;
   } else {
-    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    // one step above the lowest priority, which the link-bound text of
+    // low_stream() takes
+    int least = 0, greatest = 0;
+    cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priority range");
+    cuda_check(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, least > greatest ? least - 1 : least),
+               "cudaStreamCreate");
     own_stream_ = true;
   }
   // keep freed pool memory cached: repeated calls reuse it without syncs
@@ -145,6 +151,8 @@ Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullp
   }
   desc_ = DevVec<unsigned long long>(stream_);
   counter_ = DevVec<uint32_t>(stream_);
+  sref_buf = DevVec<uint32_t>(stream_);
+  rep_buf = DevVec<uint32_t>(stream_);
   cuda_check(cudaMalloc((void **)&d_status_, sizeof(DevStatus)), "status alloc");
   cuda_check(cudaMallocHost((void **)&h_status_, sizeof(DevStatus)), "status alloc");
   std::memset(h_status_, 0, sizeof(DevStatus));
@@ -181,8 +189,12 @@ Context::~Context() {
     cudaEventDestroy(p.b);
   }
   for (auto e : event_pool_) cudaEventDestroy(e);
+  // every device vector of the context frees on its stream: before the
+  // stream is destroyed below
   desc_.release();
   counter_.release();
+  sref_buf.release();
+  rep_buf.release();
   cudaStreamSynchronize(stream_);
   cudaFree(d_status_);
   cudaFreeHost(h_status_);
@@ -190,7 +202,28 @@ Context::~Context() {
     if (h.pinned) cudaFreeHost(h.p);
     else std::free(h.p);
   }
+  if (low_) {
+    cudaStreamSynchronize(low_);
+    cudaStreamDestroy(low_);
+    for (auto e : order_ev_) cudaEventDestroy(e);
+  }
   if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+cudaStream_t Context::low_stream() {
+  if (!low_) {
+    int least = 0, greatest = 0;
+    cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priority range");
+    cuda_check(cudaStreamCreateWithPriority(&low_, cudaStreamNonBlocking, least), "low-priority stream");
+    for (auto &e : order_ev_) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  }
+  return low_;
+}
+
+void Context::order(cudaStream_t from, cudaStream_t to) {
+  cudaEvent_t e = order_ev_[from == stream_ ? 0 : 1];
+  cuda_check(cudaEventRecord(e, from), "event record");
+  cuda_check(cudaStreamWaitEvent(to, e, 0), "stream wait");
 }
 
 int32_t *Context::host_buffer(int i, uint64_t n) {
@@ -366,9 +399,13 @@ static void sort_used_rules(Context &ctx, PairTable tab, uint64_t U, uint32_t by
 // +-(temp_base + slot).  Writes B and offB and sets the bit of every used
 // slot in used_bits (zeroed, tab.cap bits); the output length lands in
 // status u64[2] for the caller to read.
+// With sref / rep_bits (the count's slot references and repeated-slot
+// bitmap) the classification and emit passes read them instead of probing
+// the table.
 static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint64_t *offA, uint64_t ntrav,
                           const uint32_t *heads, PairTable tab, int32_t temp_base, int32_t *B, uint64_t *offB,
-                          uint32_t *used_bits, int cls, ReplaceWork &w) {
+                          uint32_t *used_bits, int cls, ReplaceWork &w, const uint32_t *sref = nullptr,
+                          const uint32_t *rep_bits = nullptr) {
   cudaStream_t st = ctx.stream();
   DevStatus *ds = ctx.dstatus();
   const uint64_t tiles = apply_num_tiles(n);
@@ -380,6 +417,14 @@ static void replace_pairs(Context &ctx, const int32_t *A, uint64_t n, const uint
   w.tile_state.resize(std::max<uint64_t>(tiles, 1));
   GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA, ntrav, n, w.tile_trav.ptr, st));
   const ApplyScratch sc{w.tword.ptr, w.tile_agg.ptr, w.tile_state.ptr, desc, counter};
+  if (sref) {
+    GFZ_TIMED_B(ctx, "apply_classify", 4.0 * n, launch_apply_classify_sref(sref, n, rep_bits, sc, st));
+    GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
+    GFZ_TIMED_B(ctx, "apply_emit", 8.0 * n,
+                launch_apply_emit_sref(A, sref, n, offA, ntrav, w.tile_trav.ptr, tab, temp_base, B, offB, used_bits, sc,
+                                       ds, st));
+    return;
+  }
   // classify variant: forced by option, else tuned per stream class like
   // the count kernel (both write the same words); emit follows the choice
   // (it flags rules used, so a second timing run would not be alike)
@@ -422,6 +467,8 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
   DevVec<unsigned long long> &ukeys = su.keys;
   DevVec<uint32_t> &uslots = su.slots;
   DevVec<uint32_t> heads(st), used_bits(st);
+  // the count's slot references and repeated-slot bitmap, kept by the context
+  DevVec<uint32_t> &sref = ctx.sref_buf, &rep_bits = ctx.rep_buf;
   ReplaceWork rw(st);
 
   for (int round = round0; round < rounds; ++round) {
@@ -465,6 +512,23 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       if (it != ctx.tuned.end()) kind = (CountKernel)it->second;
       else tune = true;
     }
+    // slot references: every count kernel but the warp-folding one records
+    // them (the tuner's candidates never include it)
+    const bool use_sref = ctx.slot_refs && kind != CountKernel::kTiledWarpDedup;
+    uint32_t *d_sref = nullptr, *d_rep = nullptr;
+    if (use_sref) {
+      sref.resize(n);
+      d_sref = sref.ptr;
+    }
+    // the table cleared for a count, with its repeated-slot bitmap
+    auto prepare = [&](uint64_t c) {
+      tab.prepare(c, st);
+      if (use_sref) {
+        rep_bits.resize((c + 31) / 32);
+        cuda_check(cudaMemsetAsync(rep_bits.ptr, 0, (c + 31) / 32 * sizeof(uint32_t), st), "repeated bitmap clear");
+        d_rep = rep_bits.ptr;
+      }
+    };
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
       if (tune) {
@@ -475,9 +539,10 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
         bool refill = false;
         const uint64_t ns = tune_len(ctx, n);
         for (int i = 0; i < 3; ++i) {
-          tab.prepare(cap, st);
+          prepare(cap);
           ctx.reset_status();
-          t[i] = ctx.time_launches([&] { launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(cap), ds, cand[i], st); });
+          t[i] = ctx.time_launches(
+              [&] { launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(cap), ds, cand[i], st, d_sref, d_rep); });
           const DevStatus &s0 = ctx.read_status();
           if ((s0.err & kErrTableFull) || s0.u64[0] * 10 > cap * 8) {
             refill = true;
@@ -499,10 +564,10 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
         tune = false;
         continue;  // the full count
       } else {
-        tab.prepare(cap, st);
+        prepare(cap);
         ctx.reset_status();
-        GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n,
-                    launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
+        GFZ_TIMED_B(ctx, "count_pairs", (use_sref ? 8.0 : 4.0) * n,
+                    launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st, d_sref, d_rep));
       }
       const DevStatus &s = ctx.read_status();
       distinct = s.u64[0];
@@ -530,8 +595,8 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       for (const uint64_t c : caps) {
         ctx.reset_status();
         const float t = ctx.time_launches([&] {
-          tab.prepare(c, st);
-          launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(c), ds, kind, st);
+          prepare(c);
+          launch_count_pairs(A.ptr, ns, heads.ptr, tab.view(c), ds, kind, st, d_sref, d_rep);
         });
         // a probe chain past its limit at this load: not a candidate (the
         // next reset clears the bit)
@@ -547,9 +612,10 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       ctx.record_tuned(Context::kTuneCap, cap_cls, (int)ceil_log2(cap_default) - (int)ceil_log2(best));
       cap = best;
       // the timed runs cleared the table: the full count at the kept size
-      tab.prepare(cap, st);
+      prepare(cap);
       ctx.reset_status();
-      GFZ_TIMED_B(ctx, "count_pairs", 4.0 * n, launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st));
+      GFZ_TIMED_B(ctx, "count_pairs", (use_sref ? 8.0 : 4.0) * n,
+                  launch_count_pairs(A.ptr, n, heads.ptr, tab.view(cap), ds, kind, st, d_sref, d_rep));
       ctx.read_status();
       ctx.check_status("count_pairs");
     }
@@ -562,8 +628,11 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
     used_bits.resize((cap + 31) / 32);
     cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
+    // slot references hold slots below 2^30 (bit 31 and one value are
+    // taken); a larger table is classified and emitted by probing
+    const bool by_sref = use_sref && cap <= kSrefMaxCap;
     replace_pairs(ctx, A.ptr, n, offA.ptr, ntrav, heads.ptr, tab.view(cap), temp_base, B.ptr, offB.ptr,
-                  used_bits.ptr, cls, rw);
+                  used_bits.ptr, cls, rw, by_sref ? d_sref : nullptr, by_sref ? d_rep : nullptr);
     ukeys.resize(std::max<uint64_t>(repeated, 1));
     uslots.resize(std::max<uint64_t>(repeated, 1));
     GFZ_TIMED_B(ctx, "collect_used", cap / 8.0,
@@ -600,6 +669,11 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
   }
   ctx.read_status();
   ctx.check_status("rule sort");
+  if (ctx.hbm_budget) {
+    // under a device-memory budget the round scratch is not kept
+    sref.release();
+    rep_bits.release();
+  }
 }
 
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
@@ -673,7 +747,8 @@ uint64_t resident_bytes(uint64_t n, uint64_t prev_distinct, uint64_t nrules) {
   uint64_t est = prev_distinct ? prev_distinct * 3 : std::min<uint64_t>(n / 8, 1u << 22);
   est = std::min(est, n);
   const uint64_t cap = next_pow2(std::max<uint64_t>(est * 2, 1u << 16));
-  return 8 * n + n / 8 + n / 2 + n / 32 + 16 * cap + cap / 8 + 6 * cap + 8 * (nrules + n / 2) + (64ull << 20);
+  // + the count's slot references (4 B per step) and repeated-slot bitmap
+  return 12 * n + n / 8 + n / 2 + n / 32 + 16 * cap + cap / 4 + 6 * cap + 8 * (nrules + n / 2) + (64ull << 20);
 }
 
 // Copies steps [a, b) of the stream made of segs (back to back) to dst.
@@ -1090,9 +1165,10 @@ void exclusive_scan(Context &ctx, const uint64_t *in, uint64_t n, uint64_t *out,
 
 bool resident_fits(const Context &ctx, uint64_t n) {
   if (ctx.encode_chunk) return false;
-  // input, two stream buffers, per-tile words, a pair table
+  // input, two stream buffers, the count's slot references, per-tile words,
+  // a pair table
   return !ctx.hbm_budget ||
-         12 * n + n / 2 + (64ull << 20) + 16 * std::min<uint64_t>(n, 1ull << 23) <= ctx.hbm_budget;
+         16 * n + n / 2 + (64ull << 20) + 16 * std::min<uint64_t>(n, 1ull << 23) <= ctx.hbm_budget;
 }
 
 void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
@@ -1532,9 +1608,13 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   ctx.check_status("text lengths");
   const uint64_t size = body + pieces.tail.size();
   char *dst;
+  bool to_host = false;
   if (direct) {
     if (direct_cap < size) throw std::length_error("output buffer too small");
     dst = direct;
+    cudaPointerAttributes a{};
+    to_host = cudaPointerGetAttributes(&a, direct) == cudaSuccess && a.type == cudaMemoryTypeHost;
+    (void)cudaGetLastError();
   } else {
     text.resize(std::max<uint64_t>(size, 1));
     text.size = size;
@@ -1544,8 +1624,17 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   DevVec<uint64_t> toff(st);
   toff.resize(std::max<uint64_t>(expand_num_tiles(P.total), 1));
   GFZ_TIMED(ctx, "symbol_text", launch_tile_text_off(E, T, g.delta_round, soff.ptr, sdig.ptr, toff.ptr, st));
-  GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
-              launch_text_write(E, T, g.delta_round, toff.ptr, dst, st));
+  if (to_host) {
+    // bound by the chip-to-chip link: on the low-priority stream
+    cudaStream_t low = ctx.low_stream();
+    ctx.order(st, low);
+    GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
+                launch_text_write(E, T, g.delta_round, toff.ptr, dst, low);
+                ctx.order(low, st));
+  } else {
+    GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
+                launch_text_write(E, T, g.delta_round, toff.ptr, dst, st));
+  }
   if (!pieces.tail.empty())
     cuda_check(cudaMemcpyAsync(dst + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyDefault, st),
                "text tail");

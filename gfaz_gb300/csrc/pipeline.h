@@ -133,6 +133,7 @@ class Context {
   uint64_t hbm_budget = 0;       // device bytes host-input compression may use (0 = no limit)
   uint64_t encode_chunk = 0;     // steps per chunk of host-input compression (0 = from the budget)
   uint64_t decode_chunk = 0;     // expanded steps per device text pass of the full-file writer (0 = all)
+  bool slot_refs = true;         // resident rounds: the count records slot references for classify / emit
   int count_kernel = -1;         // CountKernel forced by option; -1 = chosen by the tuner
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
@@ -155,11 +156,27 @@ class Context {
   // calls (chunked compression's host stream buffers); pageable memory when
   // page-locking fails.
   int32_t *host_buffer(int i, uint64_t n);
+  // A stream of the lowest priority, made on first use: the P/W text that
+  // gfz_decode_text writes into host memory runs there, bound by the
+  // chip-to-chip link for tens of ms, so that kernels of streams of higher
+  // priority (another context's compression) take SMs as its blocks retire
+  // instead of waiting for the whole text kernel.
+  cudaStream_t low_stream();
+  // Makes `to` wait for the work queued so far on `from` (this context's
+  // stream and its low-priority stream).
+  void order(cudaStream_t from, cudaStream_t to);
+  // Scratch of the grammar rounds kept for later calls, so that repeated
+  // compressions do not return gigabytes to the pool and take them back
+  // (the pool then spends milliseconds mapping memory for the next call):
+  // the count's slot references and its repeated-slot bitmap.
+  DevVec<uint32_t> sref_buf, rep_buf;
 
  private:
   int device_ = 0, sms_ = 152;
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
+  cudaStream_t low_ = nullptr;
+  cudaEvent_t order_ev_[2] = {nullptr, nullptr};
   DevStatus *d_status_ = nullptr;
   DevStatus *h_status_ = nullptr;
   DevVec<unsigned long long> desc_;
@@ -237,11 +254,11 @@ void exclusive_scan(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out,
 void exclusive_scan(Context &ctx, const uint64_t *in, uint64_t n, uint64_t *out, const char *timer);
 
 // Whether compression of n steps runs resident in HBM under ctx's budget
-// and chunk options (working set about 12.5 bytes per step).
+// and chunk options (working set about 16.5 bytes per step).
 bool resident_fits(const Context &ctx, uint64_t n);
 
 // Compression of host-resident input: resident in HBM when its working set
-// (about 12.5 bytes per step) fits ctx.hbm_budget, else in chunks
+// (about 16.5 bytes per step) fits ctx.hbm_budget, else in chunks
 // (encode_host_chunked) sized from the budget or ctx.encode_chunk.
 void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vector<uint64_t> &h_off,
                  const EncodeParams &p, Grammar &g);

@@ -59,7 +59,12 @@ int gfz_has_gpu(void);
 unsigned gfz_zstd_version(void);
 
 /* ---- contexts ------------------------------------------------------------ */
-/* cuda_stream may be NULL (the context creates its own stream).  Grammars
+/* cuda_stream may be NULL (the context creates its own stream, one step
+ * above the lowest priority).  Text that gfz_decode_text writes into host
+ * memory is bound by the chip-to-chip link; its kernel runs on a stream of
+ * the lowest priority ordered after the context's stream, so that work of
+ * other streams of higher priority (another context's compression) takes
+ * SMs while it runs.  Grammars
  * free their device memory on the stream of the context that made them:
  * free them before that context, and keep a caller's stream alive until
  * the context is destroyed. */
@@ -81,9 +86,13 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * the tiled and the flat kernels, timed the first time the context meets a
  * stream class (length, repeat density) and remembered, 0 = tiled, 1 =
  * tiled with warp folding, 2 = flat (one pair per thread), 3 = flat with
- * four pairs per thread and run folding; "classify_kernel"
- * = the candidate classification pass, tuned alike: -1 (default), 0 =
- * persistent with staged tiles, 1 = flat (one tile per block);
+ * four pairs per thread and run folding; "slot_refs" = 1 (default): the
+ * count records each position's table slot, and the candidate
+ * classification and the replacement read it instead of probing the table
+ * again (0 = probe; the same result); "classify_kernel" = the candidate
+ * classification pass when it probes the table (slot references off),
+ * tuned alike: -1 (default), 0 = persistent with staged tiles, 1 = flat
+ * (one tile per block);
  * "hbm_budget" = device bytes that compression of host-resident input may
  * use (default 0 = no limit): above it the stream stays in host memory and
  * passes through HBM in chunks, with identical output; "encode_chunk" =

@@ -156,17 +156,21 @@ def test_load_grammar_decodes_oracle_output(gpu_ctx):
 
 def test_count_kernels_give_same_result(gpu_ctx):
     """Every pair-count kernel (the tuner's pick, tiled, tiled with warp
-    folding, flat), both classification kernels, the warp folding switch
-    and the table size (load-factor tuner on and off, a forced first-round
-    size too small for the pairs) give the same grammar."""
+    folding, flat, flat with four pairs), classification and emit from the
+    count's slot references or by table probes (persistent and flat), the
+    warp folding switch and the table size (load-factor tuner on and off, a
+    forced first-round size too small for the pairs, so that the count
+    refills and rewrites its slot references) give the same grammar."""
     steps, off, _ = synthetic.cfg2_stream(seed=4, n_segments=80_000, n_paths=6)
     a = gz.encode(steps, off, ctx=gpu_ctx).arrays()
-    for opt, val in [("count_kernel", 0), ("count_kernel", 1), ("count_kernel", 2), ("count_kernel", 3),
-                     ("warp_dedup", 1),
-                     ("classify_kernel", 0), ("classify_kernel", 1),
-                     ("table_tuner", 0), ("first_table_cap", 1 << 16)]:
+    probe = ("slot_refs", 0)
+    for opts in [[("count_kernel", 0)], [("count_kernel", 1)], [("count_kernel", 2)], [("count_kernel", 3)],
+                 [("warp_dedup", 1)], [probe], [probe, ("classify_kernel", 0)], [probe, ("classify_kernel", 1)],
+                 [probe, ("count_kernel", 3)], [("table_tuner", 0)], [("first_table_cap", 1 << 16)],
+                 [probe, ("first_table_cap", 1 << 16)]]:
         ctx2 = gz.Context(0)
-        ctx2.set_option(opt, val)
+        for opt, val in opts:
+            ctx2.set_option(opt, val)
         b = gz.encode(steps, off, ctx=ctx2).arrays()
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x, y)
