@@ -177,6 +177,38 @@ def run_cpu_port(steps, off, sample_paths, threads, grammar=False):
             r[3] if grammar else None)
 
 
+def _cpu_leg_child(base, sample_paths, threads, q):
+    """Spawned child of run_cpu_port_isolated: the port's timed pass on the
+    steps saved at base, its grammar saved beside them."""
+    steps = np.load(base + ".steps.npy")
+    off = np.load(base + ".off.npy")
+    v, dt, nb, sample, gram = run_cpu_port(steps, off, sample_paths, threads, grammar=True)
+    np.savez(base + ".gram.npz", enc=gram[0], off=gram[1], rules=gram[2])
+    q.put((v, dt, nb, sample, len(os.sched_getaffinity(0))))
+
+
+def run_cpu_port_isolated(steps, off, sample_paths, threads):
+    """run_cpu_port (with the grammar) in a freshly spawned process, so that
+    the port's OpenMP threads start from a clean process: inside the bench
+    process, after the CUDA work, the same pass ran about 5x slower.
+    Returns (GB/s, seconds, text bytes, sample, cpus usable, grammar)."""
+    import multiprocessing as mp
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        base = os.path.join(td, "cpu_leg")
+        np.save(base + ".steps.npy", steps)
+        np.save(base + ".off.npy", off)
+        mpc = mp.get_context("spawn")
+        q = mpc.Queue()
+        p = mpc.Process(target=_cpu_leg_child, args=(base, sample_paths, threads, q))
+        p.start()
+        res = q.get()
+        p.join()
+        z = np.load(base + ".gram.npz")
+        gram = (z["enc"], z["off"], z["rules"])
+    return res + (gram,)
+
+
 def calibration():
     """The port's time relative to the reference CLI's on the same input
     (oracle/calibration.json), or None."""
@@ -560,11 +592,11 @@ def main():
     grammar_parity = "not compared"
     grammar_ok = True
     if not args.no_cpu_baseline and rank == 0:
-        v, dt, nb, sample, cpu_grammar = run_cpu_port(steps, off, args.cpu_sample_paths, os.cpu_count() or 1,
-                                                      grammar=True)
-        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s "
-                         "(oracle/gfaz_oracle.c, OpenMP)", "calibration": calibration()}
+        threads = os.cpu_count() or 1
+        v, dt, nb, sample, usable, cpu_grammar = run_cpu_port_isolated(steps, off, args.cpu_sample_paths, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s in a spawned process "
+                         f"({usable} CPUs usable; oracle/gfaz_oracle.c, OpenMP)", "calibration": calibration()}
         if args.cpu_sample_paths >= ntrav:
             # the GPU grammar of the parity step against the port's, element by element
             grammar_ok = all(np.array_equal(a, b) for a, b in zip(gpu_grammar, cpu_grammar))
