@@ -242,3 +242,25 @@ def test_tuners_on_a_prefix(monkeypatch):
         got = gz.encode(steps, off, ctx=ctx).arrays()
         for x, y in zip(got, want):
             np.testing.assert_array_equal(x, y)
+
+
+
+def test_text_into_page_locked_memory():
+    """P text decoded straight into page-locked host memory (the text kernel
+    writes it there, on the context's low-priority stream) equals the
+    oracle's text; the steps decode back exactly."""
+    torch = pytest.importorskip("torch")
+    steps, off, _ = synthetic.cfg2_stream(seed=8, n_segments=60_000, n_paths=7)
+    ctx = gz.Context(0)
+    g = gz.encode(steps, off, ctx=ctx)
+    n = len(off) - 1
+    names = [f"hap{i}" for i in range(n)]
+    ovs = ["*"] * n
+    want = oracle.format_p(steps, off, names, ovs)
+    buf = torch.zeros(len(want) + 64, dtype=torch.uint8).pin_memory()
+    size = g.decode_text(0, n, names=names, overlaps=ovs, out_ptr=buf.data_ptr(), cap=buf.numel(),
+                         where=gz.WHERE_HOST)
+    assert size == len(want)
+    assert bytes(buf[:size].numpy().tobytes()) == want
+    x, xoff = g.decode()
+    np.testing.assert_array_equal(x, steps)
