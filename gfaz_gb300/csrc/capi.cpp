@@ -241,6 +241,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "table_tuner") {
       require(value == 0 || value == 1, "table_tuner must be 0 or 1");
       c.table_tuner = value != 0;
+    } else if (std::string(name) == "rule_layout") {
+      require(value == 0 || value == 1, "rule_layout must be 0 (rule ids) or 1 (first use)");
+      c.rule_layout = (int)value;
     } else if (std::string(name) == "static_text") {
       require(value == 0 || value == 1, "static_text must be 0 (host) or 1 (device)");
       c.static_text = (int)value;

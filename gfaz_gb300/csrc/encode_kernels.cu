@@ -103,6 +103,29 @@ __device__ __forceinline__ void load_slot(const PairSlot *p, unsigned long long 
   flags = (uint32_t)w.y;
 }
 
+__global__ void k_copy_bytes(const char *__restrict__ src, char *__restrict__ dst, uint64_t n) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t done = 0;
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15u) == 0) {
+    const uint64_t words = n / 16;
+    for (uint64_t i = tid; i < words; i += stride)
+      reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+    done = words * 16;
+  }
+  for (uint64_t i = done + tid; i < n; i += stride) dst[i] = src[i];
+}
+
+__global__ void k_zero_bytes(char *dst, uint64_t n) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t gap = (16u - ((uintptr_t)dst & 15u)) & 15u;
+  const uint64_t lead = gap < n ? gap : n;
+  for (uint64_t i = tid; i < lead; i += stride) dst[i] = 0;
+  const uint64_t words = (n - lead) / 16;
+  uint4 *w = reinterpret_cast<uint4 *>(dst + lead);
+  for (uint64_t i = tid; i < words; i += stride) w[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (uint64_t i = lead + words * 16 + tid; i < n; i += stride) dst[i] = 0;
+}
+
 __global__ void k_table_clear(PairTable tab, uint32_t val_init) {
   const uint4 empty = make_uint4((uint32_t)kEmptyKey, (uint32_t)(kEmptyKey >> 32), 0u, val_init);
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tab.cap; i += (uint64_t)gridDim.x * blockDim.x)
@@ -376,7 +399,10 @@ __global__ void __launch_bounds__(kBlock) k_count_flat(const int32_t *__restrict
 // Four consecutive pairs per thread, read straight from global memory;
 // a run of equal keys inside the thread is inserted once (flagged repeated
 // when longer than one), as in the tiled kernel, but with no barrier.
-__global__ void __launch_bounds__(kBlock) k_count_flat4(const int32_t *__restrict__ s, uint64_t n,
+// Six resident blocks per SM (at most 40 registers, a few bytes spilled):
+// more warps to cover the slot loads' latency than the 52 registers it
+// takes unbounded allow (round 1 1.78 against 1.86 ms).
+__global__ void __launch_bounds__(kBlock, 6) k_count_flat4(const int32_t *__restrict__ s, uint64_t n,
                                                         const uint32_t *__restrict__ heads, PairTable tab,
                                                         DevStatus *status, uint32_t *sref, uint32_t *rep_bits) {
   constexpr int K = 4;
@@ -1045,8 +1071,10 @@ __global__ void __launch_bounds__(BLOCK) k_apply_emit_flat(const int32_t *__rest
 
 // Emit from slot references: one tile per block (as k_apply_emit_flat on a
 // whole resident stream), the replaced positions' rules read from sref.
+// Six resident blocks per SM (at most 40 registers): 2.50 against 2.85 ms
+// per step at the four blocks its 63 registers would allow.
 template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_apply_emit_sref(const int32_t *__restrict__ s,
+__global__ void __launch_bounds__(BLOCK, 6) k_apply_emit_sref(const int32_t *__restrict__ s,
                                                            const uint32_t *__restrict__ sref, uint64_t n,
                                                            const uint32_t *__restrict__ tword,
                                                            const unsigned long long *__restrict__ tile_agg,
@@ -1686,6 +1714,17 @@ void launch_remap(int32_t *s, uint64_t n, int32_t temp_base, const PairSlot *slo
     k_remap<true><<<grid_for((n + 3) / 4, kBlock), kBlock, 0, st>>>(s, n, temp_base, slots);
   else
     k_remap<false><<<grid_for(n, kBlock), kBlock, 0, st>>>(s, n, temp_base, slots);
+}
+
+void launch_copy_bytes(const void *src, void *dst, uint64_t n, cudaStream_t st) {
+  if (!n) return;
+  k_copy_bytes<<<grid_for((n + 15) / 16, kBlock, 152u * 4u), kBlock, 0, st>>>(static_cast<const char *>(src),
+                                                                              static_cast<char *>(dst), n);
+}
+
+void launch_zero_bytes(void *dst, uint64_t n, cudaStream_t st) {
+  if (!n) return;
+  k_zero_bytes<<<grid_for((n + 15) / 16, kBlock, 152u * 8u), kBlock, 0, st>>>(static_cast<char *>(dst), n);
 }
 
 void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st) {

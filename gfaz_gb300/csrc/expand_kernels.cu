@@ -73,6 +73,37 @@ struct RangeAcc {
   }
 };
 
+// First use of every rule in the encoded stream (see launch_first_use).
+__global__ void k_first_use_init(uint64_t nrules, unsigned long long *key, uint32_t *idx) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nrules; r += (uint64_t)gridDim.x * blockDim.x) {
+    key[r] = 0xFFFFFFFFull;
+    idx[r] = (uint32_t)r;
+  }
+}
+
+__global__ void k_first_use(const int32_t *__restrict__ enc, uint64_t m, uint32_t min_id, uint64_t nrules,
+                            unsigned long long *key) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = abs32(enc[i]);
+    if (!is_rule(a, min_id, nrules)) continue;
+    unsigned long long *k = key + (a - min_id);
+    if (*k > i) atomicMin(k, (unsigned long long)i);  // a plain read skips most atomics of later uses
+  }
+}
+
+__global__ void k_lens_in_order(const uint32_t *__restrict__ idx, const uint32_t *__restrict__ rlen, uint64_t nrules,
+                                uint32_t *lens) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nrules; j += (uint64_t)gridDim.x * blockDim.x)
+    lens[j] = rlen[idx[j]];
+}
+
+__global__ void k_offsets_from_order(const uint32_t *__restrict__ idx, const uint64_t *__restrict__ at,
+                                     uint64_t nrules, uint64_t *roff) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= nrules;
+       j += (uint64_t)gridDim.x * blockDim.x)
+    roff[j < nrules ? idx[j] : nrules] = at[j];
+}
+
 constexpr uint32_t kWarpRule = 16;  // rules longer than this are written by a whole warp
 
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
@@ -247,8 +278,11 @@ __global__ void k_tile_symbols(const uint64_t *__restrict__ pos, uint64_t m, uin
 // ---------------------------------------------------------------------------
 // Symbols of one output tile staged in shared memory: pos[0 .. cnt] and the
 // records of symbols lo .. lo + cnt - 1.  Tiles spanning more than kStageSyms
-// symbols (little compression) read both from global memory instead.
-constexpr uint32_t kStageSyms = 512;
+// symbols (little compression) read both from global memory instead.  256
+// symbols (an output tile of 2048 steps holds about 50 on the
+// chromosome-scale workload) keep the text kernel's shared memory at 31 KB,
+// for seven resident blocks per SM.
+constexpr uint32_t kStageSyms = 256;
 struct SymStage {
   uint64_t pos[kStageSyms + 1];
   int4 rec[kStageSyms];
@@ -485,8 +519,11 @@ __global__ void k_tile_text_off(ExpandSource E, TextSource T, const uint64_t *__
 // out with 16-byte stores.  toff[tile] (k_tile_text_off) places the tile;
 // its end must meet the next tile's start (or the body end), else the
 // per-symbol lengths and the text disagree and kErrLength is raised.
+// Seven resident blocks per SM (32 registers, 31 KB of shared memory): the
+// kernel is bound by issue and gather latency, and more warps cover both
+// (4.49 against 5.22 ms per step at five blocks).
 template <int BLOCK, int ITEMS, int DELTA>
-__global__ void __launch_bounds__(BLOCK) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ toff,
+__global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ toff,
                                                       char *__restrict__ text) {
   static_assert(ITEMS <= 8, "digit counts are packed 4 bits per step");
   constexpr uint32_t TILE = BLOCK * ITEMS;
@@ -662,6 +699,24 @@ uint64_t expand_num_tiles(uint64_t total) { return (total + kExpandTile - 1) / k
 uint64_t excl_scan_tiles(uint64_t n) {
   constexpr uint64_t TILE = kBlock * kScanItemsU;
   return (n + TILE - 1) / TILE;
+}
+
+void launch_first_use(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules, unsigned long long *key,
+                      uint32_t *idx, cudaStream_t st) {
+  if (!nrules) return;
+  k_first_use_init<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(nrules, key, idx);
+  if (m) k_first_use<<<grid_for(m, kBlock), kBlock, 0, st>>>(enc, m, min_id, nrules, key);
+}
+
+void launch_lens_in_order(const uint32_t *idx, const uint32_t *rlen, uint64_t nrules, uint32_t *lens,
+                          cudaStream_t st) {
+  if (!nrules) return;
+  k_lens_in_order<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(idx, rlen, nrules, lens);
+}
+
+void launch_offsets_from_order(const uint32_t *idx, const uint64_t *at, uint64_t nrules, uint64_t *roff,
+                               cudaStream_t st) {
+  k_offsets_from_order<<<grid_for(nrules + 1, kBlock), kBlock, 0, st>>>(idx, at, nrules, roff);
 }
 
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,

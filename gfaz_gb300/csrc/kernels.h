@@ -36,6 +36,11 @@ struct PairTable {
   PairSlot *slots;  // cap slots
   uint64_t cap;     // power of two, at most 2^31
 };
+// dst[0, n) = src[0, n) by a kernel (either side may be page-locked host
+// memory); 16-byte words where both ends are 16-byte aligned.
+void launch_copy_bytes(const void *src, void *dst, uint64_t n, cudaStream_t st);
+// dst[0, n) = 0 by a kernel.
+void launch_zero_bytes(void *dst, uint64_t n, cudaStream_t st);
 // Sets every slot to {kEmptyKey, 0, val_init}.
 void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st);
 
@@ -258,6 +263,19 @@ struct TextSource {
   uint64_t cap;   // bytes of the text buffer
   uint32_t *err;  // kErrLength when the text would not fit where its lengths say
 };
+// Rule order of the prefix buffer by first use: key[r] = the first position
+// of the encoded stream enc[0, m) (m < 2^32) that holds rule r (either
+// orientation), 2^32 - 1 for rules never used there; idx[r] = r.  Sorted
+// by key, idx lists the rules in the order their buffers are laid out.
+void launch_first_use(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules, unsigned long long *key,
+                      uint32_t *idx, cudaStream_t st);
+// lens[j] = rlen[idx[j]] for j < nrules.
+void launch_lens_in_order(const uint32_t *idx, const uint32_t *rlen, uint64_t nrules, uint32_t *lens,
+                          cudaStream_t st);
+// roff[idx[j]] = at[j] for j < nrules and roff[nrules] = at[nrules]: the
+// buffer offsets of rules laid out in the order idx.
+void launch_offsets_from_order(const uint32_t *idx, const uint64_t *at, uint64_t nrules, uint64_t *roff,
+                               cudaStream_t st);
 // One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
 // waiting, zero before pass 1).  status->pass_open[slot] += rules still
 // waiting.

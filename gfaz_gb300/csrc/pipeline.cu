@@ -6,9 +6,8 @@
 //   signed packed key -> final ids next_id + rank -> remap temporaries.
 #include "pipeline.h"
 
-#include <chrono>
-
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -127,6 +126,8 @@ bool debug_enabled() {
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
+constexpr unsigned long long kAllOnes = ~0ull;
+
 Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullptr), counter_(nullptr) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
   cudaDeviceProp prop;
@@ -198,6 +199,7 @@ Context::~Context() {
   cudaStreamSynchronize(stream_);
   cudaFree(d_status_);
   cudaFreeHost(h_status_);
+  if (stage_) cudaFreeHost(stage_);
   for (auto &h : host_) {
     if (h.pinned) cudaFreeHost(h.p);
     else std::free(h.p);
@@ -245,14 +247,71 @@ int32_t *Context::host_buffer(int i, uint64_t n) {
 }
 
 void Context::reset_status() {
-  cuda_check(cudaMemsetAsync(d_status_, 0, offsetof(DevStatus, sticky_err), stream_), "status clear");
+  launch_zero_bytes(d_status_, offsetof(DevStatus, sticky_err), stream_);
+  count_launch();
 }
 
 const DevStatus &Context::read_status() {
-  cuda_check(cudaMemcpyAsync(h_status_, d_status_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_),
-             "status read");
-  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  // h_status_ is page-locked: the kernel writes it straight into host memory
+  launch_copy_bytes(d_status_, h_status_, sizeof(DevStatus), stream_);
+  count_launch();
+  sync();
   return *h_status_;
+}
+
+char *Context::stage(size_t bytes) {
+  const size_t need = (bytes + 15) & ~size_t(15);
+  if (stage_used_ + need > stage_cap_) {
+    sync();  // every queued transfer through the staging is done
+    if (need > stage_cap_) {
+      if (stage_) cudaFreeHost(stage_);
+      stage_ = nullptr;
+      stage_cap_ = 0;
+      const size_t cap = std::max<size_t>(need, 4u << 20);
+      cuda_check(cudaMallocHost(reinterpret_cast<void **>(&stage_), cap), "staging alloc");
+      stage_cap_ = cap;
+    }
+  }
+  char *p = stage_ + stage_used_;
+  stage_used_ += need;
+  return p;
+}
+
+void Context::upload(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  if (bytes > kSmallCopy) {
+    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "upload");
+    return;
+  }
+  char *p = stage(bytes);
+  std::memcpy(p, src, bytes);
+  launch_copy_bytes(p, dst, bytes, stream_);
+  count_launch();
+}
+
+void Context::download(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  if (bytes > kSmallCopy) {
+    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "download");
+    return;
+  }
+  char *p = stage(bytes);
+  launch_copy_bytes(src, p, bytes, stream_);
+  count_launch();
+  downloads_.push_back(PendingDownload{dst, p, bytes});
+}
+
+void Context::zero(void *dst, size_t bytes) {
+  if (!bytes) return;
+  launch_zero_bytes(dst, bytes, stream_);
+  count_launch();
+}
+
+void Context::sync() {
+  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  for (const PendingDownload &d : downloads_) std::memcpy(d.dst, d.from, d.bytes);
+  downloads_.clear();
+  stage_used_ = 0;
 }
 
 void Context::check_status(const char *stage) {
@@ -260,18 +319,16 @@ void Context::check_status(const char *stage) {
   if (!e) return;
   if (h_status_->sticky_err) {
     h_status_->sticky_err = 0;
-    cudaMemsetAsync(&d_status_->sticky_err, 0, sizeof(uint32_t), stream_);
+    zero(&d_status_->sticky_err, sizeof(uint32_t));
   }
   throw std::runtime_error(describe_device_error(stage, e));
 }
 
 unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) {
   desc_.resize(std::max<uint64_t>(tiles, 1));
-  cuda_check(cudaMemsetAsync(desc_.ptr, 0, std::max<uint64_t>(tiles, 1) * sizeof(unsigned long long), stream_),
-             "descriptor clear");
-  cuda_check(cudaMemsetAsync(counter_.ptr, 0, sizeof(uint32_t), stream_), "counter clear");
+  zero(desc_.ptr, std::max<uint64_t>(tiles, 1) * sizeof(unsigned long long));
+  zero(counter_.ptr, sizeof(uint32_t));
   *counter = counter_.ptr;
-  count_launch(0);
   return desc_.ptr;
 }
 
@@ -372,7 +429,7 @@ static void sort_used_rules(Context &ctx, PairTable tab, uint64_t U, uint32_t by
   su.keys_tmp.resize(U);
   su.slots_tmp.resize(U);
   su.hist.resize(8 * 256);
-  cuda_check(cudaMemsetAsync(su.hist.ptr, 0, 8 * 256 * sizeof(uint32_t), st), "histogram clear");
+  ctx.zero(su.hist.ptr, 8 * 256 * sizeof(uint32_t));
   ctx.reset_status();
   bool in_tmp = false;
   GFZ_TIMED(ctx, "radix_sort", launch_sort_hist(su.keys.ptr, U, byte_mask, su.hist.ptr, st));
@@ -473,6 +530,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
 
   for (int round = round0; round < rounds; ++round) {
     if (n < 2) break;
+    const auto round_t0 = std::chrono::steady_clock::now();
     // first round: at most 4M distinct pairs expected (delta-coded
     // traversals repeat few pairs); the table grows when it runs fuller
     // later rounds: distinct pairs grow by up to ~3x per round as rules
@@ -484,7 +542,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     if (forced_cap) cap = ctx.first_table_cap;
     uint64_t distinct = 0, repeated = 0;
     heads.resize(head_words(n));
-    cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(n) * sizeof(uint32_t), st), "head bitmap clear");
+    ctx.zero(heads.ptr, head_words(n) * sizeof(uint32_t));
     GFZ_TIMED(ctx, "head_bits", launch_head_bits(offA.ptr, ntrav, heads.ptr, st));
     // Count kernel: forced by option, else the faster of the tiled and the
     // flat kernel for this stream class (first round or not, length, and the
@@ -525,7 +583,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       tab.prepare(c, st);
       if (use_sref) {
         rep_bits.resize((c + 31) / 32);
-        cuda_check(cudaMemsetAsync(rep_bits.ptr, 0, (c + 31) / 32 * sizeof(uint32_t), st), "repeated bitmap clear");
+        ctx.zero(rep_bits.ptr, (c + 31) / 32 * sizeof(uint32_t));
         d_rep = rep_bits.ptr;
       }
     };
@@ -535,10 +593,11 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
         // every candidate kernel counts the stream's first tune_len steps
         // into a cleared table; the full count with the fastest follows
         const CountKernel cand[] = {CountKernel::kTiled, CountKernel::kFlat, CountKernel::kFlat4};
-        float best = 0, t[3] = {0, 0, 0};
+        constexpr int kCand = sizeof(cand) / sizeof(cand[0]);
+        float best = 0, t[kCand] = {};
         bool refill = false;
         const uint64_t ns = tune_len(ctx, n);
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < kCand; ++i) {
           prepare(cap);
           ctx.reset_status();
           t[i] = ctx.time_launches(
@@ -625,9 +684,9 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       throw std::overflow_error("Compression workflow error: rule id space exhausted");
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
-    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
+    ctx.upload(&ds->u64[5], &kAllOnes, sizeof(kAllOnes));
     used_bits.resize((cap + 31) / 32);
-    cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
+    ctx.zero(used_bits.ptr, (cap + 31) / 32 * sizeof(uint32_t));
     // slot references hold slots below 2^30 (bit 31 and one value are
     // taken); a larger table is classified and emitted by probing
     const bool by_sref = use_sref && cap <= kSrefMaxCap;
@@ -654,12 +713,15 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     GFZ_TIMED_B(ctx, "remap", 8.0 * n_out, launch_remap(B.ptr, n_out, temp_base, tab.slots.ptr, st));
     // the sort's error bits reach the host with the next round's count (or
     // the read after the last round): no wait here
-    cuda_check(cudaMemcpyAsync(&ds->sticky_err, &ds->err, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
-               "status carry");
+    launch_copy_bytes(&ds->err, &ds->sticky_err, sizeof(uint32_t), st);
+    ctx.count_launch();
     if (debug_enabled())
-      fprintf(stderr, "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu\n",
+      fprintf(stderr,
+              "[gfaz gb300] round %d: n=%llu cap=%llu distinct=%llu candidates=%llu used=%llu n_out=%llu "
+              "(host %.2f ms)\n",
               round + 1, (unsigned long long)n, (unsigned long long)cap, (unsigned long long)distinct,
-              (unsigned long long)repeated, (unsigned long long)U, (unsigned long long)n_out);
+              (unsigned long long)repeated, (unsigned long long)U, (unsigned long long)n_out,
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - round_t0).count());
     g.nrules += U;
     next_id += (uint32_t)U;
     n = n_out;
@@ -679,6 +741,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
 void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<uint64_t> &h_off,
                        const EncodeParams &p, Grammar &g) {
   cudaStream_t st = ctx.stream();
+  const auto t_start = std::chrono::steady_clock::now();
   if (h_off.empty()) throw std::invalid_argument("offsets must hold ntrav + 1 entries");
   const uint64_t ntrav = h_off.size() - 1;
   const uint64_t N = h_off.back();
@@ -694,8 +757,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   DevVec<uint64_t> offA(st), offB(st);
   offA.resize(ntrav + 1);
   offB.resize(ntrav + 1);
-  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
-             "offsets upload");
+  ctx.upload(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t));
   DevVec<int32_t> A(st), B(st);
   A.resize(std::max<uint64_t>(N, 1));
   B.resize(std::max<uint64_t>(N, 1));
@@ -713,6 +775,9 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
     }
   }
   const DevStatus &s0 = ctx.read_status();
+  if (debug_enabled())
+    fprintf(stderr, "[gfaz gb300] delta transform of %llu steps done (host %.2f ms)\n", (unsigned long long)N,
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
   const uint32_t max_abs = s0.aux;
   if (max_abs == UINT32_MAX)
     throw std::overflow_error("Compression workflow error: delta values too large for rule ID assignment");
@@ -728,11 +793,10 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   g.enc = std::move(A);
   g.off = std::move(offA);
   g.h_off.resize(ntrav + 1);
-  cuda_check(cudaMemcpyAsync(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
-             "offsets download");
+  ctx.download(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t));
   rules.size = g.nrules;
   g.rules = std::move(rules);
-  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  ctx.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -788,8 +852,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   DevVec<uint64_t> offA(st), offB(st);
   offA.resize(ntrav + 1);
   offB.resize(ntrav + 1);
-  cuda_check(cudaMemcpyAsync(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
-             "offsets upload");
+  ctx.upload(offA.ptr, h_off.data(), (ntrav + 1) * sizeof(uint64_t));
   // chunk buffers: steps in (one before / one after the chunk), steps out,
   // chunk-relative head bitmap
   DevVec<int32_t> cin(st), cout(st);
@@ -798,7 +861,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   DevVec<uint32_t> hloc(st);
   hloc.resize(head_words(C + 1));
   auto local_heads = [&](const uint64_t *off, uint64_t lo, uint64_t span) {
-    cuda_check(cudaMemsetAsync(hloc.ptr, 0, head_words(C + 1) * sizeof(uint32_t), st), "head bitmap clear");
+    ctx.zero(hloc.ptr, head_words(C + 1) * sizeof(uint32_t));
     launch_head_bits_range(off, ntrav, lo, span, hloc.ptr, st);
   };
   // host stream buffers (the context keeps them for later calls)
@@ -852,14 +915,14 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
         if (c0) {
           upload_range(cur, c0 - 1, c1, cin.ptr, st);
         } else {
-          cuda_check(cudaMemsetAsync(cin.ptr, 0, sizeof(int32_t), st), "chunk clear");
+          ctx.zero(cin.ptr, sizeof(int32_t));
           upload_range(cur, 0, c1, cin.ptr + 1, st);
         }
         local_heads(offA.ptr, c0, c1 - c0);
         GFZ_TIMED_B(ctx, "delta_encode", 8.0 * (c1 - c0),
                     launch_delta_chunk(cin.ptr, A.ptr + c0, c1 - c0, hloc.ptr, &ds->aux, st));
       }
-      cuda_check(cudaStreamSynchronize(st), "stream sync");
+      ctx.sync();
       cur.clear();  // the stream is in A only
       continue;
     }
@@ -868,7 +931,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       if (c0) {
         upload_range(cur, c0 - 1, c1, cin.ptr, st);
       } else {
-        cuda_check(cudaMemsetAsync(cin.ptr, 0, sizeof(int32_t), st), "chunk clear");
+        ctx.zero(cin.ptr, sizeof(int32_t));
         upload_range(cur, 0, c1, cin.ptr + 1, st);
       }
       local_heads(offA.ptr, c0, c1 - c0);
@@ -877,7 +940,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       cuda_check(cudaMemcpyAsync(nxt + c0, cout.ptr, (c1 - c0) * sizeof(int32_t), cudaMemcpyDefault, st),
                  "chunk download");
     }
-    cuda_check(cudaStreamSynchronize(st), "stream sync");
+    ctx.sync();
     cur = {HostSeg{nxt, N}};
     nxt = nxt == X ? Y : X;
   }
@@ -931,7 +994,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
       dev_next = false;
       phase("upload for the resident rounds");
       run_rounds(ctx, A, B, offA, offB, ntrav, n, next_id, prev_distinct, round, p.rounds, rules, g);
-      cuda_check(cudaStreamSynchronize(st), "stream sync");
+      ctx.sync();
       phase("resident rounds");
       resident = true;
       break;
@@ -1024,9 +1087,9 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     rw.tile_agg.resize(tiles);
     rw.tile_state.resize(tiles);
     ctx.reset_status();
-    cuda_check(cudaMemsetAsync(&ds->u64[5], 0xFF, sizeof(unsigned long long), st), "status init");
+    ctx.upload(&ds->u64[5], &kAllOnes, sizeof(kAllOnes));
     used_bits.resize((cap + 31) / 32);
-    cuda_check(cudaMemsetAsync(used_bits.ptr, 0, (cap + 31) / 32 * sizeof(uint32_t), st), "used bitmap clear");
+    ctx.zero(used_bits.ptr, (cap + 31) / 32 * sizeof(uint32_t));
     uint32_t *counter;
     unsigned long long *desc = ctx.lookback(apply_state_blocks(n), &counter);
     const ApplyScratch sc{rw.tword.ptr, rw.tile_agg.ptr, rw.tile_state.ptr, desc, counter};
@@ -1039,9 +1102,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
     GFZ_TIMED(ctx, "apply_states", launch_apply_states(n, sc, ds, st));
     GFZ_TIMED(ctx, "tile_trav", launch_tile_trav(offA.ptr, ntrav, n, rw.tile_trav.ptr, st));
     h_state.resize(tiles);
-    cuda_check(cudaMemcpyAsync(h_state.data(), rw.tile_state.ptr, tiles * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, st),
-               "tile states");
+    ctx.download(h_state.data(), rw.tile_state.ptr, tiles * sizeof(unsigned long long));
     ctx.read_status();
     ctx.check_status("apply");
     // output position of a chunk's first kept step: tile start minus the
@@ -1144,11 +1205,10 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   }
   g.off = std::move(offA);
   g.h_off.resize(ntrav + 1);
-  cuda_check(cudaMemcpyAsync(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
-             "offsets download");
+  ctx.download(g.h_off.data(), g.off.ptr, (ntrav + 1) * sizeof(uint64_t));
   rules.size = g.nrules;
   g.rules = std::move(rules);
-  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  ctx.sync();
 }
 
 void exclusive_scan(Context &ctx, const uint32_t *in, uint64_t n, uint64_t *out, const char *timer) {
@@ -1197,7 +1257,7 @@ void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vec
   d.resize(std::max<uint64_t>(N, 1));
   uint64_t at = 0;
   for (const HostSeg &sg : input) {
-    if (sg.n) cuda_check(cudaMemcpyAsync(d.ptr + at, sg.p, sg.n * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload");
+    if (sg.n) ctx.upload(d.ptr + at, sg.p, sg.n * sizeof(int32_t));
     at += sg.n;
   }
   if (at != N) throw std::invalid_argument("input segments do not hold the offsets' steps");
@@ -1217,12 +1277,12 @@ void rule_columns_delta(Context &ctx, const Grammar &g, DevVec<int32_t> &first, 
   DevVec<uint64_t> off(st);
   off.resize(2);
   const uint64_t h[2] = {0, R};
-  cuda_check(cudaMemcpyAsync(off.ptr, h, sizeof(h), cudaMemcpyHostToDevice, st), "upload");
+  ctx.upload(off.ptr, h, sizeof(h));
   GFZ_TIMED(ctx, "split_rules", (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, tf.ptr, ts.ptr)));
   ctx.reset_status();
   GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(tf.ptr, first.ptr, R, off.ptr, 1, &ctx.dstatus()->aux, st));
   GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(ts.ptr, second.ptr, R, off.ptr, 1, &ctx.dstatus()->aux, st));
-  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  ctx.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -1240,13 +1300,13 @@ void load_rules(Context &ctx, Grammar &g, const int32_t *first, const int32_t *s
   g.rlen_ready = false;
   g.rpre_state = 0;
   if (!nrules) return;
-  cuda_check(cudaMemcpyAsync(g.first.ptr, first, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
-  cuda_check(cudaMemcpyAsync(g.second.ptr, second, nrules * 4, cudaMemcpyHostToDevice, st), "rules upload");
+  ctx.upload(g.first.ptr, first, nrules * 4);
+  ctx.upload(g.second.ptr, second, nrules * 4);
   // stored columns are delta coded (codec.cpp:88-95): prefix sums on device
   DevVec<uint64_t> off(st);
   off.resize(2);
   const uint64_t h[2] = {0, nrules};
-  cuda_check(cudaMemcpyAsync(off.ptr, h, sizeof(h), cudaMemcpyHostToDevice, st), "upload");
+  ctx.upload(off.ptr, h, sizeof(h));
   ctx.reset_status();
   uint32_t *counter;
   unsigned long long *desc = ctx.lookback(inverse_delta_num_tiles(nrules), &counter);
@@ -1266,10 +1326,10 @@ void load_encoded(Context &ctx, Grammar &g, const int32_t *enc, const std::vecto
   g.ntrav = nt;
   g.h_off = off;
   g.off.resize(nt + 1);
-  cuda_check(cudaMemcpyAsync(g.off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "offsets upload");
+  ctx.upload(g.off.ptr, off.data(), (nt + 1) * 8);
   g.enc.resize(std::max<uint64_t>(m, 1));
   g.enc.size = m;
-  if (m) cuda_check(cudaMemcpyAsync(g.enc.ptr, enc, m * 4, cudaMemcpyHostToDevice, st), "stream upload");
+  if (m) ctx.upload(g.enc.ptr, enc, m * 4);
 }
 
 static void ensure_rule_lengths(Context &ctx, Grammar &g) {
@@ -1287,7 +1347,7 @@ static void ensure_rule_lengths(Context &ctx, Grammar &g) {
       GFZ_TIMED(ctx, "split_rules",
                 (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, g.first.ptr, g.second.ptr)));
     }
-    cuda_check(cudaMemsetAsync(g.rlen.ptr, 0, R * sizeof(uint32_t), st), "rlen clear");
+    ctx.zero(g.rlen.ptr, R * sizeof(uint32_t));
     // level passes in batches, one status read per batch (extra passes
     // after the last level find nothing to do)
     uint64_t prev_open = UINT64_MAX;
@@ -1321,11 +1381,44 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
   const uint64_t R = g.nrules;
   g.roff.resize(R + 1);
   ctx.reset_status();
-  uint32_t *counter;
-  unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
-  GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(g.rlen.ptr, R, g.roff.ptr, desc, counter, ctx.dstatus(), st));
+  const uint64_t m = g.h_off.empty() ? 0 : g.h_off.back();
+  if (ctx.rule_layout == 1 && R > 1 && m < 0xFFFFFFFFull) {
+    // buffers in first-use order: sort the rules by the first position of
+    // the encoded stream that holds them (4 bytes of key), then lay their
+    // lengths out in that order
+    DevVec<unsigned long long> key(st), key2(st);
+    DevVec<uint32_t> idx(st), idx2(st), hist(st), lens(st);
+    DevVec<uint64_t> at(st);
+    key.resize(R);
+    key2.resize(R);
+    idx.resize(R);
+    idx2.resize(R);
+    hist.resize(8 * 256);
+    lens.resize(R);
+    at.resize(R + 1);
+    GFZ_TIMED(ctx, "rule_prefix", launch_first_use(g.enc.ptr, m, g.layer_start, R, key.ptr, idx.ptr, st));
+    ctx.zero(hist.ptr, 8 * 256 * sizeof(uint32_t));
+    GFZ_TIMED(ctx, "rule_prefix", launch_sort_hist(key.ptr, R, 0x0Fu, hist.ptr, st));
+    for (int b = 0; b < 4; ++b) {
+      uint32_t *counter;
+      unsigned long long *desc = ctx.lookback(sort_tiles(R) * 256, &counter);
+      const bool odd = b & 1;
+      GFZ_TIMED(ctx, "rule_prefix",
+                launch_sort_pass(odd ? key2.ptr : key.ptr, odd ? idx2.ptr : idx.ptr, odd ? key.ptr : key2.ptr,
+                                 odd ? idx.ptr : idx2.ptr, R, b, hist.ptr, desc, counter, &ctx.dstatus()->err, st));
+    }
+    GFZ_TIMED(ctx, "rule_prefix", launch_lens_in_order(idx.ptr, g.rlen.ptr, R, lens.ptr, st));
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
+    GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(lens.ptr, R, at.ptr, desc, counter, ctx.dstatus(), st));
+    GFZ_TIMED(ctx, "rule_prefix", launch_offsets_from_order(idx.ptr, at.ptr, R, g.roff.ptr, st));
+  } else {
+    uint32_t *counter;
+    unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
+    GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(g.rlen.ptr, R, g.roff.ptr, desc, counter, ctx.dstatus(), st));
+  }
   uint64_t steps = 0;
-  cuda_check(cudaMemcpyAsync(&steps, g.roff.ptr + R, sizeof(steps), cudaMemcpyDeviceToHost, st), "prefix size");
+  ctx.download(&steps, g.roff.ptr + R, sizeof(steps));
   ctx.read_status();
   ctx.check_status("rule prefix offsets");
   if (steps > kMaxPrefixSteps) {
@@ -1337,7 +1430,7 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
   if (R) {
     DevVec<uint32_t> built(st);
     built.resize(R);
-    cuda_check(cudaMemsetAsync(built.ptr, 0, R * sizeof(uint32_t), st), "prefix clear");
+    ctx.zero(built.ptr, R * sizeof(uint32_t));
     const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, R};
     uint64_t prev_open = UINT64_MAX;
     for (uint32_t pass = 1;; pass += kPassBatch) {
@@ -1395,9 +1488,7 @@ static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, E
   GFZ_TIMED(ctx, "gather_pos", (k_gather_pos<<<grid_for(nt + 1, 256), 256, 0, st>>>(
                                    P.pos.ptr, g.off.ptr + t0, nt + 1, e0, P.out_off.ptr)));
   P.h_out_off.resize(nt + 1);
-  cuda_check(cudaMemcpyAsync(P.h_out_off.data(), P.out_off.ptr, (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
-                             st),
-             "offsets download");
+  ctx.download(P.h_out_off.data(), P.out_off.ptr, (nt + 1) * sizeof(uint64_t));
   ctx.read_status();
   ctx.check_status("expansion offsets");
   P.total = P.h_out_off[nt];
@@ -1411,8 +1502,7 @@ static void plan_expansion(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, E
     std::vector<uint64_t> h_loc(nt + 1);
     for (uint64_t t = 0; t <= nt; ++t) h_loc[t] = g.h_off[t0 + t] - e0;
     loc.resize(nt + 1);
-    cuda_check(cudaMemcpyAsync(loc.ptr, h_loc.data(), (nt + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
-               "offsets upload");
+    ctx.upload(loc.ptr, h_loc.data(), (nt + 1) * sizeof(uint64_t));
     GFZ_TIMED_B(ctx, "symbol_sums", 24.0 * m, launch_symbol_records(g.enc.ptr + e0, m, rv, P.rec.ptr, sums.ptr, st));
     desc = ctx.lookback(inverse_delta_num_tiles(m), &counter);
     GFZ_TIMED_B(ctx, "symbol_sums", 8.0 * m,
@@ -1461,13 +1551,12 @@ void decode_traversals(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1, DevVe
     GFZ_TIMED_B(ctx, "symbol_positions", 12.0 * m, launch_symbol_positions(g.enc.ptr + e0, m, g.layer_start, g.nrules,
                                                                g.rlen.ptr, pos.ptr, desc, counter, ctx.dstatus(), st));
   } else {
-    cuda_check(cudaMemsetAsync(pos.ptr, 0, sizeof(uint64_t), st), "pos clear");
+    ctx.zero(pos.ptr, sizeof(uint64_t));
   }
   GFZ_TIMED(ctx, "gather_pos", (k_gather_pos<<<grid_for(nt + 1, 256), 256, 0, st>>>(
                                    pos.ptr, g.off.ptr + t0, nt + 1, e0, d_out_off.ptr)));
   out_off.resize(nt + 1);
-  cuda_check(cudaMemcpyAsync(out_off.data(), d_out_off.ptr, (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
-             "offsets download");
+  ctx.download(out_off.data(), d_out_off.ptr, (nt + 1) * sizeof(uint64_t));
   const DevStatus &s = ctx.read_status();
   ctx.check_status("expansion offsets");
   (void)s;
@@ -1504,8 +1593,8 @@ uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uin
     text.resize(std::max<uint64_t>(all.size(), 1));
     text.size = all.size();
     if (!all.empty())
-      cuda_check(cudaMemcpyAsync(text.ptr, all.data(), all.size(), cudaMemcpyHostToDevice, st), "text upload");
-    cuda_check(cudaStreamSynchronize(st), "stream sync");
+      ctx.upload(text.ptr, all.data(), all.size());
+    ctx.sync();
     return all.size();
   }
   DevVec<uint64_t> d_off(st), d_pre(st), d_suf(st);
@@ -1515,15 +1604,13 @@ uint64_t emit_text(Context &ctx, const DevVec<int32_t> &x, const std::vector<uin
   d_suf.resize(nt + 1);
   d_blob.resize(std::max<size_t>(pieces.blob.size(), 1));
   d_tail.resize(std::max<size_t>(pieces.tail.size(), 1));
-  cuda_check(cudaMemcpyAsync(d_off.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
-  cuda_check(cudaMemcpyAsync(d_pre.ptr, pieces.pre_off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
-  cuda_check(cudaMemcpyAsync(d_suf.ptr, pieces.suf_off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+  ctx.upload(d_off.ptr, off.data(), (nt + 1) * 8);
+  ctx.upload(d_pre.ptr, pieces.pre_off.data(), (nt + 1) * 8);
+  ctx.upload(d_suf.ptr, pieces.suf_off.data(), (nt + 1) * 8);
   if (!pieces.blob.empty())
-    cuda_check(cudaMemcpyAsync(d_blob.ptr, pieces.blob.data(), pieces.blob.size(), cudaMemcpyHostToDevice, st),
-               "upload");
+    ctx.upload(d_blob.ptr, pieces.blob.data(), pieces.blob.size());
   if (!pieces.tail.empty())
-    cuda_check(cudaMemcpyAsync(d_tail.ptr, pieces.tail.data(), pieces.tail.size(), cudaMemcpyHostToDevice, st),
-               "upload");
+    ctx.upload(d_tail.ptr, pieces.tail.data(), pieces.tail.size());
   const uint64_t bound = n * 12 + pieces.blob.size() + pieces.tail.size() + 64;
   text.resize(bound);
   TextMeta meta{d_blob.ptr, d_pre.ptr, d_suf.ptr, d_tail.ptr, (uint64_t)pieces.tail.size(), mode};
@@ -1544,18 +1631,18 @@ struct DevPieces {
   explicit DevPieces(cudaStream_t st) : pre(st), suf(st), blob(st), tail(st) {}
   DevVec<uint64_t> pre, suf;
   DevVec<char> blob, tail;
-  void upload(const TextPieces &p, cudaStream_t st) {
+  void upload(Context &ctx, const TextPieces &p) {
     const uint64_t n1 = p.pre_off.size();
     pre.resize(n1);
     suf.resize(n1);
     blob.resize(std::max<size_t>(p.blob.size(), 1));
     tail.resize(std::max<size_t>(p.tail.size(), 1));
-    cuda_check(cudaMemcpyAsync(pre.ptr, p.pre_off.data(), n1 * 8, cudaMemcpyHostToDevice, st), "upload");
-    cuda_check(cudaMemcpyAsync(suf.ptr, p.suf_off.data(), n1 * 8, cudaMemcpyHostToDevice, st), "upload");
+    ctx.upload(pre.ptr, p.pre_off.data(), n1 * 8);
+    ctx.upload(suf.ptr, p.suf_off.data(), n1 * 8);
     if (!p.blob.empty())
-      cuda_check(cudaMemcpyAsync(blob.ptr, p.blob.data(), p.blob.size(), cudaMemcpyHostToDevice, st), "upload");
+      ctx.upload(blob.ptr, p.blob.data(), p.blob.size());
     if (!p.tail.empty())
-      cuda_check(cudaMemcpyAsync(tail.ptr, p.tail.data(), p.tail.size(), cudaMemcpyHostToDevice, st), "upload");
+      ctx.upload(tail.ptr, p.tail.data(), p.tail.size());
   }
 };
 
@@ -1573,7 +1660,7 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
     if (direct) {
       if (direct_cap < n) throw std::length_error("output buffer too small");
       if (n) cuda_check(cudaMemcpyAsync(direct, text.ptr, n, cudaMemcpyDefault, st), "text copy");
-      cuda_check(cudaStreamSynchronize(st), "stream sync");
+      ctx.sync();
     }
     return n;
   }
@@ -1582,10 +1669,10 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   const uint64_t nt = t1 - t0;
   const TextPieces pieces = make_pieces(P.h_out_off);
   DevPieces dp(st);
-  dp.upload(pieces, st);
+  dp.upload(ctx, pieces);
   DevVec<uint32_t> heads(st);
   heads.resize(head_words(P.total));
-  cuda_check(cudaMemsetAsync(heads.ptr, 0, head_words(P.total) * sizeof(uint32_t), st), "head bitmap clear");
+  ctx.zero(heads.ptr, head_words(P.total) * sizeof(uint32_t));
   GFZ_TIMED(ctx, "head_bits", launch_head_bits(P.out_off.ptr, nt, heads.ptr, st));
   const TextMeta meta{dp.blob.ptr, dp.pre.ptr, dp.suf.ptr, dp.tail.ptr, (uint64_t)pieces.tail.size(), mode};
   TextSource T{P.out_off.ptr, nt, heads.ptr, meta, 0, &ctx.dstatus()->err};
@@ -1603,7 +1690,7 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   GFZ_TIMED_B(ctx, "symbol_text", 16.0 * P.m,
               launch_excl_scan_u64(slen.ptr, P.m, soff.ptr, desc, counter, ctx.dstatus(), st));
   uint64_t body = 0;
-  cuda_check(cudaMemcpyAsync(&body, soff.ptr + P.m, sizeof(body), cudaMemcpyDeviceToHost, st), "text size");
+  ctx.download(&body, soff.ptr + P.m, sizeof(body));
   ctx.read_status();
   ctx.check_status("text lengths");
   const uint64_t size = body + pieces.tail.size();
@@ -1635,9 +1722,12 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
     GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
                 launch_text_write(E, T, g.delta_round, toff.ptr, dst, st));
   }
-  if (!pieces.tail.empty())
-    cuda_check(cudaMemcpyAsync(dst + body, pieces.tail.data(), pieces.tail.size(), cudaMemcpyDefault, st),
-               "text tail");
+  // the tail (the last line's end) after the body: bytes the text kernel
+  // does not write
+  if (!pieces.tail.empty()) {
+    if (to_host) std::memcpy(dst + body, pieces.tail.data(), pieces.tail.size());
+    else ctx.upload(dst + body, pieces.tail.data(), pieces.tail.size());
+  }
   ctx.read_status();
   ctx.check_status("text emission");
   return size;
@@ -1658,8 +1748,8 @@ void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second
   DevVec<uint64_t> offA(st), offB(st), d_len(st);
   offA.resize(nt + 1);
   offB.resize(nt + 1);
-  cuda_check(cudaMemcpyAsync(offA.ptr, off.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
-  if (N) cuda_check(cudaMemcpyAsync(B.ptr, steps.data(), N * 4, cudaMemcpyHostToDevice, st), "upload");
+  ctx.upload(offA.ptr, off.data(), (nt + 1) * 8);
+  if (N) ctx.upload(B.ptr, steps.data(), N * 4);
   ctx.reset_status();
   for (int r = 0; r < delta_round; ++r) {
     GFZ_TIMED(ctx, "delta_encode", launch_delta_encode(B.ptr, A.ptr, N, offA.ptr, nt, &ctx.dstatus()->aux, st));
@@ -1703,8 +1793,8 @@ void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second
         const uint64_t nc = cs.size();
         d_cs.resize(std::max<uint64_t>(nc, 1));
         d_ce.resize(std::max<uint64_t>(nc, 1));
-        cuda_check(cudaMemcpyAsync(d_cs.ptr, cs.data(), nc * 8, cudaMemcpyHostToDevice, st), "upload");
-        cuda_check(cudaMemcpyAsync(d_ce.ptr, ce.data(), nc * 8, cudaMemcpyHostToDevice, st), "upload");
+        ctx.upload(d_cs.ptr, cs.data(), nc * 8);
+        ctx.upload(d_ce.ptr, ce.data(), nc * 8);
         top.resize(n);
         fl.resize(n);
         ctx.reset_status();
@@ -1724,7 +1814,7 @@ void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second
                                                                                             0, offB.ptr)));
         A.swap(B);
         offA.swap(offB);
-        cuda_check(cudaMemcpyAsync(h_off.data(), offA.ptr, (nt + 1) * 8, cudaMemcpyDeviceToHost, st), "download");
+        ctx.download(h_off.data(), offA.ptr, (nt + 1) * 8);
         ctx.read_status();
         ctx.check_status("append encoding");
         n = h_off[nt];
@@ -1737,15 +1827,15 @@ void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second
         std::vector<uint64_t> len(nt);
         for (uint64_t t = 0; t < nt; ++t) len[t] = h_off[t + 1] - h_off[t];
         d_len.resize(nt);
-        cuda_check(cudaMemcpyAsync(d_len.ptr, len.data(), nt * 8, cudaMemcpyHostToDevice, st), "upload");
+        ctx.upload(d_len.ptr, len.data(), nt * 8);
         GFZ_TIMED(ctx, "stack_encode", launch_stack_encode(A.ptr, offA.ptr, d_len.ptr, nt, tab.view(cap),
                                                            ctx.dstatus(), st));
-        cuda_check(cudaMemcpyAsync(len.data(), d_len.ptr, nt * 8, cudaMemcpyDeviceToHost, st), "download");
+        ctx.download(len.data(), d_len.ptr, nt * 8);
         ctx.read_status();
         ctx.check_status("append encoding");
         std::vector<uint64_t> packed(nt + 1, 0);
         for (uint64_t t = 0; t < nt; ++t) packed[t + 1] = packed[t] + len[t];
-        cuda_check(cudaMemcpyAsync(offB.ptr, packed.data(), (nt + 1) * 8, cudaMemcpyHostToDevice, st), "upload");
+        ctx.upload(offB.ptr, packed.data(), (nt + 1) * 8);
         launch_gather_ranges(A.ptr, offA.ptr, offB.ptr, nt, B.ptr, st);
         A.swap(B);
         offA.swap(offB);
@@ -1757,8 +1847,8 @@ void append_encode(Context &ctx, const int32_t *d_first, const int32_t *d_second
   lens.resize(nt);
   for (uint64_t t = 0; t < nt; ++t) lens[t] = h_off[t + 1] - h_off[t];
   steps.resize(n);
-  if (n) cuda_check(cudaMemcpyAsync(steps.data(), A.ptr, n * 4, cudaMemcpyDeviceToHost, st), "download");
-  cuda_check(cudaStreamSynchronize(st), "stream sync");
+  if (n) ctx.download(steps.data(), A.ptr, n * 4);
+  ctx.sync();
 }
 
 }  // namespace gfz

@@ -115,6 +115,21 @@ class Context {
   // Zeroed look-back descriptors (n tiles) + tile counter.
   unsigned long long *lookback(uint64_t tiles, uint32_t **counter);
 
+  // Transfers of up to kSmallCopy bytes between host memory and this
+  // context's device buffers, moved by a kernel through page-locked staging
+  // rather than by a copy engine: a copy engine serves its transfers in
+  // order, so a few bytes of offsets or status would otherwise wait behind
+  // another stream's gigabyte transfer (tens of ms each).  Larger transfers
+  // use cudaMemcpyAsync.  upload: src may be reused on return.  download:
+  // dst holds the bytes after the next sync() or read_status().
+  static constexpr size_t kSmallCopy = 1u << 20;
+  void upload(void *dst, const void *src, size_t bytes);
+  void download(void *dst, const void *src, size_t bytes);
+  // Zero-fills device memory with a kernel (see upload).
+  void zero(void *dst, size_t bytes);
+  // Waits for the stream and completes the pending downloads.
+  void sync();
+
   // Kernel timing (CUDA events on the context stream).
   bool timing = false;
   void tbegin(const char *name, double bytes = 0);
@@ -138,6 +153,13 @@ class Context {
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
   int static_text = 1;           // S/L text of the full-file writer: 1 = device, 0 = host
+#ifndef GFZ_RULE_LAYOUT_DEFAULT
+#define GFZ_RULE_LAYOUT_DEFAULT 0
+#endif
+  // rule prefix buffers in the order of the rules' first use in the encoded
+  // stream (1), so that neighbouring output tiles read neighbouring
+  // buffers, or in rule-id order (0)
+  int rule_layout = GFZ_RULE_LAYOUT_DEFAULT;
   // Tuner: (kernel, stream class) -> the variant that was faster the first
   // time the class came up (see encode_traversals).  With GFAZ_TUNE_FILE
   // set, decisions are loaded from that file when the context is made and
@@ -179,6 +201,17 @@ class Context {
   cudaEvent_t order_ev_[2] = {nullptr, nullptr};
   DevStatus *d_status_ = nullptr;
   DevStatus *h_status_ = nullptr;
+  // page-locked staging of upload / download: bytes [0, stage_used_) belong
+  // to transfers queued since the last sync()
+  char *stage_ = nullptr;
+  size_t stage_cap_ = 0, stage_used_ = 0;
+  struct PendingDownload {
+    void *dst;
+    const char *from;
+    size_t bytes;
+  };
+  std::vector<PendingDownload> downloads_;
+  char *stage(size_t bytes);
   DevVec<unsigned long long> desc_;
   DevVec<uint32_t> counter_;
   struct Pending {

@@ -68,7 +68,10 @@ __device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, c
   for (uint32_t i = head + 16u * body + threadIdx.x; i < len; i += BLOCK) dst[i] = sbuf[i];
 }
 
-constexpr uint32_t kTextBuf = 28 * 1024;
+// Text staging of one output tile: 2048 steps of up to 11 bytes; tiles
+// whose text is longer (long line pieces, ten-digit ids) write to global
+// memory directly.
+constexpr uint32_t kTextBuf = 24 * 1024;
 
 // The four decimal characters of every x < 10000 ("0000" .. "9999"), the
 // first in the low byte; 40 KB that stays in L1 while text is written.
