@@ -13,7 +13,7 @@ delta + P-line text emission).
   e2e    the same through the C ABI with host buffers: pinned host steps in,
          encoded stream + rulebook out to the host (what the entropy stage
          consumes), loaded back from the host and decoded to pinned host
-         text; every copy inside the timed region; two such jobs in flight
+         text; every copy inside the timed region; three such jobs in flight
          at once (--e2e-jobs), each on its own context and stream.
 
 `--impl reference` times the reference algorithm's CPU implementation on
@@ -59,7 +59,7 @@ def parse_args():
                     help="P-lines of the CPU port's timed pass (all 90 by default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-jobs", type=int, default=2, help="end-to-end jobs in flight at once")
+    ap.add_argument("--e2e-jobs", type=int, default=3, help="end-to-end jobs in flight at once")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-traversal-per-launch GPU baseline")
     ap.add_argument("--serve-rate", type=float, default=5000.0, help="extract requests per second")
@@ -395,11 +395,11 @@ def e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, device, ws):
     steps uploaded and compressed (gfz_encode), the encoded stream and rule
     columns copied to pinned host memory (what the entropy stage consumes),
     loaded back from there (gfz_grammar_load) and decoded to P-line text in a
-    pinned host buffer (gfz_decode_text).  args.e2e_jobs jobs are in flight
-    at once, each on its own context, CUDA stream and host buffers (host
-    threads; the library calls release the interpreter lock), so one job's
-    uploads and kernels overlap another's text download over the
-    chip-to-chip link.  Every step is one whole job with all of its copies;
+    pinned host buffer (gfz_decode_text; the library stages the text in HBM
+    and a copy engine moves it).  args.e2e_jobs jobs are in flight at once,
+    each on its own context, CUDA stream and host buffers (host threads; the
+    library calls release the interpreter lock), so one job's upload and
+    kernels overlap another's text download over the chip-to-chip link.  Every step is one whole job with all of its copies;
     the time is the wall clock from the first job's start to the last one's
     end, with the device synchronised on both sides."""
     import ctypes
@@ -450,28 +450,34 @@ def e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, device, ws):
     for sl in slots:  # warm-up one after the other: each context tunes alone
         for _ in range(max(1, args.warmup // 2)):
             sl.run()
-    k2 = max(jobs, min(args.steps, 3 * jobs))
-    results = [None] * k2
     errors = []
 
-    def worker(j):
+    def worker(j, count, results):
         try:
-            for i in range(j, k2, jobs):
+            for i in range(j, count, jobs):
                 results[i] = slots[j].run()
         except Exception as e:  # reported after the join
             errors.append(e)
 
+    def in_flight(count, results):
+        ths = [threading.Thread(target=worker, args=(j, count, results)) for j in range(jobs)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        if errors:
+            raise errors[0]
+
+    # and once all at once: the device memory pool grows to what the jobs
+    # hold together now, not inside the timed region
+    in_flight(jobs, [None] * jobs)
+    k2 = max(jobs, min(args.steps, 3 * jobs))
+    results = [None] * k2
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    ths = [threading.Thread(target=worker, args=(j,)) for j in range(jobs)]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
+    in_flight(k2, results)
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
-    if errors:
-        raise errors[0]
     e2e_ms = wall * 1e3 / k2
     info, n = results[-1]
     heads_ok = all(bytes(sl.text[:64].numpy().tobytes()).startswith(b"P\thap0\t") for sl in slots)

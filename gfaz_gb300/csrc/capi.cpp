@@ -147,12 +147,15 @@ gfz::TextPieces pieces_from_meta(const gfz_line_meta *m, const std::vector<uint6
   return gfz::walk_pieces(s, h, q, a, b, off);
 }
 
+// Device bytes to the caller's buffer (complete after ctx.sync()).
 void copy_out(gfz::Context &ctx, void *dst, const void *src_dev, size_t bytes, int where) {
   if (!bytes) return;
-  gfz::cuda_check(cudaMemcpyAsync(dst, src_dev, bytes,
-                                  where == GFZ_WHERE_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                  ctx.stream()),
-                  "copy out");
+  if (where == GFZ_WHERE_DEVICE) {
+    gfz::launch_copy_bytes(src_dev, dst, bytes, ctx.stream());
+    ctx.count_launch();
+  } else {
+    ctx.download(dst, src_dev, bytes);
+  }
 }
 
 }  // namespace
@@ -241,9 +244,9 @@ gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t va
     } else if (std::string(name) == "table_tuner") {
       require(value == 0 || value == 1, "table_tuner must be 0 or 1");
       c.table_tuner = value != 0;
-    } else if (std::string(name) == "rule_layout") {
-      require(value == 0 || value == 1, "rule_layout must be 0 (rule ids) or 1 (first use)");
-      c.rule_layout = (int)value;
+    } else if (std::string(name) == "host_text") {
+      require(value == 0 || value == 1, "host_text must be 0 (written by the kernel) or 1 (staged in HBM)");
+      c.host_text = (int)value;
     } else if (std::string(name) == "static_text") {
       require(value == 0 || value == 1, "static_text must be 0 (host) or 1 (device)");
       c.static_text = (int)value;
@@ -625,7 +628,7 @@ gfz_status gfz_grammar_copy(gfz_context *ctx, const gfz_grammar *g, int32_t *enc
     if (encoded) copy_out(c, encoded, g->g.enc.ptr, m * 4, where);
     if (rules) copy_out(c, rules, g->g.rules.ptr, g->g.nrules * 8, where);
     if (offsets) std::memcpy(offsets, g->g.h_off.data(), g->g.h_off.size() * 8);
-    gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+    c.sync();
   });
 }
 
@@ -638,7 +641,7 @@ gfz_status gfz_grammar_rule_columns(gfz_context *ctx, const gfz_grammar *g, int3
     gfz::rule_columns_delta(c, g->g, f, s);
     copy_out(c, first, f.ptr, g->g.nrules * 4, where);
     copy_out(c, second, s.ptr, g->g.nrules * 4, where);
-    gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+    c.sync();
   });
 }
 
@@ -671,7 +674,7 @@ gfz_status gfz_grammar_load(gfz_context *ctx, const int32_t *encoded, const uint
     gfz::load_rules(c, g->g, pf, ps, num_rules, min_rule_id);
     g->g.delta_round = delta_round < 0 ? 0 : delta_round;
     gfz::load_encoded(c, g->g, pe, off);
-    gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+    c.sync();
     *out = g.release();
   });
 }
@@ -692,7 +695,7 @@ gfz_status gfz_decode(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64_t t1
       if (cap < off.back()) throw std::length_error("output buffer too small");
       copy_out(c, out, x.ptr, off.back() * 4, where);
     }
-    gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+    c.sync();
   });
 }
 
@@ -717,7 +720,7 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
     }
     if (direct) {
       g->text_size = gfz::decode_text(c, g->g, t0, t1, pieces, meta->mode, g->text, direct, cap);
-      gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+      c.sync();
       g->text_external = true;
     } else {
       g->text_size = gfz::decode_text(c, g->g, t0, t1, pieces, meta->mode, g->text);
@@ -727,7 +730,7 @@ gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64
     if (out && !direct) {
       if (cap < g->text_size) throw std::length_error("output buffer too small");
       copy_out(c, out, g->text.ptr, g->text_size, where);
-      gfz::cuda_check(cudaStreamSynchronize(c.stream()), "stream sync");
+      c.sync();
     }
     (void)where;
   });

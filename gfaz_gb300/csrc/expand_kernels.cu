@@ -73,37 +73,6 @@ struct RangeAcc {
   }
 };
 
-// First use of every rule in the encoded stream (see launch_first_use).
-__global__ void k_first_use_init(uint64_t nrules, unsigned long long *key, uint32_t *idx) {
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nrules; r += (uint64_t)gridDim.x * blockDim.x) {
-    key[r] = 0xFFFFFFFFull;
-    idx[r] = (uint32_t)r;
-  }
-}
-
-__global__ void k_first_use(const int32_t *__restrict__ enc, uint64_t m, uint32_t min_id, uint64_t nrules,
-                            unsigned long long *key) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = abs32(enc[i]);
-    if (!is_rule(a, min_id, nrules)) continue;
-    unsigned long long *k = key + (a - min_id);
-    if (*k > i) atomicMin(k, (unsigned long long)i);  // a plain read skips most atomics of later uses
-  }
-}
-
-__global__ void k_lens_in_order(const uint32_t *__restrict__ idx, const uint32_t *__restrict__ rlen, uint64_t nrules,
-                                uint32_t *lens) {
-  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nrules; j += (uint64_t)gridDim.x * blockDim.x)
-    lens[j] = rlen[idx[j]];
-}
-
-__global__ void k_offsets_from_order(const uint32_t *__restrict__ idx, const uint64_t *__restrict__ at,
-                                     uint64_t nrules, uint64_t *roff) {
-  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= nrules;
-       j += (uint64_t)gridDim.x * blockDim.x)
-    roff[j < nrules ? idx[j] : nrules] = at[j];
-}
-
 constexpr uint32_t kWarpRule = 16;  // rules longer than this are written by a whole warp
 
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
@@ -524,13 +493,13 @@ __global__ void k_tile_text_off(ExpandSource E, TextSource T, const uint64_t *__
 // (4.49 against 5.22 ms per step at five blocks).
 template <int BLOCK, int ITEMS, int DELTA>
 __global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSource T, const uint64_t *__restrict__ toff,
-                                                      char *__restrict__ text) {
+                                                      char *__restrict__ text, uint64_t tile0, uint64_t ntiles) {
   static_assert(ITEMS <= 8, "digit counts are packed 4 bits per step");
   constexpr uint32_t TILE = BLOCK * ITEMS;
   constexpr uint32_t kWords = kTextBuf / 4 + 8;
   __shared__ __align__(16) uint32_t sbuf[kWords];
   __shared__ SymStage S;
-  const uint64_t tile = blockIdx.x;
+  const uint64_t tile = tile0 + blockIdx.x;
   const bool pmode = T.meta.mode == 0;
   const uint32_t per = pmode ? 2u : 1u;
   stage_symbols<BLOCK>(E, tile, S);
@@ -566,7 +535,7 @@ __global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSou
   const unsigned long long my = block_excl_sum<BLOCK>(len, total);
   const unsigned long long t0 = toff[tile];
   if (threadIdx.x == 0) {
-    const unsigned long long want = tile + 1 < gridDim.x ? toff[tile + 1] : T.cap;
+    const unsigned long long want = tile + 1 < ntiles ? toff[tile + 1] : T.cap;
     if (t0 + total != want) atomicOr(T.err, kErrLength);
   }
   if (total <= kTextBuf) {
@@ -701,24 +670,6 @@ uint64_t excl_scan_tiles(uint64_t n) {
   return (n + TILE - 1) / TILE;
 }
 
-void launch_first_use(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules, unsigned long long *key,
-                      uint32_t *idx, cudaStream_t st) {
-  if (!nrules) return;
-  k_first_use_init<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(nrules, key, idx);
-  if (m) k_first_use<<<grid_for(m, kBlock), kBlock, 0, st>>>(enc, m, min_id, nrules, key);
-}
-
-void launch_lens_in_order(const uint32_t *idx, const uint32_t *rlen, uint64_t nrules, uint32_t *lens,
-                          cudaStream_t st) {
-  if (!nrules) return;
-  k_lens_in_order<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(idx, rlen, nrules, lens);
-}
-
-void launch_offsets_from_order(const uint32_t *idx, const uint64_t *at, uint64_t nrules, uint64_t *roff,
-                               cudaStream_t st) {
-  k_offsets_from_order<<<grid_for(nrules + 1, kBlock), kBlock, 0, st>>>(idx, at, nrules, roff);
-}
-
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
                              int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status, int slot,
                              cudaStream_t st) {
@@ -790,13 +741,15 @@ void launch_tile_text_off(const ExpandSource &E, const TextSource &T, int delta,
 }
 
 void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *toff, char *text,
-                       cudaStream_t st) {
+                       cudaStream_t st, uint64_t tile0, uint64_t tile1) {
   const uint64_t nt = expand_num_tiles(E.total);
-  if (!nt) return;
+  tile1 = std::min(tile1, nt);
+  if (tile0 >= tile1) return;
+  const unsigned grid = (unsigned)(tile1 - tile0);
   if (delta)
-    k_text_write<kBlock, kExpandItems, 1><<<(unsigned)nt, kBlock, 0, st>>>(E, T, toff, text);
+    k_text_write<kBlock, kExpandItems, 1><<<grid, kBlock, 0, st>>>(E, T, toff, text, tile0, nt);
   else
-    k_text_write<kBlock, kExpandItems, 0><<<(unsigned)nt, kBlock, 0, st>>>(E, T, toff, text);
+    k_text_write<kBlock, kExpandItems, 0><<<grid, kBlock, 0, st>>>(E, T, toff, text, tile0, nt);
 }
 
 }  // namespace gfz

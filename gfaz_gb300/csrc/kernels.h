@@ -263,19 +263,6 @@ struct TextSource {
   uint64_t cap;   // bytes of the text buffer
   uint32_t *err;  // kErrLength when the text would not fit where its lengths say
 };
-// Rule order of the prefix buffer by first use: key[r] = the first position
-// of the encoded stream enc[0, m) (m < 2^32) that holds rule r (either
-// orientation), 2^32 - 1 for rules never used there; idx[r] = r.  Sorted
-// by key, idx lists the rules in the order their buffers are laid out.
-void launch_first_use(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules, unsigned long long *key,
-                      uint32_t *idx, cudaStream_t st);
-// lens[j] = rlen[idx[j]] for j < nrules.
-void launch_lens_in_order(const uint32_t *idx, const uint32_t *rlen, uint64_t nrules, uint32_t *lens,
-                          cudaStream_t st);
-// roff[idx[j]] = at[j] for j < nrules and roff[nrules] = at[nrules]: the
-// buffer offsets of rules laid out in the order idx.
-void launch_offsets_from_order(const uint32_t *idx, const uint64_t *at, uint64_t nrules, uint64_t *roff,
-                               cudaStream_t st);
 // One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
 // waiting, zero before pass 1).  status->pass_open[slot] += rules still
 // waiting.
@@ -310,9 +297,10 @@ void launch_symbol_text(const ExpandSource &E, const TextSource &T, int delta, u
 // per-symbol text offsets soff and shared digit counts sdig.
 void launch_tile_text_off(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *soff,
                           const uint8_t *sdig, uint64_t *toff, cudaStream_t st);
-// The text of every output tile at toff[tile]; T.cap = the body size.
+// The text of output tiles [tile0, tile1) (all by default) at toff[tile];
+// T.cap = the body size.
 void launch_text_write(const ExpandSource &E, const TextSource &T, int delta, const uint64_t *toff, char *text,
-                       cudaStream_t st);
+                       cudaStream_t st, uint64_t tile0 = 0, uint64_t tile1 = UINT64_MAX);
 // Adds the number of '\n' bytes in text[0, n) (16-byte aligned buffer) to
 // out[0] (zero it first); out[1 .. min(count, cap)] = their positions,
 // unordered.

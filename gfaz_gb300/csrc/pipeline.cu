@@ -277,10 +277,24 @@ char *Context::stage(size_t bytes) {
   return p;
 }
 
-void Context::upload(void *dst, const void *src, size_t bytes) {
+// Page-locked (or device) memory a kernel can address directly.
+static bool device_addressable(const void *p) {
+  cudaPointerAttributes a{};
+  const bool ok = cudaPointerGetAttributes(&a, p) == cudaSuccess &&
+                  (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice);
+  (void)cudaGetLastError();
+  return ok;
+}
+
+void Context::upload(void *dst, const void *src, size_t bytes, bool bulk) {
   if (!bytes) return;
   if (bytes > kSmallCopy) {
-    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "upload");
+    if (!bulk && device_addressable(src)) {
+      launch_copy_bytes(src, dst, bytes, stream_);
+      count_launch();
+    } else {
+      cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "upload");
+    }
     return;
   }
   char *p = stage(bytes);
@@ -289,10 +303,15 @@ void Context::upload(void *dst, const void *src, size_t bytes) {
   count_launch();
 }
 
-void Context::download(void *dst, const void *src, size_t bytes) {
+void Context::download(void *dst, const void *src, size_t bytes, bool bulk) {
   if (!bytes) return;
   if (bytes > kSmallCopy) {
-    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "download");
+    if (!bulk && device_addressable(dst)) {
+      launch_copy_bytes(src, dst, bytes, stream_);
+      count_launch();
+    } else {
+      cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), "download");
+    }
     return;
   }
   char *p = stage(bytes);
@@ -1257,7 +1276,7 @@ void encode_host(Context &ctx, const std::vector<HostSeg> &input, const std::vec
   d.resize(std::max<uint64_t>(N, 1));
   uint64_t at = 0;
   for (const HostSeg &sg : input) {
-    if (sg.n) ctx.upload(d.ptr + at, sg.p, sg.n * sizeof(int32_t));
+    if (sg.n) ctx.upload(d.ptr + at, sg.p, sg.n * sizeof(int32_t), true);
     at += sg.n;
   }
   if (at != N) throw std::invalid_argument("input segments do not hold the offsets' steps");
@@ -1381,42 +1400,9 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
   const uint64_t R = g.nrules;
   g.roff.resize(R + 1);
   ctx.reset_status();
-  const uint64_t m = g.h_off.empty() ? 0 : g.h_off.back();
-  if (ctx.rule_layout == 1 && R > 1 && m < 0xFFFFFFFFull) {
-    // buffers in first-use order: sort the rules by the first position of
-    // the encoded stream that holds them (4 bytes of key), then lay their
-    // lengths out in that order
-    DevVec<unsigned long long> key(st), key2(st);
-    DevVec<uint32_t> idx(st), idx2(st), hist(st), lens(st);
-    DevVec<uint64_t> at(st);
-    key.resize(R);
-    key2.resize(R);
-    idx.resize(R);
-    idx2.resize(R);
-    hist.resize(8 * 256);
-    lens.resize(R);
-    at.resize(R + 1);
-    GFZ_TIMED(ctx, "rule_prefix", launch_first_use(g.enc.ptr, m, g.layer_start, R, key.ptr, idx.ptr, st));
-    ctx.zero(hist.ptr, 8 * 256 * sizeof(uint32_t));
-    GFZ_TIMED(ctx, "rule_prefix", launch_sort_hist(key.ptr, R, 0x0Fu, hist.ptr, st));
-    for (int b = 0; b < 4; ++b) {
-      uint32_t *counter;
-      unsigned long long *desc = ctx.lookback(sort_tiles(R) * 256, &counter);
-      const bool odd = b & 1;
-      GFZ_TIMED(ctx, "rule_prefix",
-                launch_sort_pass(odd ? key2.ptr : key.ptr, odd ? idx2.ptr : idx.ptr, odd ? key.ptr : key2.ptr,
-                                 odd ? idx.ptr : idx2.ptr, R, b, hist.ptr, desc, counter, &ctx.dstatus()->err, st));
-    }
-    GFZ_TIMED(ctx, "rule_prefix", launch_lens_in_order(idx.ptr, g.rlen.ptr, R, lens.ptr, st));
-    uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
-    GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(lens.ptr, R, at.ptr, desc, counter, ctx.dstatus(), st));
-    GFZ_TIMED(ctx, "rule_prefix", launch_offsets_from_order(idx.ptr, at.ptr, R, g.roff.ptr, st));
-  } else {
-    uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
-    GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(g.rlen.ptr, R, g.roff.ptr, desc, counter, ctx.dstatus(), st));
-  }
+  uint32_t *counter;
+  unsigned long long *desc = ctx.lookback(excl_scan_tiles(R), &counter);
+  GFZ_TIMED(ctx, "rule_prefix", launch_excl_scan_u32(g.rlen.ptr, R, g.roff.ptr, desc, counter, ctx.dstatus(), st));
   uint64_t steps = 0;
   ctx.download(&steps, g.roff.ptr + R, sizeof(steps));
   ctx.read_status();
@@ -1646,6 +1632,9 @@ struct DevPieces {
   }
 };
 
+// Pieces of the staged host text (each copied while the next is written).
+constexpr uint64_t kStagedTextPieces = 8;
+
 uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
                      const std::function<TextPieces(const std::vector<uint64_t> &)> &make_pieces, int mode,
                      DevVec<char> &text, char *direct, uint64_t direct_cap) {
@@ -1695,13 +1684,20 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   ctx.check_status("text lengths");
   const uint64_t size = body + pieces.tail.size();
   char *dst;
-  bool to_host = false;
+  bool to_host = false, staged = false;
   if (direct) {
     if (direct_cap < size) throw std::length_error("output buffer too small");
     dst = direct;
     cudaPointerAttributes a{};
     to_host = cudaPointerGetAttributes(&a, direct) == cudaSuccess && a.type == cudaMemoryTypeHost;
     (void)cudaGetLastError();
+    if (to_host && ctx.host_text == 1) {
+      // staged: the kernel writes HBM, a copy engine moves the bytes
+      staged = true;
+      text.resize(std::max<uint64_t>(size, 1));
+      text.size = size;
+      dst = text.ptr;
+    }
   } else {
     text.resize(std::max<uint64_t>(size, 1));
     text.size = size;
@@ -1711,13 +1707,33 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   DevVec<uint64_t> toff(st);
   toff.resize(std::max<uint64_t>(expand_num_tiles(P.total), 1));
   GFZ_TIMED(ctx, "symbol_text", launch_tile_text_off(E, T, g.delta_round, soff.ptr, sdig.ptr, toff.ptr, st));
-  if (to_host) {
+  if (to_host && !staged) {
     // bound by the chip-to-chip link: on the low-priority stream
     cudaStream_t low = ctx.low_stream();
     ctx.order(st, low);
     GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
                 launch_text_write(E, T, g.delta_round, toff.ptr, dst, low);
                 ctx.order(low, st));
+  } else if (staged) {
+    // in pieces of output tiles: a copy engine moves piece k into host
+    // memory (on the low-priority stream) while the kernel writes piece k + 1
+    const uint64_t nt = expand_num_tiles(P.total);
+    const uint64_t np = std::max<uint64_t>(1, std::min<uint64_t>(nt, kStagedTextPieces));
+    std::vector<uint64_t> cut(np + 1), at(np + 1);
+    for (uint64_t k = 0; k <= np; ++k) cut[k] = nt * k / np;
+    for (uint64_t k = 0; k < np; ++k) ctx.download(&at[k], toff.ptr + cut[k], sizeof(uint64_t));
+    ctx.sync();
+    at[np] = body;
+    cudaStream_t low = ctx.low_stream();
+    for (uint64_t k = 0; k < np; ++k) {
+      GFZ_TIMED_B(ctx, "text_write", k ? 0.0 : 4.0 * P.total + (double)body,
+                  launch_text_write(E, T, g.delta_round, toff.ptr, dst, st, cut[k], cut[k + 1]));
+      ctx.order(st, low);
+      if (at[k + 1] > at[k])
+        cuda_check(cudaMemcpyAsync(direct + at[k], dst + at[k], at[k + 1] - at[k], cudaMemcpyDeviceToHost, low),
+                   "text download");
+    }
+    ctx.order(low, st);
   } else {
     GFZ_TIMED_B(ctx, "text_write", 4.0 * P.total + (double)body,
                 launch_text_write(E, T, g.delta_round, toff.ptr, dst, st));
@@ -1725,7 +1741,7 @@ uint64_t decode_text(Context &ctx, Grammar &g, uint64_t t0, uint64_t t1,
   // the tail (the last line's end) after the body: bytes the text kernel
   // does not write
   if (!pieces.tail.empty()) {
-    if (to_host) std::memcpy(dst + body, pieces.tail.data(), pieces.tail.size());
+    if (to_host) std::memcpy(direct + body, pieces.tail.data(), pieces.tail.size());
     else ctx.upload(dst + body, pieces.tail.data(), pieces.tail.size());
   }
   ctx.read_status();

@@ -115,16 +115,21 @@ class Context {
   // Zeroed look-back descriptors (n tiles) + tile counter.
   unsigned long long *lookback(uint64_t tiles, uint32_t **counter);
 
-  // Transfers of up to kSmallCopy bytes between host memory and this
-  // context's device buffers, moved by a kernel through page-locked staging
-  // rather than by a copy engine: a copy engine serves its transfers in
-  // order, so a few bytes of offsets or status would otherwise wait behind
-  // another stream's gigabyte transfer (tens of ms each).  Larger transfers
-  // use cudaMemcpyAsync.  upload: src may be reused on return.  download:
-  // dst holds the bytes after the next sync() or read_status().
+  // Transfers between host memory and this context's device buffers, moved
+  // by kernels rather than by copy engines: a copy engine serves its
+  // transfers in order, so a few bytes of offsets or status, or a grammar's
+  // megabytes, would otherwise wait behind another stream's gigabyte
+  // transfer (tens of ms each).  Up to kSmallCopy bytes go through
+  // page-locked staging; larger ones are read from or written into
+  // page-locked host memory by the kernel directly.  Larger ones with
+  // pageable host memory, and bulk ones (a long one-way stream such as the
+  // input steps, left to a copy engine so that it holds no SMs), use
+  // cudaMemcpyAsync.  upload: src may be reused on return when it is
+  // pageable.  download: dst holds the bytes after the next sync() or
+  // read_status().
   static constexpr size_t kSmallCopy = 1u << 20;
-  void upload(void *dst, const void *src, size_t bytes);
-  void download(void *dst, const void *src, size_t bytes);
+  void upload(void *dst, const void *src, size_t bytes, bool bulk = false);
+  void download(void *dst, const void *src, size_t bytes, bool bulk = false);
   // Zero-fills device memory with a kernel (see upload).
   void zero(void *dst, size_t bytes);
   // Waits for the stream and completes the pending downloads.
@@ -153,13 +158,11 @@ class Context {
   int classify_kernel = -1;      // 0 = persistent, 1 = flat; -1 = chosen by the tuner
   int front_end = 1;             // GFA parse: 1 = device front end, 0 = host parser
   int static_text = 1;           // S/L text of the full-file writer: 1 = device, 0 = host
-#ifndef GFZ_RULE_LAYOUT_DEFAULT
-#define GFZ_RULE_LAYOUT_DEFAULT 0
-#endif
-  // rule prefix buffers in the order of the rules' first use in the encoded
-  // stream (1), so that neighbouring output tiles read neighbouring
-  // buffers, or in rule-id order (0)
-  int rule_layout = GFZ_RULE_LAYOUT_DEFAULT;
+  // P/W text for page-locked host memory: 1 (default) = the kernel writes
+  // HBM and a copy engine moves it, piece by piece; 0 = the text kernel
+  // writes host memory itself (its stores then starve concurrent uploads
+  // of other contexts, whose read requests travel the same way)
+  int host_text = 1;
   // Tuner: (kernel, stream class) -> the variant that was faster the first
   // time the class came up (see encode_traversals).  With GFAZ_TUNE_FILE
   // set, decisions are loaded from that file when the context is made and

@@ -60,11 +60,12 @@ unsigned gfz_zstd_version(void);
 
 /* ---- contexts ------------------------------------------------------------ */
 /* cuda_stream may be NULL (the context creates its own stream, one step
- * above the lowest priority).  Text that gfz_decode_text writes into host
- * memory is bound by the chip-to-chip link; its kernel runs on a stream of
- * the lowest priority ordered after the context's stream, so that work of
- * other streams of higher priority (another context's compression) takes
- * SMs while it runs.  Grammars
+ * above the lowest priority).  Text that gfz_decode_text puts into host
+ * memory is bound by the chip-to-chip link: its copies (or, with
+ * "host_text" 0, its kernel) run on a stream of the lowest priority
+ * ordered after the context's stream.  Every other transfer of a context
+ * is made by kernels, so that it never waits behind another stream's
+ * copy-engine transfer.  Grammars
  * free their device memory on the stream of the context that made them:
  * free them before that context, and keep a caller's stream alive until
  * the context is destroyed. */
@@ -111,7 +112,11 @@ gfz_status gfz_context_kernel_stats(gfz_context *ctx, int reset, char **json, si
  * table's size (hash load factor) is tuned per stream class (the count
  * timed with tables for load <= 3/4, 1/2, 1/4 and at the estimate's size,
  * the fastest kept), 0 = sized from the estimate alone; results are the
- * same either way. */
+ * same either way; "host_text" = how gfz_decode_text fills a page-locked
+ * host buffer: 1 (default) = the text is written to HBM and moved by a copy
+ * engine in pieces, each copied while the next is written, 0 = the text
+ * kernel writes host memory directly (its stores then slow uploads of
+ * other contexts running at the same time); the same bytes. */
 gfz_status gfz_context_set_option(gfz_context *ctx, const char *name, int64_t value);
 
 /* ---- workflows (ctx may be NULL: a default context on device 0) ---------- */
@@ -261,10 +266,11 @@ typedef struct {
  * and format_*_line_numeric, src/io/gfa_write_utils.cpp:238-290).  With
  * out == NULL the text stays in a device buffer owned by `g`
  * (gfz_grammar_text gives its address); otherwise it goes to out (capacity
- * cap bytes, host or device per `where`).  When out is device memory or
- * page-locked host memory the kernels write the text there directly (no
- * staging copy; host memory over the chip-to-chip link) and `g` keeps no
- * copy: gfz_grammar_text then fails until the next decode without out. */
+ * cap bytes, host or device per `where`).  When out is device memory the
+ * kernels write the text there directly; page-locked host memory gets it
+ * as "host_text" says (staged in HBM and copied in pieces by default, or
+ * written by the kernel); either way `g` keeps no copy: gfz_grammar_text
+ * then fails until the next decode without out. */
 gfz_status gfz_decode_text(gfz_context *ctx, gfz_grammar *g, uint64_t t0, uint64_t t1, const gfz_line_meta *meta,
                            char *out, uint64_t cap, uint64_t *size, int where);
 gfz_status gfz_grammar_text(const gfz_grammar *g, const char **device_text, uint64_t *size);

@@ -176,25 +176,6 @@ def test_count_kernels_give_same_result(gpu_ctx):
             np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("delta_round", [0, 1])
-def test_rule_layout_first_use(delta_round):
-    """Rule prefix buffers laid out in first-use order (rule_layout 1) and
-    in rule-id order (0) decode to the same steps and the oracle's P text."""
-    steps, off, _ = synthetic.cfg2_stream(seed=6, n_segments=300_000, n_paths=9)
-    n = len(off) - 1
-    names = [f"h{i}" for i in range(n)]
-    ovs = ["*"] * n
-    want = oracle.format_p(steps, off, names, ovs)
-    for layout in (1, 0):
-        ctx = gz.Context(0)
-        ctx.set_option("rule_layout", layout)
-        g = gz.encode(steps, off, delta_round=delta_round, ctx=ctx)
-        assert g.text(0, n, names=names, overlaps=ovs) == want
-        x, xoff = g.decode()
-        np.testing.assert_array_equal(x, steps)
-        del g, ctx
-
-
 def test_cfg3_walk_text(gpu_ctx):
     # config-3 shape: uneven walks (lognormal lengths, sigma 2) as W lines
     steps, off, _, meta = synthetic.cfg3_stream(seed=3, n_backbone=200_000, n_walks=300, median=5e3, sigma=2.0,
@@ -264,13 +245,16 @@ def test_tuners_on_a_prefix(monkeypatch):
 
 
 
-def test_text_into_page_locked_memory():
-    """P text decoded straight into page-locked host memory (the text kernel
-    writes it there, on the context's low-priority stream) equals the
-    oracle's text; the steps decode back exactly."""
+@pytest.mark.parametrize("host_text", [0, 1])
+def test_text_into_page_locked_memory(host_text):
+    """P text decoded into page-locked host memory, written there by the text
+    kernel on the context's low-priority stream (host_text 0) or staged in
+    HBM and moved by a copy engine (1), equals the oracle's text; the steps
+    decode back exactly."""
     torch = pytest.importorskip("torch")
     steps, off, _ = synthetic.cfg2_stream(seed=8, n_segments=60_000, n_paths=7)
     ctx = gz.Context(0)
+    ctx.set_option("host_text", host_text)
     g = gz.encode(steps, off, ctx=ctx)
     n = len(off) - 1
     names = [f"hap{i}" for i in range(n)]
