@@ -471,7 +471,7 @@ def e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, device, ws):
     # and once all at once: the device memory pool grows to what the jobs
     # hold together now, not inside the timed region
     in_flight(jobs, [None] * jobs)
-    k2 = max(jobs, min(args.steps, 3 * jobs))
+    k2 = jobs * max(1, -(-args.steps // jobs))  # the timed steps rounded up to whole rounds of the jobs
     results = [None] * k2
     torch.cuda.synchronize()
     w0 = time.perf_counter()
@@ -589,11 +589,6 @@ def main():
                    "gbps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None}
                for k, v in sorted(kstats.items(), key=lambda kv: -kv[1]["ms"])}
 
-    # end to end through the C ABI with host buffers
-    e2e = None
-    if not args.no_e2e:
-        e2e = e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, local, ws)
-
     cpu = None
     grammar_parity = "not compared"
     grammar_ok = True
@@ -607,6 +602,12 @@ def main():
             # the GPU grammar of the parity step against the port's, element by element
             grammar_ok = all(np.array_equal(a, b) for a, b in zip(gpu_grammar, cpu_grammar))
             grammar_parity = "identical to the CPU port's" if grammar_ok else "MISMATCH with the CPU port's"
+
+    # end to end through the C ABI with host buffers (after the CPU leg: the
+    # jobs' page-locked buffers stay with the process)
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_bench(args, steps, off, names, overlaps, ginfo, text_bytes, local, ws)
 
     # plain GPU form: the same kernels with one traversal per launch sequence
     # (compression encodes each P-line as its own stream, so its rulebooks
