@@ -126,10 +126,15 @@ __global__ void k_zero_bytes(char *dst, uint64_t n) {
   for (uint64_t i = lead + words * 16 + tid; i < n; i += stride) dst[i] = 0;
 }
 
-__global__ void k_table_clear(PairTable tab, uint32_t val_init) {
+__global__ void k_table_clear(PairTable tab, uint32_t val_init, uint32_t *bits_a, uint32_t *bits_b) {
   const uint4 empty = make_uint4((uint32_t)kEmptyKey, (uint32_t)(kEmptyKey >> 32), 0u, val_init);
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tab.cap; i += (uint64_t)gridDim.x * blockDim.x)
-    reinterpret_cast<uint4 *>(tab.slots)[i] = empty;
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = tid; i < tab.cap; i += stride) reinterpret_cast<uint4 *>(tab.slots)[i] = empty;
+  const uint64_t words = (tab.cap + 31) / 32;
+  for (uint64_t i = tid; i < words; i += stride) {
+    if (bits_a) bits_a[i] = 0;
+    if (bits_b) bits_b[i] = 0;
+  }
 }
 
 struct InsertCounts {
@@ -1727,8 +1732,8 @@ void launch_zero_bytes(void *dst, uint64_t n, cudaStream_t st) {
   k_zero_bytes<<<grid_for((n + 15) / 16, kBlock, 152u * 8u), kBlock, 0, st>>>(static_cast<char *>(dst), n);
 }
 
-void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st) {
-  k_table_clear<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, val_init);
+void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st, uint32_t *bits_a, uint32_t *bits_b) {
+  k_table_clear<<<grid_for(tab.cap, kBlock), kBlock, 0, st>>>(tab, val_init, bits_a, bits_b);
 }
 
 void launch_build_rule_table(const int32_t *first, const int32_t *second, uint64_t lo, uint64_t hi, uint32_t start,

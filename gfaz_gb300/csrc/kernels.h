@@ -41,8 +41,10 @@ struct PairTable {
 void launch_copy_bytes(const void *src, void *dst, uint64_t n, cudaStream_t st);
 // dst[0, n) = 0 by a kernel.
 void launch_zero_bytes(void *dst, uint64_t n, cudaStream_t st);
-// Sets every slot to {kEmptyKey, 0, val_init}.
-void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st);
+// Sets every slot to {kEmptyKey, 0, val_init} and clears the (cap + 31) / 32
+// words of the slot bitmaps given (bits_a, bits_b; either may be null).
+void launch_table_clear(PairTable tab, uint32_t val_init, cudaStream_t st, uint32_t *bits_a = nullptr,
+                        uint32_t *bits_b = nullptr);
 
 // Traversal-head bitmap of an n-step stream: head_words(n) words (padded
 // for tile staging); bit q set <=> some off[t] == q (t <= ntrav, so bit n is

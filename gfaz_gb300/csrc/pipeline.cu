@@ -128,7 +128,7 @@ bool debug_enabled() {
 // ---------------------------------------------------------------------------
 constexpr unsigned long long kAllOnes = ~0ull;
 
-Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullptr), counter_(nullptr) {
+Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullptr) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
   cudaDeviceProp prop;
   cuda_check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
@@ -151,14 +151,12 @@ Context::Context(int device, cudaStream_t stream) : device_(device), desc_(nullp
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
   desc_ = DevVec<unsigned long long>(stream_);
-  counter_ = DevVec<uint32_t>(stream_);
   sref_buf = DevVec<uint32_t>(stream_);
   rep_buf = DevVec<uint32_t>(stream_);
   cuda_check(cudaMalloc((void **)&d_status_, sizeof(DevStatus)), "status alloc");
   cuda_check(cudaMallocHost((void **)&h_status_, sizeof(DevStatus)), "status alloc");
   std::memset(h_status_, 0, sizeof(DevStatus));
   cuda_check(cudaMemsetAsync(d_status_, 0, sizeof(DevStatus), stream_), "status clear");
-  counter_.resize(1);
   if (const char *e = std::getenv("GFAZ_TUNE_STEPS")) {
     const long long v = std::atoll(e);
     if (v > 0) tune_steps = (uint64_t)v;
@@ -193,7 +191,6 @@ Context::~Context() {
   // every device vector of the context frees on its stream: before the
   // stream is destroyed below
   desc_.release();
-  counter_.release();
   sref_buf.release();
   rep_buf.release();
   cudaStreamSynchronize(stream_);
@@ -343,11 +340,16 @@ void Context::check_status(const char *stage) {
   throw std::runtime_error(describe_device_error(stage, e));
 }
 
-unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) {
-  desc_.resize(std::max<uint64_t>(tiles, 1));
-  zero(desc_.ptr, std::max<uint64_t>(tiles, 1) * sizeof(unsigned long long));
-  zero(counter_.ptr, sizeof(uint32_t));
-  *counter = counter_.ptr;
+unsigned long long *Context::lookback(uint64_t tiles, uint32_t **counter) { return lookback_n(tiles, 1, counter); }
+
+unsigned long long *Context::lookback_n(uint64_t tiles, int n, uint32_t **counters) {
+  tiles = std::max<uint64_t>(tiles, 1);
+  // the n regions, then the n tile counters (two to a word): one fill
+  const uint64_t words = tiles * (uint64_t)n + ((uint64_t)n + 1) / 2;
+  desc_.resize(words);
+  zero(desc_.ptr, words * sizeof(unsigned long long));
+  uint32_t *c = reinterpret_cast<uint32_t *>(desc_.ptr + tiles * (uint64_t)n);
+  for (int k = 0; k < n; ++k) counters[k] = c + k;
   return desc_.ptr;
 }
 
@@ -452,14 +454,19 @@ static void sort_used_rules(Context &ctx, PairTable tab, uint64_t U, uint32_t by
   ctx.reset_status();
   bool in_tmp = false;
   GFZ_TIMED(ctx, "radix_sort", launch_sort_hist(su.keys.ptr, U, byte_mask, su.hist.ptr, st));
+  // the look-back regions of all passes, cleared at once
+  const int passes = __builtin_popcount(byte_mask);
+  const uint64_t region = sort_tiles(U) * 256;
+  uint32_t *counters[8];
+  unsigned long long *desc = ctx.lookback_n(region, std::max(passes, 1), counters);
+  int pass = 0;
   for (int b = 0; b < 8; ++b) {
     if (!((byte_mask >> b) & 1u)) continue;
-    uint32_t *counter;
-    unsigned long long *desc = ctx.lookback(sort_tiles(U) * 256, &counter);
     GFZ_TIMED(ctx, "radix_sort",
               launch_sort_pass(in_tmp ? su.keys_tmp.ptr : su.keys.ptr, in_tmp ? su.slots_tmp.ptr : su.slots.ptr,
                                in_tmp ? su.keys.ptr : su.keys_tmp.ptr, in_tmp ? su.slots.ptr : su.slots_tmp.ptr, U, b,
-                               su.hist.ptr, desc, counter, &ds->err, st));
+                               su.hist.ptr, desc + region * pass, counters[pass], &ds->err, st));
+    ++pass;
     in_tmp = !in_tmp;
   }
   rules.reserve(nrules + U, true);
@@ -597,14 +604,17 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
       sref.resize(n);
       d_sref = sref.ptr;
     }
-    // the table cleared for a count, with its repeated-slot bitmap
+    // the table cleared for a count, with its repeated-slot bitmap and the
+    // replacement's used-slot bitmap (one launch)
     auto prepare = [&](uint64_t c) {
-      tab.prepare(c, st);
+      tab.slots.resize(c);
+      used_bits.resize((c + 31) / 32);
       if (use_sref) {
         rep_bits.resize((c + 31) / 32);
-        ctx.zero(rep_bits.ptr, (c + 31) / 32 * sizeof(uint32_t));
         d_rep = rep_bits.ptr;
       }
+      launch_table_clear(tab.view(c), 0, st, use_sref ? rep_bits.ptr : nullptr, used_bits.ptr);
+      ctx.count_launch();
     };
     for (;;) {
       if (cap > kMaxTableCap) throw std::runtime_error("pair table would exceed 2^31 slots");
@@ -704,8 +714,6 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
     const int32_t temp_base = (int32_t)next_id;
     ctx.reset_status();
     ctx.upload(&ds->u64[5], &kAllOnes, sizeof(kAllOnes));
-    used_bits.resize((cap + 31) / 32);
-    ctx.zero(used_bits.ptr, (cap + 31) / 32 * sizeof(uint32_t));
     // slot references hold slots below 2^30 (bit 31 and one value are
     // taken); a larger table is classified and emitted by probing
     const bool by_sref = use_sref && cap <= kSrefMaxCap;

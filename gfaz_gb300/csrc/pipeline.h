@@ -114,6 +114,9 @@ class Context {
 
   // Zeroed look-back descriptors (n tiles) + tile counter.
   unsigned long long *lookback(uint64_t tiles, uint32_t **counter);
+  // n zeroed regions of `tiles` descriptors (region k at the result +
+  // k * tiles) and their n tile counters, cleared by one launch.
+  unsigned long long *lookback_n(uint64_t tiles, int n, uint32_t **counters);
 
   // Transfers between host memory and this context's device buffers, moved
   // by kernels rather than by copy engines: a copy engine serves its
@@ -216,7 +219,6 @@ class Context {
   std::vector<PendingDownload> downloads_;
   char *stage(size_t bytes);
   DevVec<unsigned long long> desc_;
-  DevVec<uint32_t> counter_;
   struct Pending {
     std::string name;
     cudaEvent_t a, b;
