@@ -14,6 +14,34 @@
 
 namespace gfz {
 
+// Powers of ten 10^0 .. 10^9 (a device copy for kernels, read through the
+// read-only cache, and a host copy).
+#if defined(__CUDACC__)
+static __device__ const uint32_t g_pow10[10] = {1u, 10u, 100u, 1000u, 10000u, 100000u, 1000000u, 10000000u,
+                                                100000000u, 1000000000u};
+#endif
+static const uint32_t g_pow10_host[10] = {1u, 10u, 100u, 1000u, 10000u, 100000u, 1000000u, 10000000u,
+                                          100000000u, 1000000000u};
+
+// Decimal digits of v (1 for 0): t = floor(bits(w) * log10(2)), with
+// 1233 / 4096 for log10(2) (exact on 1..32 bits), is the digit count of
+// w = v | 1 or one less, and one comparison with 10^t decides (setting the
+// low bit moves no value across a power of ten above 1, and makes 0 count
+// as one digit).
+GFZ_HD uint32_t dec_count(uint32_t v) {
+  const uint32_t w = v | 1u;
+#if defined(__CUDA_ARCH__)
+  const uint32_t bits = 32u - (uint32_t)__clz(w);
+  const uint32_t t = (bits * 1233u) >> 12;
+  const uint32_t p = __ldg(&g_pow10[t]);
+#else
+  const uint32_t bits = 32u - (uint32_t)__builtin_clz(w);
+  const uint32_t t = (bits * 1233u) >> 12;
+  const uint32_t p = g_pow10_host[t];
+#endif
+  return t + 1u - (w < p ? 1u : 0u);
+}
+
 // The 8 decimal digits of v < 10^8 as byte values 0..9, the most
 // significant digit in the lowest byte (the order they are written in).
 //   x / 100 = (x * 5243) >> 19   exact for x < 43699

@@ -540,7 +540,12 @@ __global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSou
   }
   if (total <= kTextBuf) {
     const uint32_t nw = (uint32_t)(total / 4) + 2;
-    for (uint32_t k = threadIdx.x; k < nw; k += BLOCK) sbuf[k] = 0;
+    // only words that receive OR-ed bytes need clearing: a word two threads
+    // share holds a thread's first byte past the word's start (that thread
+    // clears it), and the tile's last, partial word (the last thread clears
+    // it); every other word is stored whole by one thread
+    if (my & 3u) sbuf[(uint32_t)my >> 2] = 0;
+    if (threadIdx.x == BLOCK - 1) sbuf[(uint32_t)total >> 2] = 0;
     __syncthreads();
     WordWriter wr;
     wr.init(sbuf, (uint32_t)my, nw);

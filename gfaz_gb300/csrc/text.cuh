@@ -10,19 +10,7 @@
 
 namespace gfz {
 
-__device__ __forceinline__ uint32_t dec_digits(uint32_t v) {
-  uint32_t d = 1;
-  d += v >= 10u;
-  d += v >= 100u;
-  d += v >= 1000u;
-  d += v >= 10000u;
-  d += v >= 100000u;
-  d += v >= 1000000u;
-  d += v >= 10000000u;
-  d += v >= 100000000u;
-  d += v >= 1000000000u;
-  return d;
-}
+__device__ __forceinline__ uint32_t dec_digits(uint32_t v) { return dec_count(v); }
 
 __device__ __forceinline__ void put_dec(char *dst, uint32_t v, uint32_t nd) {
   for (uint32_t i = nd; i-- > 0;) {

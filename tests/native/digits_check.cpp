@@ -1,5 +1,7 @@
 // Checks gfz::digits8 / gfz::ascii_digits against plain division for every
-// value below 10^8 (or below argv[1]).  Exit status 0 when all agree.
+// value below 10^8 (or below argv[1]), and gfz::dec_count against
+// comparisons with the powers of ten for every 32-bit value.  Exit status 0
+// when all agree.
 #include <cstdio>
 #include <cstdlib>
 
@@ -31,6 +33,15 @@ int main(int argc, char **argv) {
           return 1;
         }
       }
+    }
+  }
+  for (uint64_t v = 0; v <= 0xFFFFFFFFull; ++v) {
+    const uint32_t x = (uint32_t)v;
+    uint32_t want = 1;
+    for (uint64_t p = 10; p <= x; p *= 10) ++want;
+    if (gfz::dec_count(x) != want) {
+      std::printf("dec_count mismatch at %u\n", x);
+      return 1;
     }
   }
   std::printf("ok %u\n", n);
