@@ -30,9 +30,10 @@ inline unsigned grid_for(uint64_t n, int block, unsigned cap = 152u * 16u) {
 // Rule lengths
 // ---------------------------------------------------------------------------
 __global__ void k_rule_len_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
-                                uint64_t nrules, uint32_t min_id, uint32_t *rlen, DevStatus *status, int slot) {
+                                uint64_t nrules, uint32_t min_id, uint32_t *rlen, DevStatus *status, int slot,
+                                uint64_t lo, uint64_t hi) {
   uint32_t open = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nrules;
+  for (uint64_t i = lo + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < hi;
        i += (uint64_t)gridDim.x * blockDim.x) {
     if (rlen[i]) continue;
     const uint32_t a = abs32(first[i]), b = abs32(second[i]);
@@ -342,9 +343,11 @@ constexpr int kDeltaItems = 16;
 constexpr int kTextItems = 8;
 
 void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
-                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st) {
-  if (!nrules) return;
-  k_rule_len_pass<<<grid_for(nrules, kBlock), kBlock, 0, st>>>(first, second, nrules, min_id, rlen, status, slot);
+                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st, uint64_t lo, uint64_t hi) {
+  hi = std::min(hi, nrules);
+  if (lo >= hi) return;
+  k_rule_len_pass<<<grid_for(hi - lo, kBlock), kBlock, 0, st>>>(first, second, nrules, min_id, rlen, status, slot,
+                                                                 lo, hi);
 }
 
 uint64_t scan_num_tiles(uint64_t n) {

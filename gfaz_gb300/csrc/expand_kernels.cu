@@ -77,20 +77,22 @@ constexpr uint32_t kWarpRule = 16;  // rules longer than this are written by a w
 
 __global__ void k_rule_prefix_pass(const int32_t *__restrict__ first, const int32_t *__restrict__ second,
                                    RulePrefixView rv, int32_t *rpre, int4 *rstat, int delta, uint32_t *built,
-                                   uint32_t pass, DevStatus *status, int slot) {
+                                   uint32_t pass, DevStatus *status, int slot, uint64_t lo, uint64_t hi) {
   __shared__ uint32_t s_open;
   if (threadIdx.x == 0) s_open = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   uint32_t open = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  // whole warps walk the rules together so that long rules can be shared
-  const uint64_t span = (rv.nrules + 31) & ~31ull;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < span; i += stride) {
+  // whole warps walk the rules [lo, hi) together so that long rules can be
+  // shared
+  const uint64_t span = (hi - lo + 31) & ~31ull;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < span; j += stride) {
+    const uint64_t i = lo + j;
     bool ready = false;
     int32_t f = 0, g = 0;
     uint32_t lf = 0, lg = 0;
-    if (i < rv.nrules && !built[i]) {
+    if (i < hi && !built[i]) {
       f = first[i];
       g = second[i];
       const uint32_t af = abs32(f), ag = abs32(g);
@@ -677,10 +679,12 @@ uint64_t excl_scan_tiles(uint64_t n) {
 
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
                              int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status, int slot,
-                             cudaStream_t st) {
-  if (!rv.nrules) return;
-  k_rule_prefix_pass<<<grid_for(rv.nrules, kBlock, 152u * 32u), kBlock, 0, st>>>(first, second, rv, rpre, rstat,
-                                                                                 delta, built, pass, status, slot);
+                             cudaStream_t st, uint64_t lo, uint64_t hi) {
+  hi = std::min(hi, rv.nrules);
+  if (lo >= hi) return;
+  k_rule_prefix_pass<<<grid_for(hi - lo, kBlock, 152u * 32u), kBlock, 0, st>>>(first, second, rv, rpre, rstat,
+                                                                               delta, built, pass, status, slot, lo,
+                                                                               hi);
 }
 
 void launch_excl_scan_u32(const uint32_t *in, uint64_t n, uint64_t *out, unsigned long long *desc,

@@ -182,10 +182,11 @@ void launch_stack_encode(int32_t *s, const uint64_t *off, uint64_t *len, uint64_
 
 // ---- decode side ------------------------------------------------------------
 // Rule expansion lengths: len[i] for rule min_id + i.  One pass resolves the
-// rules whose children are resolved; status->pass_open[slot] counts rules
-// still open.
+// rules of [lo, hi) (all by default) whose children are resolved;
+// status->pass_open[slot] counts rules still open.
 void launch_rule_len_pass(const int32_t *first, const int32_t *second, uint64_t nrules, uint32_t min_id,
-                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st);
+                          uint32_t *rlen, DevStatus *status, int slot, cudaStream_t st,
+                          uint64_t lo = 0, uint64_t hi = UINT64_MAX);
 // Exclusive scan of the expansion length of every encoded symbol into
 // pos[0..m] (pos[m] = total); desc/tile_counter zeroed.
 void launch_symbol_positions(const int32_t *enc, uint64_t m, uint32_t min_id, uint64_t nrules,
@@ -265,12 +266,12 @@ struct TextSource {
   uint64_t cap;   // bytes of the text buffer
   uint32_t *err;  // kErrLength when the text would not fit where its lengths say
 };
-// One build pass over the rule prefix buffer; built[r] = pass of rule r (0 =
-// waiting, zero before pass 1).  status->pass_open[slot] += rules still
-// waiting.
+// One build pass over the rule prefix buffer for the rules of [lo, hi) (all
+// by default); built[r] = pass of rule r (0 = waiting, zero before pass 1).
+// status->pass_open[slot] += rules still waiting.
 void launch_rule_prefix_pass(const int32_t *first, const int32_t *second, RulePrefixView rv, int32_t *rpre,
                              int4 *rstat, int delta, uint32_t *built, uint32_t pass, DevStatus *status, int slot,
-                             cudaStream_t st);
+                             cudaStream_t st, uint64_t lo = 0, uint64_t hi = UINT64_MAX);
 // out[0 .. n] = exclusive scan of in[0 .. n) (out[n] = total); desc: one u64
 // per excl_scan_tiles(n) tile (at least one), zeroed; tile_counter zeroed.
 uint64_t excl_scan_tiles(uint64_t n);

@@ -750,6 +750,7 @@ static void run_rounds(Context &ctx, DevVec<int32_t> &A, DevVec<int32_t> &B, Dev
               (unsigned long long)repeated, (unsigned long long)U, (unsigned long long)n_out,
               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - round_t0).count());
     g.nrules += U;
+    g.round_end.push_back(g.nrules);
     next_id += (uint32_t)U;
     n = n_out;
     A.swap(B);
@@ -780,6 +781,7 @@ void encode_traversals(Context &ctx, const int32_t *d_steps, const std::vector<u
   g.delta_round = dr;
   g.rounds_done = 0;
   g.nrules = 0;
+  g.round_end.clear();
 
   DevVec<uint64_t> offA(st), offB(st);
   offA.resize(ntrav + 1);
@@ -875,6 +877,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
   g.delta_round = dr;
   g.rounds_done = 0;
   g.nrules = 0;
+  g.round_end.clear();
 
   DevVec<uint64_t> offA(st), offB(st);
   offA.resize(ntrav + 1);
@@ -1207,6 +1210,7 @@ void encode_host_chunked(Context &ctx, const std::vector<HostSeg> &input, const 
               (unsigned long long)cap,
               (unsigned long long)distinct, (unsigned long long)U, (unsigned long long)n_out);
     g.nrules += U;
+    g.round_end.push_back(g.nrules);
     next_id += (uint32_t)U;
     n = n_out;
     phase("round");
@@ -1359,6 +1363,9 @@ void load_encoded(Context &ctx, Grammar &g, const int32_t *enc, const std::vecto
   if (m) ctx.upload(g.enc.ptr, enc, m * 4);
 }
 
+// The grammar's rules are known round by round (see Grammar::round_end).
+static bool layered(const Grammar &g) { return !g.round_end.empty() && g.round_end.back() == g.nrules; }
+
 static void ensure_rule_lengths(Context &ctx, Grammar &g) {
   if (g.rlen_ready) return;
   cudaStream_t st = ctx.stream();
@@ -1375,10 +1382,25 @@ static void ensure_rule_lengths(Context &ctx, Grammar &g) {
                 (k_split_rules<<<grid_for(R, 256), 256, 0, st>>>(g.rules.ptr, R, g.first.ptr, g.second.ptr)));
     }
     ctx.zero(g.rlen.ptr, R * sizeof(uint32_t));
+    bool done = false;
+    if (layered(g)) {
+      // one launch per grammar round over that round's rules: their parts
+      // are steps or rules of earlier rounds, whose lengths are known by then
+      ctx.reset_status();
+      uint64_t lo = 0;
+      for (const uint64_t hi : g.round_end) {
+        GFZ_TIMED(ctx, "rule_len", launch_rule_len_pass(g.first.ptr, g.second.ptr, R, g.layer_start, g.rlen.ptr,
+                                                        ctx.dstatus(), 0, st, lo, hi));
+        lo = hi;
+      }
+      const DevStatus &s = ctx.read_status();
+      ctx.check_status("rule lengths");
+      done = s.pass_open[0] == 0;  // else the level passes below finish the job
+    }
     // level passes in batches, one status read per batch (extra passes
     // after the last level find nothing to do)
     uint64_t prev_open = UINT64_MAX;
-    for (;;) {
+    while (!done) {
       ctx.reset_status();
       for (int k = 0; k < kPassBatch; ++k)
         GFZ_TIMED(ctx, "rule_len", launch_rule_len_pass(g.first.ptr, g.second.ptr, R, g.layer_start, g.rlen.ptr,
@@ -1426,8 +1448,27 @@ static bool ensure_rule_prefix(Context &ctx, Grammar &g) {
     built.resize(R);
     ctx.zero(built.ptr, R * sizeof(uint32_t));
     const RulePrefixView rv{g.rlen.ptr, g.roff.ptr, g.rpre.ptr, g.rstat.ptr, g.layer_start, R};
+    uint32_t first_pass = 1;
+    bool done = false;
+    if (layered(g)) {
+      // one launch per grammar round over that round's rules (their parts'
+      // buffers were built by the earlier launches)
+      ctx.reset_status();
+      uint64_t lo = 0;
+      for (const uint64_t hi : g.round_end) {
+        GFZ_TIMED_B(ctx, "rule_prefix", 0,
+                    launch_rule_prefix_pass(g.first.ptr, g.second.ptr, rv, g.rpre.ptr, g.rstat.ptr,
+                                            g.delta_round == 1 ? 1 : 0, built.ptr, first_pass, ctx.dstatus(), 0, st,
+                                            lo, hi));
+        lo = hi;
+        ++first_pass;
+      }
+      const DevStatus &s = ctx.read_status();
+      ctx.check_status("rule prefix");
+      done = s.pass_open[0] == 0;  // else the level passes below finish the job
+    }
     uint64_t prev_open = UINT64_MAX;
-    for (uint32_t pass = 1;; pass += kPassBatch) {
+    for (uint32_t pass = first_pass; !done; pass += kPassBatch) {
       ctx.reset_status();
       for (int k = 0; k < kPassBatch; ++k)
         GFZ_TIMED_B(ctx, "rule_prefix", 0,

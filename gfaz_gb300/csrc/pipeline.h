@@ -255,6 +255,10 @@ struct Grammar {
   DevVec<int32_t> rpre;        // inclusive prefix sums of every rule's expansion
   DevVec<int4> rstat;          // per-rule value ranges (text lengths)
   uint64_t nrules = 0;
+  // rules made by each grammar round: round r's are [round_end[r - 1],
+  // round_end[r]) and use only earlier rounds' (known for a grammar this
+  // library compressed; empty for a loaded one)
+  std::vector<uint64_t> round_end;
   uint32_t layer_start = 0, next_id = 0;
   int delta_round = 1;
   int rounds_done = 0;
