@@ -668,14 +668,25 @@ __device__ __forceinline__ ParAgg block_par_scan(const ParAgg &a, ParAgg &total,
   if (lane == 0) excl = par_identity();
   if (lane == 31) s_warp[warp] = inc;
   __syncthreads();
-  ParAgg wpre = par_identity(), tot = par_identity();
+  // the warps' exclusive prefixes and the total, scanned by warp 0 alone
+  // (rather than every thread composing all warp aggregates in turn)
+  static_assert(NW <= 32, "one lane per warp aggregate");
+  __shared__ ParAgg s_pre[NW + 1];
+  if (warp == 0) {
+    ParAgg v = lane < NW ? s_warp[lane] : par_identity();
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    if (w == warp) wpre = tot;
-    tot = par_compose(tot, s_warp[w]);
+    for (int d = 1; d < NW; d <<= 1) {
+      const ParAgg o = par_shfl_up(v, d);
+      if (lane >= d) v = par_compose(o, v);
+    }
+    ParAgg e = par_shfl_up(v, 1);
+    if (lane == 0) e = par_identity();
+    if (lane < NW) s_pre[lane] = e;
+    if (lane == NW - 1) s_pre[NW] = v;
   }
-  total = tot;
-  return par_compose(wpre, excl);
+  __syncthreads();
+  total = s_pre[NW];
+  return par_compose(s_pre[warp], excl);
 }
 
 template <int BLOCK, int ITEMS>
