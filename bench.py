@@ -177,21 +177,30 @@ def run_cpu_port(steps, off, sample_paths, threads, grammar=False):
             r[3] if grammar else None)
 
 
-def _cpu_leg_child(base, sample_paths, threads, q):
-    """Spawned child of run_cpu_port_isolated: the port's timed pass on the
-    steps saved at base, its grammar saved beside them."""
+def _cpu_leg_child(base, sample_paths, threads, q, passes, warmup_paths, grammar):
+    """Spawned child of run_cpu_port_isolated: an untimed pass on the first
+    warmup_paths traversals (when any), then `passes` timed passes on the
+    steps saved at base; the last pass's grammar saved beside them."""
     steps = np.load(base + ".steps.npy")
     off = np.load(base + ".off.npy")
-    v, dt, nb, sample, gram = run_cpu_port(steps, off, sample_paths, threads, grammar=True)
-    np.savez(base + ".gram.npz", enc=gram[0], off=gram[1], rules=gram[2])
-    q.put((v, dt, nb, sample, len(os.sched_getaffinity(0))))
+    if warmup_paths:
+        run_cpu_port(steps, off, warmup_paths, threads)
+    res = []
+    for k in range(passes):
+        last = grammar and k == passes - 1
+        v, dt, nb, sample, gram = run_cpu_port(steps, off, sample_paths, threads, grammar=last)
+        if last:
+            np.savez(base + ".gram.npz", enc=gram[0], off=gram[1], rules=gram[2])
+        res.append((v, dt, nb, sample))
+    q.put((res, len(os.sched_getaffinity(0))))
 
 
-def run_cpu_port_isolated(steps, off, sample_paths, threads):
-    """run_cpu_port (with the grammar) in a freshly spawned process, so that
-    the port's OpenMP threads start from a clean process: inside the bench
-    process, after the CUDA work, the same pass ran about 5x slower.
-    Returns (GB/s, seconds, text bytes, sample, cpus usable, grammar)."""
+def run_cpu_port_isolated(steps, off, sample_paths, threads, passes=1, warmup_paths=0, grammar=True):
+    """run_cpu_port in a freshly spawned process, so that the port's OpenMP
+    threads start from a clean process: inside the bench process (after its
+    CUDA work, or after the workload generator's numpy calls) the same pass
+    ran up to 5x slower.  Returns ([(GB/s, seconds, text bytes, sample) per
+    pass], cpus usable, grammar of the last pass or None)."""
     import multiprocessing as mp
     import tempfile
     with tempfile.TemporaryDirectory() as td:
@@ -200,13 +209,16 @@ def run_cpu_port_isolated(steps, off, sample_paths, threads):
         np.save(base + ".off.npy", off)
         mpc = mp.get_context("spawn")
         q = mpc.Queue()
-        p = mpc.Process(target=_cpu_leg_child, args=(base, sample_paths, threads, q))
+        p = mpc.Process(target=_cpu_leg_child,
+                        args=(base, sample_paths, threads, q, passes, warmup_paths, grammar))
         p.start()
-        res = q.get()
+        res, usable = q.get()
         p.join()
-        z = np.load(base + ".gram.npz")
-        gram = (z["enc"], z["off"], z["rules"])
-    return res + (gram,)
+        gram = None
+        if grammar:
+            z = np.load(base + ".gram.npz")
+            gram = (z["enc"], z["off"], z["rules"])
+    return res, usable, gram
 
 
 def calibration():
@@ -363,16 +375,13 @@ def reference_arm(args):
         return 0
     steps, off, _ = workload(args.scale)
     threads = os.cpu_count() or 1
-    # warm-up steps page the port's code and buffers in on a 12-line sample
-    # (untimed); every timed step is the whole workload
-    for _ in range(args.warmup):
-        run_cpu_port(steps, off, min(12, args.cpu_sample_paths), threads)
-    vals, secs = [], []
-    nbytes, sample = 0, ""
-    for _ in range(args.steps):
-        v, dt, nbytes, sample, _ = run_cpu_port(steps, off, args.cpu_sample_paths, threads)
-        vals.append(v)
-        secs.append(dt)
+    # in one spawned process: warm-up passes page the port's code and buffers
+    # in on a 12-line sample (untimed); every timed step is the whole workload
+    warm = min(12, args.cpu_sample_paths) if args.warmup else 0
+    res, usable, _ = run_cpu_port_isolated(steps, off, args.cpu_sample_paths, threads, passes=args.steps,
+                                           warmup_paths=warm, grammar=False)
+    secs = [r[1] for r in res]
+    nbytes, sample = res[-1][2], res[-1][3]
     value = nbytes * len(secs) / sum(secs) / 1e9
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
@@ -382,8 +391,9 @@ def reference_arm(args):
                                    % len(steps),
                       "rounds": 8, "delta_round": 1, "threshold": 2},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": sample + " per step; oracle/gfaz_oracle.c (OpenMP), reference CLI "
-                                               "not buildable on the GPU host",
+                            "sample": sample + f" per step, in a spawned process ({usable} CPUs usable); "
+                                               "oracle/gfaz_oracle.c (OpenMP), reference CLI not buildable on "
+                                               "the GPU host",
                             "calibration": calibration()},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -594,7 +604,8 @@ def main():
     grammar_ok = True
     if not args.no_cpu_baseline and rank == 0:
         threads = os.cpu_count() or 1
-        v, dt, nb, sample, usable, cpu_grammar = run_cpu_port_isolated(steps, off, args.cpu_sample_paths, threads)
+        res, usable, cpu_grammar = run_cpu_port_isolated(steps, off, args.cpu_sample_paths, threads)
+        v, dt, nb, sample = res[-1]
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{sample}, one compress+decompress transform pass in {dt:.2f} s in a spawned process "
                          f"({usable} CPUs usable; oracle/gfaz_oracle.c, OpenMP)", "calibration": calibration()}
