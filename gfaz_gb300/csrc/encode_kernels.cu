@@ -640,7 +640,54 @@ __device__ __forceinline__ void lookup_pairs(const int32_t (&v)[ITEMS + 1], uint
   }
 }
 
+__host__ __device__ constexpr uint32_t par_pack8(uint32_t cbits) {
+  uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t c = (cbits >> k) & 1u;
+    x0 = c & (x0 ^ 1u);
+    x1 = c & (x1 ^ 1u);
+    c0 += x0;
+    c1 += x1;
+  }
+  return x0 | (x1 << 1) | (c0 << 2) | (c1 << 6);
+}
+// The aggregate of every 8-position candidate pattern, packed as
+// x_out(0) | x_out(1) << 1 | c0 << 2 | c1 << 6 (1 KB, read through L1):
+// one load in place of the eight-step recurrence.
+struct Par8Table {
+  uint32_t v[256];
+  constexpr Par8Table() : v() {
+    for (uint32_t b = 0; b < 256; ++b) v[b] = par_pack8(b);
+  }
+};
+__device__ const Par8Table g_par8 = Par8Table();
+
+// The replay of eight positions from a carried-in x: index cbits | x_in << 8,
+// value xbits | keptbits << 8 (x_p = c_p & !x_{p-1}; a position is kept
+// unless its predecessor was replaced).
+__host__ __device__ constexpr uint32_t replay8(uint32_t idx) {
+  uint32_t x = idx >> 8, xbits = 0, kept = 0;
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t prev = x;
+    x = ((idx >> k) & 1u) & (prev ^ 1u);
+    kept |= (prev ^ 1u) << k;
+    xbits |= x << k;
+  }
+  return xbits | (kept << 8);
+}
+struct Replay8Table {
+  uint32_t v[512];
+  constexpr Replay8Table() : v() {
+    for (uint32_t i = 0; i < 512; ++i) v[i] = replay8(i);
+  }
+};
+__device__ const Replay8Table g_replay8 = Replay8Table();
+
 __device__ __forceinline__ ParAgg par_of_bits(uint32_t cbits, int items) {
+  if (items == 8) {
+    const uint32_t t = __ldg(&g_par8.v[cbits & 0xFFu]);
+    return ParAgg{t & 3u, (t >> 2) & 15u, (t >> 6) & 15u};
+  }
   uint32_t x0 = 0, x1 = 1, c0 = 0, c1 = 0;
   for (int k = 0; k < items; ++k) {
     const uint32_t c = (cbits >> k) & 1u;
@@ -894,7 +941,14 @@ __device__ __forceinline__ void emit_tile(const int32_t (&v)[ITEMS + 1], uint64_
   const uint32_t x_init = par_x(excl, in_x);
   const uint32_t c_init = par_c(excl, in_x);  // replaced positions in this tile before j0
   uint32_t keptbits = 0, xbits = 0;
-  {
+  if (ITEMS == 8) {
+    // the replay of all eight positions from one table load; positions past
+    // the stream's end (the tile's last thread) are masked off
+    const uint32_t t = __ldg(&g_replay8.v[cbits | (x_init << 8)]);
+    const uint32_t valid = j0 >= len ? 0u : (len - j0 >= 8u ? 0xFFu : (1u << (len - j0)) - 1u);
+    xbits = t & valid;
+    keptbits = (t >> 8) & valid;
+  } else {
     uint32_t x = x_init;
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
