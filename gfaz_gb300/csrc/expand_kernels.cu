@@ -231,11 +231,17 @@ __global__ void k_symbol_records(const int32_t *__restrict__ enc, uint64_t m, Ru
   }
 }
 
-// With inclusive segmented sums in incl: rec[i].w = incl[i] - rec[i].w, the
-// sum of the expansions before symbol i in its traversal.
+// With inclusive segmented sums in incl: rec[i].w = S_i = incl[i] -
+// rec[i].w, the sum of the expansions before symbol i in its traversal; for
+// a reversed rule (symbol < 0), S_i minus the rule's total, which is
+// incl[i] itself (its expansion sums to minus that total), so that its
+// steps need no gather of the total: step o is rec.w + the rule's prefix
+// at L - 2 - o (0 for the last step).
 __global__ void k_symbol_exclusive(int4 *rec, const int32_t *__restrict__ incl, uint64_t m) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
-    rec[i].w = (int32_t)((uint32_t)incl[i] - (uint32_t)rec[i].w);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int4 r = rec[i];
+    rec[i].w = (r.x < 0 && r.z != 0) ? incl[i] : (int32_t)((uint32_t)incl[i] - (uint32_t)r.w);
+  }
 }
 
 // tile_sym[k] = the symbol holding output step min(k * tile, total - 1):
@@ -289,16 +295,17 @@ __device__ __forceinline__ void stage_symbols(const ExpandSource &E, uint64_t ti
   __syncthreads();
 }
 
-// Step at offset o of a symbol with record r (prefix buffer rpre).
+// Step at offset o of a symbol with record r (prefix buffer rpre; with
+// DELTA, r.w as k_symbol_exclusive leaves it).
 template <int DELTA>
-__device__ __forceinline__ int32_t symbol_step(const int4 &r, uint32_t rtot, uint32_t o, const int32_t *__restrict__ rpre) {
+__device__ __forceinline__ int32_t symbol_step(const int4 &r, uint32_t o, const int32_t *__restrict__ rpre) {
   const int32_t v = r.x;
   const uint32_t b = (uint32_t)r.y, L = (uint32_t)r.z, s = (uint32_t)r.w;
   if (L == 0) return DELTA ? (int32_t)(s + (uint32_t)v) : v;
   if (DELTA) {
     if (v > 0) return (int32_t)(s + (uint32_t)rpre[b + o]);
     const uint32_t before = o + 1 < L ? (uint32_t)rpre[b + L - 2 - o] : 0u;
-    return (int32_t)(s - (rtot - before));
+    return (int32_t)(s + before);
   }
   const uint32_t q = v > 0 ? o : L - 1 - o;
   const uint32_t x = (uint32_t)rpre[b + q] - (q ? (uint32_t)rpre[b + q - 1] : 0u);
@@ -336,7 +343,6 @@ __device__ __forceinline__ uint32_t thread_values(const ExpandSource &E, const S
     end = E.pos[lo + 1];
     r = E.rec[lo];
   }
-  uint32_t rtot = (!DELTA || r.x >= 0 || r.z == 0) ? 0u : (uint32_t)E.rules.rpre[(uint32_t)r.y + (uint32_t)r.z - 1];
   uint32_t cnt = 0;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
@@ -352,9 +358,8 @@ __device__ __forceinline__ uint32_t thread_values(const ExpandSource &E, const S
           end = E.pos[i + 1];
           r = E.rec[i];
         }
-        if (DELTA && r.x < 0 && r.z != 0) rtot = (uint32_t)E.rules.rpre[(uint32_t)r.y + (uint32_t)r.z - 1];
       }
-      val[k] = symbol_step<DELTA>(r, rtot, (uint32_t)(p - start), E.rules.rpre);
+      val[k] = symbol_step<DELTA>(r, (uint32_t)(p - start), E.rules.rpre);
       cnt = k + 1;
     }
   }
@@ -407,18 +412,17 @@ __device__ __forceinline__ uint32_t uniform_digits(long long lo, long long hi) {
   return a == b ? a : 0u;
 }
 
-// The digit count all steps of symbol r share (0 if they differ); rtot is
-// the rule total when r is a reversed rule (delta 1).
+// The digit count all steps of symbol r share (0 if they differ).
 template <int DELTA>
-__device__ __forceinline__ uint32_t symbol_digits(const int4 &r, uint32_t rtot, const RulePrefixView &rv) {
+__device__ __forceinline__ uint32_t symbol_digits(const int4 &r, const RulePrefixView &rv) {
   const int32_t v = r.x;
   const uint32_t L = (uint32_t)r.z;
   if (L == 0) return dec_digits(abs32(DELTA ? (int32_t)((uint32_t)r.w + (uint32_t)v) : v));
   const int4 st = rv.rstat[abs32(v) - rv.min_id];
   if (DELTA) {
     if (v > 0) return uniform_digits((long long)r.w + st.x, (long long)r.w + st.y);
-    const long long base = (long long)r.w - (long long)(int32_t)rtot;
-    return uniform_digits(base + st.z, base + st.w);
+    // a reversed rule's steps are r.w + {0, its prefix values but the last}
+    return uniform_digits((long long)r.w + st.z, (long long)r.w + st.w);
   }
   return v > 0 ? uniform_digits(st.x, st.y) : uniform_digits(-(long long)st.y, -(long long)st.x);
 }
@@ -426,22 +430,17 @@ __device__ __forceinline__ uint32_t symbol_digits(const int4 &r, uint32_t rtot, 
 // Text bytes of steps [from, to) of symbol r (none of them the last step of
 // its traversal): digits plus the orientation mark and, in P lines, a comma.
 template <int DELTA>
-__device__ __forceinline__ unsigned long long steps_text(const int4 &r, uint32_t rtot, uint32_t dig, uint32_t from,
-                                                         uint32_t to, bool pmode, const int32_t *__restrict__ rpre) {
+__device__ __forceinline__ unsigned long long steps_text(const int4 &r, uint32_t dig, uint32_t from, uint32_t to,
+                                                         bool pmode, const int32_t *__restrict__ rpre) {
   const uint32_t per = pmode ? 2u : 1u;
   if (dig) return (unsigned long long)(to - from) * (dig + per);
   unsigned long long len = 0;
-  for (uint32_t o = from; o < to; ++o) len += dec_digits(abs32(symbol_step<DELTA>(r, rtot, o, rpre))) + per;
+  for (uint32_t o = from; o < to; ++o) len += dec_digits(abs32(symbol_step<DELTA>(r, o, rpre))) + per;
   return len;
 }
 
 __device__ __forceinline__ uint64_t pre_len(const TextSource &T, uint64_t t) { return T.meta.pre_off[t + 1] - T.meta.pre_off[t]; }
 __device__ __forceinline__ uint64_t suf_len(const TextSource &T, uint64_t t) { return T.meta.suf_off[t + 1] - T.meta.suf_off[t]; }
-
-template <int DELTA>
-__device__ __forceinline__ uint32_t reversed_total(const int4 &r, const int32_t *__restrict__ rpre) {
-  return (DELTA && r.x < 0 && r.z != 0) ? (uint32_t)rpre[(uint32_t)r.y + (uint32_t)r.z - 1] : 0u;
-}
 
 // slen[i]: the line prefix (first symbol of a traversal), the steps, and the
 // line suffix (last symbol); sdig[i]: the shared digit count or 0.
@@ -451,9 +450,8 @@ __global__ void k_symbol_text(ExpandSource E, TextSource T, uint64_t *slen, uint
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E.m; i += (uint64_t)gridDim.x * blockDim.x) {
     const int4 r = E.rec[i];
     const uint64_t start = E.pos[i], end = E.pos[i + 1];
-    const uint32_t rtot = reversed_total<DELTA>(r, E.rules.rpre);
-    const uint32_t dig = symbol_digits<DELTA>(r, rtot, E.rules);
-    unsigned long long len = steps_text<DELTA>(r, rtot, dig, 0, (uint32_t)(end - start), pmode, E.rules.rpre);
+    const uint32_t dig = symbol_digits<DELTA>(r, E.rules);
+    unsigned long long len = steps_text<DELTA>(r, dig, 0, (uint32_t)(end - start), pmode, E.rules.rpre);
     const bool fst = head_at(T.heads, start), lst = head_at(T.heads, end);
     if (fst | lst) {
       const uint64_t t = trav_of(T.off, T.ntrav, start);
@@ -475,8 +473,7 @@ __device__ __forceinline__ unsigned long long step_offset(const ExpandSource &E,
   unsigned long long o = soff[i];
   if (p == start) return o;
   if (head_at(T.heads, start)) o += pre_len(T, trav_of(T.off, T.ntrav, start));
-  const uint32_t rtot = reversed_total<DELTA>(r, E.rules.rpre);
-  return o + steps_text<DELTA>(r, rtot, sdig[i], 0, (uint32_t)(p - start), pmode, E.rules.rpre);
+  return o + steps_text<DELTA>(r, sdig[i], 0, (uint32_t)(p - start), pmode, E.rules.rpre);
 }
 
 // Text offset of the first step of every output tile: where the tile's
