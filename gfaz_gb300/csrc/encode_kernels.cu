@@ -1292,24 +1292,23 @@ __global__ void __launch_bounds__(kBlock) k_sort_pass(const unsigned long long *
                                                       uint32_t *counter, uint32_t *err) {
   static_assert(kBlock == 256, "one thread per digit");
   constexpr int NW = kBlock / 32;
+  constexpr uint32_t kWarpKeys = 32 * kSortItems;
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t wcnt[NW][256];
-  __shared__ uint32_t running[256];
+  __shared__ uint32_t wcnt[NW][256];  // a warp's digit counts, then its offset within the tile
   __shared__ unsigned long long base[256];
   if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
-  running[threadIdx.x] = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = lane; k < 256; k += 32) wcnt[warp][k] = 0;
   __syncthreads();
   const uint64_t tile = s_tile;
-  const uint64_t b0 = tile * kSortTile;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // warp w ranks the tile's keys [w * kWarpKeys, (w + 1) * kWarpKeys) in
+  // order, with counters of its own: no block barrier per key
+  const uint64_t w0 = tile * kSortTile + (uint64_t)warp * kWarpKeys;
   unsigned long long key[kSortItems];
   uint32_t val[kSortItems], rank[kSortItems], dig[kSortItems];
 #pragma unroll
   for (int it = 0; it < kSortItems; ++it) {
-#pragma unroll
-    for (int w = 0; w < NW; ++w) wcnt[w][threadIdx.x] = 0;
-    __syncthreads();
-    const uint64_t i = b0 + (uint64_t)it * kBlock + threadIdx.x;
+    const uint64_t i = w0 + (uint64_t)it * 32 + lane;
     const bool valid = i < n;
     key[it] = 0;
     val[it] = 0;
@@ -1321,23 +1320,29 @@ __global__ void __launch_bounds__(kBlock) k_sort_pass(const unsigned long long *
     }
     const uint32_t m = __match_any_sync(0xffffffffu, dig[it]);
     const uint32_t lrank = __popc(m & lanemask_lt());
-    if (valid && lrank == 0) wcnt[warp][dig[it]] = __popc(m);
-    __syncthreads();
-    if (valid) {
-      uint32_t pre = 0;
-      for (int w = 0; w < warp; ++w) pre += wcnt[w][dig[it]];
-      rank[it] = running[dig[it]] + pre + lrank;
-    }
-    __syncthreads();
-    uint32_t add = 0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) add += wcnt[w][threadIdx.x];
-    running[threadIdx.x] += add;
+    const uint32_t before = valid ? wcnt[warp][dig[it]] : 0u;
+    __syncwarp();
+    if (valid && lrank == 0) wcnt[warp][dig[it]] = before + __popc(m);
+    __syncwarp();
+    rank[it] = before + lrank;
   }
-  (void)lane;
-  // digit d: count in this tile, keys of digit d in earlier tiles, base
+  __syncthreads();
+  // digit d: each warp's offset within the tile (exclusive over the warps)
+  // and the tile's count
   const uint32_t d = threadIdx.x;
-  const unsigned long long cnt_d = running[d];
+  uint32_t run = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const uint32_t c = wcnt[w][d];
+    wcnt[w][d] = run;
+    run += c;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it)
+    if (dig[it] < 256) rank[it] += wcnt[warp][dig[it]];
+  // digit d: count in this tile, keys of digit d in earlier tiles, base
+  const unsigned long long cnt_d = run;
   unsigned long long excl = 0;
   if (tile == 0) {
     st_desc(&desc[d], kDescIncl | cnt_d);
