@@ -558,6 +558,28 @@ __global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSou
     __syncthreads();
     WordWriter wr;
     wr.init(sbuf, (uint32_t)my, nw);
+    if (pmode && !edges) {
+      // the common case: P-line steps with no line start or end among them,
+      // every one digits, mark and comma
+#pragma unroll 1
+      for (int k = 0; k < ITEMS; ++k) {
+        if ((uint32_t)k < cnt) {
+          const int32_t v = val[k];
+          const uint32_t av = abs32(v), nd = (ndp >> (4 * k)) & 15u;
+          const uint32_t tail = (v < 0 ? '-' : '+') | ((uint32_t)',' << 8);
+          if (nd <= 8) {
+            const unsigned long long D = ascii_digits(av, nd);
+            const uint32_t sh = 8u * nd;
+            const unsigned long long s0 = sh < 64 ? D | ((unsigned long long)tail << sh) : D;
+            const uint32_t s1 = sh > 48 ? (uint32_t)((unsigned long long)tail >> (64u - sh)) : 0u;
+            wr.put12(s0, s1, nd + 2u);
+          } else {
+            wr.put_dec(av, nd);
+            wr.put(tail, 2);
+          }
+        }
+      }
+    } else {
 #pragma unroll 1  // a rolled loop keeps the kernel inside the instruction cache
     for (int k = 0; k < ITEMS; ++k) {
       if ((uint32_t)k < cnt) {
@@ -597,6 +619,7 @@ __global__ void __launch_bounds__(BLOCK, 7) k_text_write(ExpandSource E, TextSou
         if (lst)
           for (uint64_t q = T.meta.suf_off[t]; q < T.meta.suf_off[t + 1]; ++q) wr.put((uint8_t)T.meta.blob[q], 1);
       }
+    }
     }
     wr.finish();
     if (wr.overflow) atomicOr(T.err, kErrLength);
