@@ -185,9 +185,14 @@ __device__ __forceinline__ typename Op::S warp_lookback(unsigned long long *desc
 }
 
 // Block-wide exclusive sum of a u64 per thread; also returns the total.
+// The warps' sums are scanned by warp 0 alone (every thread used to add
+// them all up in turn).
 template <int BLOCK>
 __device__ __forceinline__ unsigned long long block_excl_sum(unsigned long long v, unsigned long long &total) {
-  __shared__ unsigned long long s_w[BLOCK / 32];
+  constexpr int NW = BLOCK / 32;
+  static_assert(NW >= 1 && NW <= 32, "one lane per warp sum");
+  __shared__ unsigned long long s_w[NW];
+  __shared__ unsigned long long s_x[NW + 1];  // the warps' exclusive offsets, then the total
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long inc = v;
 #pragma unroll
@@ -197,15 +202,20 @@ __device__ __forceinline__ unsigned long long block_excl_sum(unsigned long long 
   }
   if (lane == 31) s_w[warp] = inc;
   __syncthreads();
-  unsigned long long pre = 0, tot = 0;
+  if (warp == 0) {
+    const unsigned long long w = lane < NW ? s_w[lane] : 0ull;
+    unsigned long long x = w;
 #pragma unroll
-  for (int w = 0; w < BLOCK / 32; ++w) {
-    if (w == warp) pre = tot;
-    tot += s_w[w];
+    for (int d = 1; d < NW; d <<= 1) {
+      const unsigned long long o = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += o;
+    }
+    if (lane < NW) s_x[lane] = x - w;
+    if (lane == NW - 1) s_x[NW] = x;
   }
-  total = tot;
   __syncthreads();
-  return pre + inc - v;
+  total = s_x[NW];
+  return s_x[warp] + inc - v;
 }
 
 // u64 running sum.
