@@ -284,8 +284,11 @@ __device__ __forceinline__ void stage_symbols(const ExpandSource &E, uint64_t ti
   const uint64_t cnt = hi - lo + 1;
   const bool staged = cnt <= kStageSyms;
   if (staged) {
-    for (uint32_t k = threadIdx.x; k <= cnt; k += BLOCK) S.pos[k] = E.pos[lo + k];
-    for (uint32_t k = threadIdx.x; k < cnt; k += BLOCK) S.rec[k] = E.rec[lo + k];
+    // evict-first loads: a tile's symbols are read by it (and its
+    // neighbour's edge) only, and L2 is better left to the prefix buffer
+    const unsigned long long *pos = reinterpret_cast<const unsigned long long *>(E.pos) + lo;
+    for (uint32_t k = threadIdx.x; k <= cnt; k += BLOCK) S.pos[k] = __ldcs(pos + k);
+    for (uint32_t k = threadIdx.x; k < cnt; k += BLOCK) S.rec[k] = __ldcs(E.rec + lo + k);
   }
   if (threadIdx.x == 0) {
     S.lo = lo;

@@ -51,7 +51,7 @@ __device__ __forceinline__ void block_copy_out(const char *sbuf, uint32_t len, c
       val = make_uint4(__funnelshift_r(a0, a1, sh), __funnelshift_r(a1, a2, sh), __funnelshift_r(a2, a3, sh),
                        __funnelshift_r(a3, a4, sh));
     }
-    *reinterpret_cast<uint4 *>(dst + o) = val;
+    __stcs(reinterpret_cast<uint4 *>(dst + o), val);  // evict-first: nothing here reads the text again
   }
   for (uint32_t i = head + 16u * body + threadIdx.x; i < len; i += BLOCK) dst[i] = sbuf[i];
 }
