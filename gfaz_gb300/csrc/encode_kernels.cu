@@ -222,7 +222,8 @@ __device__ __forceinline__ void store_srefs(uint32_t *dst, uint32_t cnt, uint32_
   }
   if (cnt == (uint32_t)K && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k += 4) *reinterpret_cast<uint4 *>(dst + k) = make_uint4(r[k], r[k + 1], r[k + 2], r[k + 3]);
+    for (int k = 0; k < K; k += 4)  // evict-first, as the table is what L2 should hold
+      __stcs(reinterpret_cast<uint4 *>(dst + k), make_uint4(r[k], r[k + 1], r[k + 2], r[k + 3]));
   } else {
 #pragma unroll
     for (int k = 0; k < K; ++k)
@@ -427,7 +428,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_count_flat4(const int32_t *__rest
     if ((++it & 3u) == 0 && (*(volatile uint32_t *)&status->err & kErrTableFull)) break;  // as in k_count_flat
     int32_t v[K + 1];
     if (aligned && p0 + K < n) {
-      const int4 a = *reinterpret_cast<const int4 *>(s + p0);
+      // evict-first: the steps are read once here, and L2 is better left to
+      // the table
+      const int4 a = __ldcs(reinterpret_cast<const int4 *>(s + p0));
       v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
       v[4] = s[p0 + K];
     } else {
@@ -855,8 +858,10 @@ __global__ void __launch_bounds__(BLOCK) k_apply_classify_sref(const uint32_t *_
   const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
   uint32_t ref[ITEMS];
   if (p0 + ITEMS <= n && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
-    const uint4 a = *reinterpret_cast<const uint4 *>(sref + p0);
-    const uint4 b = *reinterpret_cast<const uint4 *>(sref + p0 + 4);
+    // evict-first (the emit's reads of steps and references alike): L2 is
+    // better left to the bitmaps and the emit's output
+    const uint4 a = __ldcs(reinterpret_cast<const uint4 *>(sref + p0));
+    const uint4 b = __ldcs(reinterpret_cast<const uint4 *>(sref + p0 + 4));
     ref[0] = a.x; ref[1] = a.y; ref[2] = a.z; ref[3] = a.w;
     ref[4] = b.x; ref[5] = b.y; ref[6] = b.z; ref[7] = b.w;
   } else {
@@ -1168,10 +1173,10 @@ __global__ void __launch_bounds__(BLOCK, 6) k_apply_emit_sref(const int32_t *__r
   int32_t v[ITEMS + 1];
   uint32_t ref[ITEMS];
   if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0 && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
-    const int4 a = *reinterpret_cast<const int4 *>(s + p0);
-    const int4 b = *reinterpret_cast<const int4 *>(s + p0 + 4);
-    const uint4 ra = *reinterpret_cast<const uint4 *>(sref + p0);
-    const uint4 rb = *reinterpret_cast<const uint4 *>(sref + p0 + 4);
+    const int4 a = __ldcs(reinterpret_cast<const int4 *>(s + p0));
+    const int4 b = __ldcs(reinterpret_cast<const int4 *>(s + p0 + 4));
+    const uint4 ra = __ldcs(reinterpret_cast<const uint4 *>(sref + p0));
+    const uint4 rb = __ldcs(reinterpret_cast<const uint4 *>(sref + p0 + 4));
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
     v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
     v[8] = s[p0 + ITEMS];
