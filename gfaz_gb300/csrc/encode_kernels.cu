@@ -1353,11 +1353,23 @@ __global__ void __launch_bounds__(kBlock) k_sort_pass(const unsigned long long *
     st_desc(&desc[d], kDescIncl | cnt_d);
   } else {
     st_desc(&desc[tile * 256 + d], kDescAgg | cnt_d);
-    for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
-      unsigned long long v = ld_desc(&desc[(uint64_t)j * 256 + d]);
-      if ((v & kDescMask) == 0) v = wait_desc(desc + d, (uint64_t)j * 256, err);
-      excl += v & kDescPayload;
-      if ((v & kDescMask) == kDescIncl) break;
+    // the predecessors' descriptors kSortWindow at a time, all loads in
+    // flight together, summed in order down to the first inclusive one
+    // (tile -1 counts as an inclusive zero)
+    constexpr int kSortWindow = 8;
+    bool found = false;
+    for (int64_t j = (int64_t)tile - 1; !found; j -= kSortWindow) {
+      unsigned long long v[kSortWindow];
+#pragma unroll
+      for (int i = 0; i < kSortWindow; ++i) v[i] = j - i >= 0 ? ld_desc(&desc[(uint64_t)(j - i) * 256 + d]) : kDescIncl;
+#pragma unroll
+      for (int i = 0; i < kSortWindow; ++i) {
+        if (found) break;
+        unsigned long long x = v[i];
+        if ((x & kDescMask) == 0) x = wait_desc(desc + d, (uint64_t)(j - i) * 256, err);
+        excl += x & kDescPayload;
+        found = (x & kDescMask) == kDescIncl;
+      }
     }
     st_desc(&desc[tile * 256 + d], kDescIncl | (excl + cnt_d));
   }
