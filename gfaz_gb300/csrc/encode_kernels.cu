@@ -858,8 +858,8 @@ __global__ void __launch_bounds__(BLOCK) k_apply_classify_sref(const uint32_t *_
   const uint64_t p0 = tile * TILE + (uint64_t)threadIdx.x * ITEMS;
   uint32_t ref[ITEMS];
   if (p0 + ITEMS <= n && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
-    // evict-first (the emit's reads of steps and references alike): L2 is
-    // better left to the bitmaps and the emit's output
+    // evict-first: the references stream through once per pass, and L2 is
+    // better left to the repeated-slot bitmap
     const uint4 a = __ldcs(reinterpret_cast<const uint4 *>(sref + p0));
     const uint4 b = __ldcs(reinterpret_cast<const uint4 *>(sref + p0 + 4));
     ref[0] = a.x; ref[1] = a.y; ref[2] = a.z; ref[3] = a.w;
@@ -1173,6 +1173,7 @@ __global__ void __launch_bounds__(BLOCK, 6) k_apply_emit_sref(const int32_t *__r
   int32_t v[ITEMS + 1];
   uint32_t ref[ITEMS];
   if (p0 + ITEMS < n && (reinterpret_cast<uintptr_t>(s) & 15u) == 0 && (reinterpret_cast<uintptr_t>(sref) & 15u) == 0) {
+    // evict-first, as in the classification: L2 keeps the used-slot bitmap
     const int4 a = __ldcs(reinterpret_cast<const int4 *>(s + p0));
     const int4 b = __ldcs(reinterpret_cast<const int4 *>(s + p0 + 4));
     const uint4 ra = __ldcs(reinterpret_cast<const uint4 *>(sref + p0));
